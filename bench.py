@@ -1,0 +1,370 @@
+#!/usr/bin/env python3
+"""Steps/s of the channel-flow time step on GB300.
+
+Workload: turbulent channel at Re_tau = 180, grid 128 x 129 x 128
+(nnx = 128 streamwise, nnz = 128 -> 129 wall-normal Chebyshev points,
+nny = 128 spanwise), box 4 pi x 2 x 4 pi / 3, dt = 5e-4, started from the
+laminar profile plus seeded noise.  One "step" is one iteration of the
+reference main loop: getnonlinear followed by the per-mode and (0,0)-mode
+solves.  Synthetic, seeded initial data; no dataset is involved.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64]
+    python bench.py --impl reference     # the reference algorithm on the host CPU
+
+Under torchrun (N > 1) every rank advances its own independent channel
+(replicas; the reference's decomposition of one channel needs an all-to-all
+per transform, so one channel stays on one GPU); value = all steps / max time.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FP64_PEAK_TFLOPS = 1.199  # measured FP64 FMA throughput of this machine's GB300 (profiles/fp64_peak_probe.md)
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    p.add_argument("--config", default="c3_retau180_128")
+    p.add_argument("--zpad", type=int, default=0)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_name(cfg, precision, zpad):
+    return (f"Re_tau180 channel {cfg.nnx}x{cfg.nnz + 1}x{cfg.nny} (nnx x wall-normal x nny), "
+            f"box {2 * cfg.aphi:g}pi x 2 x {2 * cfg.beta:.4g}pi, dt={cfg.dt:g}, re={cfg.re:g}, "
+            f"re_p={cfg.re_p:g}, {precision} path, product grid {zpad or 2 * cfg.nnz} intervals")
+
+
+# --------------------------------------------------------------------------
+# algorithmic work per kernel launch (bytes read + written once, FP64 flops)
+# --------------------------------------------------------------------------
+def kernel_work(cfg, zpad=0):
+    N = cfg.nnz
+    NZ = N + 1
+    KX, KY = cfg.nnx // 2, cfg.nny
+    PX, PY = 3 * cfg.nnx // 2, 3 * cfg.nny // 2
+    MZ = zpad or 2 * N
+    MP = MZ + 1
+    modes = KX * KY
+    c = 16  # complex FP64
+
+    def fft_flops(n):
+        return 5.0 * n * math.log2(n)
+
+    w = {}
+    w["k_zc2v"] = (6 * NZ * modes * c + 6 * MP * modes * c, 6 * modes * fft_flops(2 * MZ))
+    w["k_yinv"] = (6 * MP * modes * c + 6 * MP * PY * KX * c, 6 * MP * KX * fft_flops(PY))
+    w["k_xprod"] = (6 * MP * PY * KX * c + 3 * MP * PY * KX * c,
+                    MP * PY * (5 * fft_flops(PX) + 9 * PX))
+    w["k_yfwd"] = (3 * MP * PY * KX * c + 3 * MP * modes * c, 3 * MP * KX * fft_flops(PY))
+    w["k_zcurl"] = (3 * MP * modes * c + 4 * NZ * modes * c,
+                    modes * (3 * fft_flops(2 * MZ) + 2 * fft_flops(2 * N)))
+    ne, no = N // 2 + 1, N // 2
+    stride = 2 * (ne * ne + no * no)
+    # distinct k^2 values decide the matrix bytes
+    import numpy as np
+    from channel_flow_gb300.fields import wavenumbers
+    ia, ib = wavenumbers(cfg)
+    k2 = (ia[None, :] ** 2 + ib[:, None] ** 2)
+    k2[KY // 2, :] = 0.0
+    nk2 = len(np.unique(k2[k2 != 0.0]))
+    nsolve = int((k2 != 0.0).sum())
+    w["k_solve"] = ((nk2 + 1) * stride * 8 + 12 * NZ * modes * c,
+                    nsolve * (8 * (ne * ne + no * no) + 2 * fft_flops(2 * N)))
+    return w
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.idx = device_index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+# --------------------------------------------------------------------------
+# CPU baseline / reference arm: the reference algorithm restated on the host
+# --------------------------------------------------------------------------
+def cpu_reference_rate(cfg, seconds, warmup=1, steps=None):
+    import oracle
+    from channel_flow_gb300 import fields
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    o = oracle.Oracle.from_config(cfg)
+    o.setup()
+    o.set_state(fields.reference_like_state(cfg, seed=0))
+    o.getnonlinear()
+    o.solve()
+    for _ in range(warmup):
+        o.step(1)
+    if steps is None:
+        t = time.perf_counter()
+        o.step(1)
+        one = time.perf_counter() - t
+        steps = max(1, int(seconds / max(one, 1e-6)))
+    t = time.perf_counter()
+    o.step(steps)
+    el = time.perf_counter() - t
+    return steps / el, threads, steps, el
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from channel_flow_gb300 import config
+    cfg = config.CONFIGS[args.config]
+    rate, threads, steps, el = cpu_reference_rate(cfg, 0, warmup=args.warmup, steps=args.steps)
+    sample = (f"{steps} full time steps of the {cfg.nnx}x{cfg.nnz + 1}x{cfg.nny} workload "
+              f"(CPU restatement of the reference algorithm, 12+6 padded transforms, explicit inverses)")
+    line = {
+        "impl": "reference", "metric": "steps/s", "value": rate, "unit": "steps/s",
+        "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 / rate,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded laminar + noise)",
+        "config": {"workload": workload_name(cfg, "fp64", 0), "grid_points": cfg.points},
+        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import numpy as np
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from channel_flow_gb300 import Channel, build as cbuild, config, fields
+    if rank == 0:
+        cbuild.build()
+    if dist:
+        dist.barrier()
+    cfg = config.CONFIGS[args.config]
+    st = fields.reference_like_state(cfg, seed=rank)
+    ch = Channel(cfg, precision=args.precision, zpad=args.zpad, device=local)
+    stream = torch.cuda.Stream(device=local)
+    ch.set_stream(stream.cuda_stream)
+    ch.upload_state(st)
+    ch.getnonlinear()
+    ch.solve()
+    ch.step(max(3, args.warmup))
+    ch.synchronize()
+    # ---- timed region (device events on the library's stream)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ch.profile(True)
+    ch.profile_reset()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ch.step(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    prof = ch.profile_report()
+    ch.profile(False)
+    clk = clocks.stop()
+    diag = ch.diagnostics()
+    t_max = ms
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * args.steps / (t_max / 1e3)
+    # ---- end to end through the C ABI with pinned host buffers: every step
+    # uploads the module arrays, advances one step and downloads them
+    host = {}
+    for k, a in st.items():
+        pt = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        host[k] = pt.numpy()
+        host[k][...] = a
+    ch.set_stream(None)
+    ch.upload_state(host)
+    ch.getnonlinear()
+    ch.solve()
+    h2d = sum(a.nbytes for a in host.values())
+    ne2e = max(1, args.e2e_steps)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ne2e):
+        ch.upload_state(host)
+        ch.step(1)
+        out = ch.download_state()
+    el = time.perf_counter() - t0
+    e2e_t = el
+    if dist:
+        t = torch.tensor([el], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e = {"value": world * ne2e / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": sum(a.nbytes for a in out.values()),
+           "what": "chf_upload_state (all module arrays, pinned host) + chf_step(1) + chf_download_state"}
+    ch.close()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    # ---- roofline of the dominant kernel
+    work = kernel_work(cfg, args.zpad)
+    kname = max((k for k in prof if prof[k][0] > 0), key=lambda k: prof[k][1])
+    launches, kms = prof[kname]
+    avg_ms = kms / launches
+    nbytes, nflops = work.get(kname, (0, 0))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved_gbs = nbytes / (avg_ms / 1e3) / 1e9
+    traffic = read_traffic(kname)
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved_gbs, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback",
+                "traffic": traffic, "algorithmic_bytes": nbytes, "avg_launch_ms": avg_ms,
+                "fp64_tflops_achieved": nflops / (avg_ms / 1e3) / 1e12,
+                "fp64_tflops_peak": FP64_PEAK_TFLOPS,
+                "fp64_frac": nflops / (avg_ms / 1e3) / 1e12 / FP64_PEAK_TFLOPS}
+    kernels = {k: {"launches": v[0], "ms_total": v[1], "share": v[1] / max(1e-9, sum(x[1] for x in prof.values()))}
+               for k, v in prof.items() if v[0] > 0}
+    line = {
+        "metric": "steps/s", "value": value, "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+bf16x2 transforms, f64 solves",
+        "data": "synthetic (seeded laminar + noise)",
+        "config": {"workload": workload_name(cfg, args.precision, args.zpad),
+                   "grid_points": cfg.points, "precision": args.precision,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2: >0.9 GB touched per step vs 129 MB L2"},
+        "grid_point_steps_per_s": value * cfg.points,
+        "gpu_launches": ch_kernels(args.steps, prof),
+        "clocks": clk,
+        "e2e": e2e,
+        "roofline": roofline,
+        "kernels": kernels,
+        "energy_after": diag["energy"],
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        rate, threads, steps, el = cpu_reference_rate(cfg, args.cpu_seconds)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} full time steps ({el:.1f} s) of the same workload, CPU restatement "
+                      f"of the reference algorithm (oracle/), OpenMP over {threads} host threads"}
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def ch_kernels(steps, prof):
+    return int(sum(v[0] for v in prof.values()))
+
+
+def read_traffic(kname):
+    """DRAM bytes per launch of kname from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kname:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,206 @@
+"""ctypes binding of include/chflow.h and the Channel class.
+
+Status codes and error strings come straight from the library; a non-zero
+status raises ChannelError carrying chf_last_error().
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .config import ChannelConfig
+from .fields import FIELD_NAMES, MEAN_NAMES
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libchflow.so")
+
+PRECISION = {"fp64": 0, "mixed": 1}
+STATUS = {0: "CHF_OK", -1: "CHF_E_INVALID", -2: "CHF_E_CUDA", -3: "CHF_E_NOMEM",
+          -4: "CHF_E_STATE", -5: "CHF_E_NUMERIC"}
+
+# Every entry point declared in include/chflow.h.
+EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
+           "chf_download_state", "chf_getnonlinear", "chf_solve", "chf_step",
+           "chf_synchronize", "chf_diagnostics", "chf_kernels_per_step", "chf_device_field",
+           "chf_set_stream", "chf_profile_enable", "chf_profile_reset", "chf_profile_read")
+
+
+class ChannelError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class CConfig(ctypes.Structure):
+    _fields_ = [("nnx", ctypes.c_int), ("nny", ctypes.c_int), ("nnz", ctypes.c_int),
+                ("aphi", ctypes.c_double), ("beta", ctypes.c_double), ("dt", ctypes.c_double),
+                ("re", ctypes.c_double), ("re_p", ctypes.c_double), ("precision", ctypes.c_int),
+                ("zpad", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class CDiag(ctypes.Structure):
+    _fields_ = [("energy", ctypes.c_double), ("wall_shear_top", ctypes.c_double),
+                ("wall_shear_bottom", ctypes.c_double), ("max_abs", ctypes.c_double),
+                ("finite", ctypes.c_int)]
+
+
+_lib = None
+
+
+def load_library(path: str = None):
+    """Load libchflow.so (build it with channel_flow_gb300.build.build())."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ChannelError(-2, f"CUDA library not found at {p}; run channel_flow_gb300.build.build()")
+    L = ctypes.CDLL(p)
+    dp = ctypes.POINTER(ctypes.c_double)
+    vp = ctypes.c_void_p
+    L.chf_create.argtypes = [ctypes.POINTER(CConfig), ctypes.POINTER(vp)]
+    L.chf_destroy.argtypes = [vp]
+    L.chf_last_error.argtypes = [vp]
+    L.chf_last_error.restype = ctypes.c_char_p
+    L.chf_upload_state.argtypes = [vp] + [dp] * 14
+    L.chf_download_state.argtypes = [vp] + [dp] * 14
+    for name in ("chf_getnonlinear", "chf_solve", "chf_synchronize"):
+        getattr(L, name).argtypes = [vp]
+    L.chf_step.argtypes = [vp, ctypes.c_int]
+    L.chf_diagnostics.argtypes = [vp, ctypes.POINTER(CDiag)]
+    L.chf_kernels_per_step.argtypes = [vp]
+    L.chf_device_field.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp)]
+    L.chf_set_stream.argtypes = [vp, vp]
+    L.chf_profile_enable.argtypes = [vp, ctypes.c_int]
+    L.chf_profile_reset.argtypes = [vp]
+    L.chf_profile_read.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    for name in EXPORTS:
+        getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
+    L.chf_last_error.restype = ctypes.c_char_p
+    if path is None:
+        _lib = L
+    return L
+
+
+def _dptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_cconfig(cfg: ChannelConfig, precision="fp64", zpad=0, device=0) -> CConfig:
+    return CConfig(cfg.nnx, cfg.nny, cfg.nnz, cfg.aphi, cfg.beta, cfg.dt, cfg.re, cfg.re_p,
+                   PRECISION[precision] if isinstance(precision, str) else int(precision),
+                   int(zpad), int(device))
+
+
+class Channel:
+    """One channel resident on one GPU (a chf_handle)."""
+
+    def __init__(self, cfg: ChannelConfig, precision="fp64", zpad=0, device=0):
+        self.L = load_library()
+        self.cfg = cfg
+        self.shape = (cfg.nnz + 1, cfg.nny, cfg.nnx)
+        self.h = ctypes.c_void_p()
+        c = make_cconfig(cfg, precision, zpad, device)
+        rc = self.L.chf_create(ctypes.byref(c), ctypes.byref(self.h))
+        if rc != 0:
+            raise ChannelError(rc, self.L.chf_last_error(None).decode())
+
+    def _check(self, rc):
+        if rc != 0:
+            raise ChannelError(rc, self.L.chf_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.chf_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload_state(self, st: dict):
+        arrs = []
+        for k in FIELD_NAMES:
+            a = st.get(k)
+            if a is not None:
+                a = np.ascontiguousarray(a, dtype=np.float64)
+                if a.shape != self.shape:
+                    raise ChannelError(-1, f"{k}: shape {a.shape} != {self.shape}")
+            arrs.append(a)
+        for k in MEAN_NAMES:
+            a = st.get(k)
+            if a is not None:
+                a = np.ascontiguousarray(a, dtype=np.float64)
+                if a.shape != (self.cfg.nnz + 1, 2):
+                    raise ChannelError(-1, f"{k}: shape {a.shape} != {(self.cfg.nnz + 1, 2)}")
+            arrs.append(a)
+        self._check(self.L.chf_upload_state(self.h, *[_dptr(a) for a in arrs]))
+
+    def download_state(self) -> dict:
+        out = {k: np.empty(self.shape) for k in FIELD_NAMES}
+        out.update({k: np.empty((self.cfg.nnz + 1, 2)) for k in MEAN_NAMES})
+        self._check(self.L.chf_download_state(
+            self.h, *[_dptr(out[k]) for k in FIELD_NAMES], *[_dptr(out[k]) for k in MEAN_NAMES]))
+        return out
+
+    def getnonlinear(self):
+        self._check(self.L.chf_getnonlinear(self.h))
+
+    def solve(self):
+        self._check(self.L.chf_solve(self.h))
+
+    def step(self, n=1):
+        self._check(self.L.chf_step(self.h, int(n)))
+
+    def synchronize(self):
+        self._check(self.L.chf_synchronize(self.h))
+
+    def diagnostics(self) -> dict:
+        d = CDiag()
+        rc = self.L.chf_diagnostics(self.h, ctypes.byref(d))
+        if rc not in (0, -5):
+            self._check(rc)
+        return {"energy": d.energy, "wall_shear_top": d.wall_shear_top,
+                "wall_shear_bottom": d.wall_shear_bottom, "max_abs": d.max_abs,
+                "finite": bool(d.finite)}
+
+    def kernels_per_step(self) -> int:
+        return int(self.L.chf_kernels_per_step(self.h))
+
+    def set_stream(self, stream_ptr):
+        """Run on a caller CUDA stream (an integer cudaStream_t, e.g.
+        torch.cuda.Stream().cuda_stream); None restores the own stream."""
+        self._check(self.L.chf_set_stream(self.h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def profile(self, on=True):
+        self._check(self.L.chf_profile_enable(self.h, int(bool(on))))
+
+    def profile_reset(self):
+        self._check(self.L.chf_profile_reset(self.h))
+
+    def profile_report(self) -> dict:
+        """{kernel name: (launches, total device ms)} since the last reset."""
+        out = {}
+        i = 0
+        while True:
+            name = ctypes.c_char_p()
+            n = ctypes.c_int()
+            ms = ctypes.c_double()
+            rc = self.L.chf_profile_read(self.h, i, ctypes.byref(name), ctypes.byref(n), ctypes.byref(ms))
+            if rc != 0:
+                break
+            out[name.value.decode()] = (n.value, ms.value)
+            i += 1
+        return out

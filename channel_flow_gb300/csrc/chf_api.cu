@@ -1,0 +1,382 @@
+// chf_api.cu -- the C ABI declared in include/chflow.h.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "chf_internal.h"
+
+namespace chf {
+
+bool cuda_ok(Handle* h, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  if (h) h->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return false;
+}
+
+FftPlan make_plan(int L) {
+  FftPlan p{};
+  p.L = L;
+  int m = L, Ns = 1;
+  while (m > 1) {
+    int r = (m % 4 == 0) ? 4 : (m % 2 == 0) ? 2 : (m % 3 == 0) ? 3 : 5;
+    p.R[p.nst] = r;
+    p.Ns[p.nst] = Ns;
+    ++p.nst;
+    Ns *= r;
+    m /= r;
+  }
+  return p;
+}
+
+static bool factors_235(int n) {
+  if (n <= 0) return false;
+  for (int p : {2, 3, 5})
+    while (n % p == 0) n /= p;
+  return n == 1;
+}
+
+static std::vector<cd> twiddles(int L) {
+  std::vector<cd> t(L);
+  const double twopi = 8.0 * std::atan(1.0);
+  for (int k = 0; k < L; ++k) {
+    double a = -twopi * (double)k / (double)L;
+    t[k] = cd{std::cos(a), std::sin(a)};
+  }
+  return t;
+}
+
+const char* const kKernelNames[K_COUNT] = {"k_zc2v", "k_yinv", "k_xprod", "k_yfwd",
+                                           "k_zcurl", "k_solve", "k_diag"};
+
+static cudaEvent_t take_event(Handle* h) {
+  if (!h->event_pool.empty()) {
+    cudaEvent_t e = h->event_pool.back();
+    h->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void prof_begin(Handle* h, int kid, cudaEvent_t* a) {
+  (void)kid;
+  *a = nullptr;
+  if (!h->profiling) return;
+  *a = take_event(h);
+  cudaEventRecord(*a, h->stream);
+}
+
+void prof_end(Handle* h, int kid, cudaEvent_t a) {
+  if (!h->profiling || !a) return;
+  cudaEvent_t b = take_event(h);
+  cudaEventRecord(b, h->stream);
+  h->pending.push_back({kid, a, b});
+}
+
+static void prof_collect(Handle* h) {
+  if (h->pending.empty()) return;
+  cudaStreamSynchronize(h->stream);
+  for (auto& p : h->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    h->prof[p.kid].launches += 1;
+    h->prof[p.kid].ms += ms;
+    h->event_pool.push_back(p.a);
+    h->event_pool.push_back(p.b);
+  }
+  h->pending.clear();
+}
+
+}  // namespace chf
+
+using namespace chf;
+
+struct chf_handle : public Handle {};
+
+static thread_local std::string g_create_error;
+
+static std::string validate(const chf_config* c) {
+  if (!c) return "config is NULL";
+  if (c->nnx < 4 || c->nnx % 4) return "nnx must be a positive multiple of 4";
+  if (c->nny < 4 || c->nny % 4) return "nny must be a positive multiple of 4";
+  if (c->nnz < 4 || c->nnz % 2) return "nnz must be even and >= 4";
+  if (c->nnz > 382) return "nnz must be <= 382";
+  if (!(c->aphi > 0) || !(c->beta > 0)) return "aphi and beta must be positive";
+  if (!(c->dt > 0) || !(c->re > 0)) return "dt and re must be positive";
+  if (!std::isfinite(c->re_p)) return "re_p must be finite";
+  if (c->precision != CHF_FP64 && c->precision != CHF_MIXED) return "precision must be CHF_FP64 or CHF_MIXED";
+  int mz = c->zpad == 0 ? 2 * c->nnz : c->zpad;
+  if (2 * mz <= 3 * c->nnz) return "zpad must satisfy 2*zpad > 3*nnz (exact dealiasing)";
+  if (!factors_235(3 * c->nnx / 2) || !factors_235(3 * c->nny / 2) || !factors_235(2 * mz) ||
+      !factors_235(2 * c->nnz))
+    return "transform lengths 3nnx/2, 3nny/2, 2nnz and 2zpad must factor into 2, 3 and 5";
+  return "";
+}
+
+static void release(chf_handle* h) {
+  if (!h) return;
+  if (h->device >= 0) cudaSetDevice(h->device);
+  for (auto& p : h->f) cudaFree(p);
+  for (auto& p : h->mean) cudaFree(p);
+  void* ptrs[] = {h->iapha, h->ibeta, h->t0, h->t2, h->t4, h->k2vals, h->xinv, h->xmean,
+                  h->group_start, h->group_modes, h->tw_py, h->tw_px, h->tw_z2, h->tw_zm,
+                  h->twf_py, h->twf_px, h->wz, h->wy, h->scratch};
+  for (void* p : ptrs) cudaFree(p);
+  for (auto& p : h->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : h->event_pool) cudaEventDestroy(e);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+extern "C" {
+
+int chf_create(const chf_config* cfg, chf_handle** out) {
+  if (!out) {
+    g_create_error = "out is NULL";
+    return CHF_E_INVALID;
+  }
+  *out = nullptr;
+  std::string why = validate(cfg);
+  if (!why.empty()) {
+    g_create_error = why;
+    return CHF_E_INVALID;
+  }
+  if (cfg->precision == CHF_MIXED) {
+    g_create_error = "CHF_MIXED is not available in this build";
+    return CHF_E_INVALID;
+  }
+  chf_handle* h = new (std::nothrow) chf_handle();
+  if (!h) {
+    g_create_error = "host allocation failed";
+    return CHF_E_NOMEM;
+  }
+  h->cfg = *cfg;
+  h->device = cfg->device;
+  Dims& d = h->d;
+  d.nnx = cfg->nnx;
+  d.nny = cfg->nny;
+  d.nnz = cfg->nnz;
+  d.N = cfg->nnz;
+  d.NZ = cfg->nnz + 1;
+  d.KX = cfg->nnx / 2;
+  d.KY = cfg->nny;
+  d.NYQ = cfg->nny / 2;
+  d.PX = 3 * cfg->nnx / 2;
+  d.PY = 3 * cfg->nny / 2;
+  d.MZ = cfg->zpad == 0 ? 2 * cfg->nnz : cfg->zpad;
+  d.MP = d.MZ + 1;
+  auto fail = [&](int code) {
+    g_create_error = h->err.empty() ? "chf_create failed" : h->err;
+    release(h);
+    delete h;
+    return code;
+  };
+  int ndev = 0;
+  if (!cuda_ok(h, cudaGetDeviceCount(&ndev), "cudaGetDeviceCount")) return fail(CHF_E_CUDA);
+  if (cfg->device < 0 || cfg->device >= ndev) {
+    h->err = "device ordinal out of range";
+    h->device = -1;
+    return fail(CHF_E_INVALID);
+  }
+  if (!cuda_ok(h, cudaSetDevice(cfg->device), "cudaSetDevice") ||
+      !cuda_ok(h, cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "cudaStreamCreate"))
+    return fail(CHF_E_CUDA);
+  h->stream = h->own_stream;
+  h->prof.resize(K_COUNT);
+  for (int k = 0; k < K_COUNT; ++k) h->prof[k] = {kKernelNames[k], 0, 0.0};
+  const size_t fe = d.field_elems();
+  for (int i = 0; i < F_COUNT; ++i) {
+    if (!cuda_ok(h, cudaMalloc((void**)&h->f[i], sizeof(cd) * fe), "state alloc")) return fail(CHF_E_NOMEM);
+    cudaMemsetAsync(h->f[i], 0, sizeof(cd) * fe, h->stream);
+  }
+  for (int i = 0; i < M_COUNT; ++i) {
+    if (!cuda_ok(h, cudaMalloc((void**)&h->mean[i], sizeof(double) * 2 * d.NZ), "mean alloc"))
+      return fail(CHF_E_NOMEM);
+    cudaMemsetAsync(h->mean[i], 0, sizeof(double) * 2 * d.NZ, h->stream);
+  }
+  const size_t wz_elems = (size_t)6 * d.MP * d.modes();
+  const size_t wy_elems = (size_t)6 * d.MP * d.PY * d.KX;
+  if (!cuda_ok(h, cudaMalloc((void**)&h->wz, sizeof(cd) * wz_elems), "work alloc") ||
+      !cuda_ok(h, cudaMalloc((void**)&h->wy, sizeof(cd) * wy_elems), "work alloc"))
+    return fail(CHF_E_NOMEM);
+  h->scratch_bytes = 4096;
+  if (!cuda_ok(h, cudaMalloc(&h->scratch, h->scratch_bytes), "scratch alloc")) return fail(CHF_E_NOMEM);
+  h->py = make_plan(d.PY);
+  h->px = make_plan(d.PX);
+  h->pz2 = make_plan(2 * d.N);
+  h->pzm = make_plan(2 * d.MZ);
+  struct {
+    cd** dst;
+    int L;
+  } tws[] = {{&h->tw_py, d.PY}, {&h->tw_px, d.PX}, {&h->tw_z2, 2 * d.N}, {&h->tw_zm, 2 * d.MZ}};
+  for (auto& t : tws) {
+    std::vector<cd> v = twiddles(t.L);
+    if (!cuda_ok(h, cudaMalloc((void**)t.dst, sizeof(cd) * v.size()), "twiddle alloc") ||
+        !cuda_ok(h, cudaMemcpy(*t.dst, v.data(), sizeof(cd) * v.size(), cudaMemcpyHostToDevice),
+                 "twiddle upload"))
+      return fail(CHF_E_CUDA);
+  }
+  int rc = setup_solver(h);
+  if (rc != CHF_OK) return fail(rc);
+  h->kernels_per_step = 6;
+  if (!cuda_ok(h, cudaStreamSynchronize(h->stream), "create sync")) return fail(CHF_E_CUDA);
+  *out = h;
+  return CHF_OK;
+}
+
+int chf_destroy(chf_handle* h) {
+  if (!h) return CHF_E_INVALID;
+  release(h);
+  delete h;
+  return CHF_OK;
+}
+
+const char* chf_last_error(const chf_handle* h) {
+  if (!h) return g_create_error.c_str();
+  return h->err.c_str();
+}
+
+static int transfer(chf_handle* h, bool up, double* const* fields, double* const* means) {
+  if (!h) return CHF_E_INVALID;
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
+  const size_t fb = sizeof(cd) * h->d.field_elems();
+  const size_t mb = sizeof(double) * 2 * h->d.NZ;
+  for (int i = 0; i < F_COUNT; ++i) {
+    if (!fields[i]) continue;
+    cudaError_t e = up ? cudaMemcpyAsync(h->f[i], fields[i], fb, cudaMemcpyHostToDevice, h->stream)
+                       : cudaMemcpyAsync(fields[i], h->f[i], fb, cudaMemcpyDeviceToHost, h->stream);
+    if (!cuda_ok(h, e, up ? "upload" : "download")) return CHF_E_CUDA;
+  }
+  for (int i = 0; i < M_COUNT; ++i) {
+    if (!means[i]) continue;
+    cudaError_t e = up ? cudaMemcpyAsync(h->mean[i], means[i], mb, cudaMemcpyHostToDevice, h->stream)
+                       : cudaMemcpyAsync(means[i], h->mean[i], mb, cudaMemcpyDeviceToHost, h->stream);
+    if (!cuda_ok(h, e, up ? "upload" : "download")) return CHF_E_CUDA;
+  }
+  if (!cuda_ok(h, cudaStreamSynchronize(h->stream), up ? "upload sync" : "download sync"))
+    return CHF_E_CUDA;
+  if (up) h->uploaded = true;
+  return CHF_OK;
+}
+
+int chf_upload_state(chf_handle* h, const double* vnp1, const double* omegaynp1, const double* unp1,
+                     const double* wnp1, const double* omegaxnp1, const double* omegaznp1,
+                     const double* rhsvn, const double* rhsomegayn, const double* clamb1n,
+                     const double* clamb1nm1, const double* clamb3n, const double* clamb3nm1,
+                     const double* au0, const double* w0) {
+  double* f[F_COUNT] = {(double*)vnp1, (double*)omegaynp1, (double*)unp1, (double*)wnp1,
+                        (double*)omegaxnp1, (double*)omegaznp1, (double*)rhsvn, (double*)rhsomegayn};
+  double* m[M_COUNT] = {(double*)clamb1n, (double*)clamb1nm1, (double*)clamb3n,
+                        (double*)clamb3nm1, (double*)au0, (double*)w0};
+  return transfer(h, true, f, m);
+}
+
+int chf_download_state(chf_handle* h, double* vnp1, double* omegaynp1, double* unp1, double* wnp1,
+                       double* omegaxnp1, double* omegaznp1, double* rhsvn, double* rhsomegayn,
+                       double* clamb1n, double* clamb1nm1, double* clamb3n, double* clamb3nm1,
+                       double* au0, double* w0) {
+  double* f[F_COUNT] = {vnp1, omegaynp1, unp1, wnp1, omegaxnp1, omegaznp1, rhsvn, rhsomegayn};
+  double* m[M_COUNT] = {clamb1n, clamb1nm1, clamb3n, clamb3nm1, au0, w0};
+  return transfer(h, false, f, m);
+}
+
+int chf_getnonlinear(chf_handle* h) {
+  if (!h) return CHF_E_INVALID;
+  if (!h->uploaded) {
+    h->err = "chf_getnonlinear before chf_upload_state";
+    return CHF_E_STATE;
+  }
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
+  return launch_nonlinear_fp64(h);
+}
+
+int chf_solve(chf_handle* h) {
+  if (!h) return CHF_E_INVALID;
+  if (!h->uploaded) {
+    h->err = "chf_solve before chf_upload_state";
+    return CHF_E_STATE;
+  }
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
+  return launch_solve_fp64(h);
+}
+
+int chf_step(chf_handle* h, int nsteps) {
+  if (!h) return CHF_E_INVALID;
+  if (nsteps < 0) {
+    h->err = "nsteps must be >= 0";
+    return CHF_E_INVALID;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    int rc = chf_getnonlinear(h);
+    if (rc != CHF_OK) return rc;
+    rc = chf_solve(h);
+    if (rc != CHF_OK) return rc;
+  }
+  return CHF_OK;
+}
+
+int chf_synchronize(chf_handle* h) {
+  if (!h) return CHF_E_INVALID;
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice") ||
+      !cuda_ok(h, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))
+    return CHF_E_CUDA;
+  return CHF_OK;
+}
+
+int chf_diagnostics(chf_handle* h, chf_diag* out) {
+  if (!h || !out) return CHF_E_INVALID;
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
+  int rc = launch_diagnostics(h, out);
+  if (rc == CHF_E_NUMERIC) h->err = "non-finite values in the state";
+  return rc;
+}
+
+int chf_kernels_per_step(const chf_handle* h) { return h ? h->kernels_per_step : 0; }
+
+int chf_set_stream(chf_handle* h, void* stream) {
+  if (!h) return CHF_E_INVALID;
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
+  // order the switch: work already queued on the old stream completes first
+  if (!cuda_ok(h, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize")) return CHF_E_CUDA;
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return CHF_OK;
+}
+
+int chf_profile_enable(chf_handle* h, int on) {
+  if (!h) return CHF_E_INVALID;
+  prof_collect(h);
+  h->profiling = on != 0;
+  return CHF_OK;
+}
+
+int chf_profile_reset(chf_handle* h) {
+  if (!h) return CHF_E_INVALID;
+  prof_collect(h);
+  for (auto& r : h->prof) {
+    r.launches = 0;
+    r.ms = 0.0;
+  }
+  return CHF_OK;
+}
+
+int chf_profile_read(chf_handle* h, int idx, const char** name, int* launches, double* total_ms) {
+  if (!h || idx < 0 || idx >= (int)h->prof.size()) return CHF_E_INVALID;
+  prof_collect(h);
+  if (name) *name = h->prof[idx].name;
+  if (launches) *launches = h->prof[idx].launches;
+  if (total_ms) *total_ms = h->prof[idx].ms;
+  return CHF_OK;
+}
+
+int chf_device_field(chf_handle* h, int which, void** dptr) {
+  if (!h || !dptr || which < 0 || which >= F_COUNT) return CHF_E_INVALID;
+  *dptr = h->f[which];
+  return CHF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,119 @@
+// chf_internal.h -- handle layout, device buffers and kernel launchers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/chflow.h"
+#include "fft_dev.cuh"
+
+namespace chf {
+
+using cd = cplx<double>;
+using cf = cplx<float>;
+
+// Field slots of the resident state (the paraandcons.f90:28-38 arrays).
+enum Field { F_V = 0, F_OY, F_U, F_W, F_OX, F_OZ, F_RV, F_RG, F_COUNT };
+enum Mean { M_CL1N = 0, M_CL1NM1, M_CL3N, M_CL3NM1, M_AU0, M_W0, M_COUNT };
+
+struct Dims {
+  int nnx, nny, nnz;
+  int N;    // Chebyshev degree (= nnz)
+  int NZ;   // N + 1 coefficients / Gauss-Lobatto points
+  int KX;   // streamwise complex modes kept = nnx/2
+  int KY;   // spanwise complex modes = nny (slot NYQ unused)
+  int NYQ;  // spanwise Nyquist slot = nny/2
+  int PX;   // padded streamwise points = 3 nnx / 2
+  int PY;   // padded spanwise points = 3 nny / 2
+  int MZ;   // product-grid intervals in z (2 nnz in the reference)
+  int MP;   // product-grid points = MZ + 1
+  __host__ __device__ long modes() const { return (long)KX * KY; }
+  __host__ __device__ size_t field_elems() const { return (size_t)NZ * KY * KX; }  // complex elements
+};
+
+// Even/odd split of the collocation operators (see k_solve.cu).
+struct SolveLayout {
+  int ne_v, no_v;  // even / odd unknowns of the v equation
+  int ne_w, no_w;  // even / odd unknowns of the omega_y equation
+  size_t stride;   // doubles per k^2 entry: ne_v^2 + no_v^2 + ne_w^2 + no_w^2
+};
+
+struct Handle {
+  chf_config cfg;
+  Dims d;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool uploaded = false;
+
+  // resident state, FP64 (identical layout to the host arrays)
+  cd* f[F_COUNT] = {};
+  double* mean[M_COUNT] = {};  // each 2*NZ doubles, (2,0:nz)
+
+  // wavenumbers
+  double* iapha = nullptr;  // KX
+  double* ibeta = nullptr;  // KY
+  // Chebyshev collocation matrices (SCHEB), column-major NZ x NZ
+  double *t0 = nullptr, *t2 = nullptr, *t4 = nullptr;
+  // implicit operator inverses per distinct k^2 (even/odd blocks)
+  SolveLayout sl{};
+  int nk2 = 0;
+  double* k2vals = nullptr;   // nk2
+  double* xinv = nullptr;     // nk2 * sl.stride
+  double* xmean = nullptr;    // inverse of the (0,0) operator, NZ x NZ column-major
+  int* group_start = nullptr; // nk2 + 1 (modes grouped by k^2)
+  int* group_modes = nullptr; // solved modes, sorted by k^2 index
+  int nsolve = 0;
+
+  // FFT plans and twiddles
+  FftPlan py, px, pz2, pzm;   // PY, PX, 2N, 2MZ
+  cd *tw_py = nullptr, *tw_px = nullptr, *tw_z2 = nullptr, *tw_zm = nullptr;
+  cf *twf_py = nullptr, *twf_px = nullptr;
+
+  // work buffers
+  cd* wz = nullptr;   // 6 x [MP][KY][KX]  (values on the product grid)
+  cd* wy = nullptr;   // 6 x [MP][PY][KX]  (after the spanwise transform)
+  void* scratch = nullptr;  // reduction scratch (diagnostics)
+  size_t scratch_bytes = 0;
+
+  // statistics
+  int kernels_per_step = 0;
+  cudaStream_t own_stream = nullptr;
+
+  // per-kernel event timing (chf_profile_*)
+  struct ProfRec {
+    const char* name;
+    int launches;
+    double ms;
+  };
+  struct ProfPending {
+    int kid;
+    cudaEvent_t a, b;
+  };
+  bool profiling = false;
+  std::vector<ProfRec> prof;
+  std::vector<ProfPending> pending;
+  std::vector<cudaEvent_t> event_pool;
+};
+
+// Kernel ids for profiling.
+enum KernelId { K_ZC2V = 0, K_YINV, K_XPROD, K_YFWD, K_ZCURL, K_SOLVE, K_DIAG, K_COUNT };
+extern const char* const kKernelNames[K_COUNT];
+
+// Bracket one launch with events when profiling is on.
+void prof_begin(Handle* h, int kid, cudaEvent_t* a);
+void prof_end(Handle* h, int kid, cudaEvent_t a);
+
+bool cuda_ok(Handle* h, cudaError_t e, const char* what);
+
+// launchers (k_nonlinear.cu)
+int launch_nonlinear_fp64(Handle* h);
+// launchers (k_solve.cu)
+int setup_solver(Handle* h);
+int launch_solve_fp64(Handle* h);
+int launch_diagnostics(Handle* h, chf_diag* out);
+
+// FFT plan helper (host)
+FftPlan make_plan(int L);
+}  // namespace chf

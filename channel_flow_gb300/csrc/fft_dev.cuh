@@ -1,0 +1,179 @@
+// fft_dev.cuh -- batched complex DFTs in shared memory for sm_103a.
+//
+// Stockham auto-sort formulation (each stage reads stride L/R, writes
+// blocks of Ns), radices 4, 2, 3 and 5.  The whole CTA cooperates on
+// `nlines` lines that live in shared memory; each stage reads every
+// butterfly's inputs into registers, synchronises, then writes, so one
+// buffer suffices.  Twiddles come from a host-computed table
+// tw[k] = exp(-2 pi i k / L) (accurate libm values, identical on every run).
+//
+// Sign convention: SIGN = -1 is FFTW_FORWARD, +1 is FFTW_BACKWARD
+// (unnormalised), matching the reference's fftw_f77_one calls.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace chf {
+
+template <typename T>
+struct cplx {
+  T re, im;
+};
+
+struct FftPlan {
+  int L;
+  int nst;
+  int R[16];
+  int Ns[16];
+};
+
+template <typename T>
+__device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
+  cplx<T> r;
+  r.re = a.re * b.re - a.im * b.im;
+  r.im = a.re * b.im + a.im * b.re;
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) {
+  return cplx<T>{a.re + b.re, a.im + b.im};
+}
+
+template <typename T>
+__device__ __forceinline__ cplx<T> csub(cplx<T> a, cplx<T> b) {
+  return cplx<T>{a.re - b.re, a.im - b.im};
+}
+
+// v[k] <- sum_r v[r] exp(SIGN 2 pi i r k / R)
+template <typename T, int SIGN>
+__device__ __forceinline__ void bfly2(cplx<T>* v) {
+  cplx<T> a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void bfly4(cplx<T>* v) {
+  cplx<T> t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+  cplx<T> t2 = cadd(v[1], v[3]), t3 = csub(v[1], v[3]);
+  cplx<T> st3;  // (SIGN i) * t3
+  st3.re = (T)(-SIGN) * t3.im;
+  st3.im = (T)(SIGN)*t3.re;
+  v[0] = cadd(t0, t2);
+  v[2] = csub(t0, t2);
+  v[1] = cadd(t1, st3);
+  v[3] = csub(t1, st3);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void bfly3(cplx<T>* v) {
+  const T c = (T)0.86602540378443864676;  // sqrt(3)/2
+  cplx<T> s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+  cplx<T> a = v[0];
+  cplx<T> m{a.re - (T)0.5 * s.re, a.im - (T)0.5 * s.im};
+  cplx<T> e{(T)(-SIGN) * c * d.im, (T)(SIGN)*c * d.re};
+  v[0] = cadd(a, s);
+  v[1] = cadd(m, e);
+  v[2] = csub(m, e);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void bfly5(cplx<T>* v) {
+  // Direct 5-point DFT with the exact roots cos/sin(2 pi k / 5).
+  const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+  const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;
+  cplx<T> a = v[0];
+  cplx<T> p1 = cadd(v[1], v[4]), m1 = csub(v[1], v[4]);
+  cplx<T> p2 = cadd(v[2], v[3]), m2 = csub(v[2], v[3]);
+  cplx<T> r1{a.re + c1 * p1.re + c2 * p2.re, a.im + c1 * p1.im + c2 * p2.im};
+  cplx<T> r2{a.re + c2 * p1.re + c1 * p2.re, a.im + c2 * p1.im + c1 * p2.im};
+  // SIGN i (s1 m1 + s2 m2) and SIGN i (s2 m1 - s1 m2)
+  cplx<T> i1{(T)(-SIGN) * (s1 * m1.im + s2 * m2.im), (T)(SIGN) * (s1 * m1.re + s2 * m2.re)};
+  cplx<T> i2{(T)(-SIGN) * (s2 * m1.im - s1 * m2.im), (T)(SIGN) * (s2 * m1.re - s1 * m2.re)};
+  v[0] = cplx<T>{a.re + p1.re + p2.re, a.im + p1.im + p2.im};
+  v[1] = cadd(r1, i1);
+  v[4] = csub(r1, i1);
+  v[2] = cadd(r2, i2);
+  v[3] = csub(r2, i2);
+}
+
+// One stage helper: load R inputs of butterfly (line, j), twiddle, butterfly.
+template <typename T, int SIGN, int R>
+__device__ __forceinline__ void stage_load(const cplx<T>* __restrict__ base, int j, int nr, int jm,
+                                           int twstep, const cplx<T>* __restrict__ tw,
+                                           cplx<T>* v) {
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    cplx<T> x = base[j + r * nr];
+    if (r > 0) {
+      cplx<T> w = tw[r * jm * twstep];
+      if (SIGN > 0) w.im = -w.im;
+      x = cmul(x, w);
+    }
+    v[r] = x;
+  }
+  if (R == 2) bfly2<T, SIGN>(v);
+  if (R == 3) bfly3<T, SIGN>(v);
+  if (R == 4) bfly4<T, SIGN>(v);
+  if (R == 5) bfly5<T, SIGN>(v);
+}
+
+// One Stockham stage with compile-time radix R; each thread owns up to MB
+// butterflies (b = tid + k * blockDim.x).  Reads all inputs, synchronises,
+// writes all outputs, synchronises.
+template <typename T, int SIGN, int R, int MB>
+__device__ __forceinline__ void fft_stage(cplx<T>* s, int nlines, int lstride, int L, int Ns,
+                                          const cplx<T>* __restrict__ tw) {
+  const int nt = blockDim.x, tid = threadIdx.x;
+  const int nr = L / R;
+  const int total = nlines * nr;
+  const int twstep = L / (Ns * R);
+  cplx<T> v[MB][R];
+#pragma unroll
+  for (int b = 0; b < MB; ++b) {
+    int t = tid + b * nt;
+    if (t < total) {
+      int line = t / nr, j = t - line * nr;
+      stage_load<T, SIGN, R>(s + line * lstride, j, nr, j % Ns, twstep, tw, v[b]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < MB; ++b) {
+    int t = tid + b * nt;
+    if (t < total) {
+      int line = t / nr, j = t - line * nr;
+      int jm = j % Ns;
+      cplx<T>* base = s + line * lstride + (j / Ns) * Ns * R + jm;
+#pragma unroll
+      for (int r = 0; r < R; ++r) base[r * Ns] = v[b][r];
+    }
+  }
+  __syncthreads();
+}
+
+// Batched in-place DFT of `nlines` lines of length p.L in shared memory,
+// line l at s + l * lstride.  All threads of the CTA must call it.
+// MB2 bounds the radix-2 butterflies per thread:
+//   MB2 >= ceil(nlines * L / 2 / blockDim.x)   (checked by the launchers).
+template <typename T, int SIGN, int MB2>
+__device__ void smem_fft(cplx<T>* s, int nlines, int lstride, const FftPlan& p,
+                         const cplx<T>* __restrict__ tw) {
+  constexpr int MB4 = (MB2 + 1) / 2;
+  constexpr int MB3 = (2 * MB2 + 2) / 3;
+  constexpr int MB5 = (2 * MB2 + 4) / 5;
+  for (int st = 0; st < p.nst; ++st) {
+    const int R = p.R[st], Ns = p.Ns[st];
+    if (R == 4) fft_stage<T, SIGN, 4, MB4>(s, nlines, lstride, p.L, Ns, tw);
+    else if (R == 2) fft_stage<T, SIGN, 2, MB2>(s, nlines, lstride, p.L, Ns, tw);
+    else if (R == 3) fft_stage<T, SIGN, 3, MB3>(s, nlines, lstride, p.L, Ns, tw);
+    else fft_stage<T, SIGN, 5, MB5>(s, nlines, lstride, p.L, Ns, tw);
+  }
+}
+
+// Host-side check of the MB2 bound for a launch.
+inline bool fft_fits(int nlines, int L, int nthreads, int mb2) {
+  return (long)nlines * (L / 2) <= (long)mb2 * nthreads;
+}
+
+}  // namespace chf

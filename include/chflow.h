@@ -1,0 +1,149 @@
+/*
+ * chflow.h -- C ABI of the GB300 channel-flow time step.
+ *
+ * Drop-in for the per-step call sequence of poiseuilleflow.f90: the Fortran
+ * main loop calls getnonlinear (poiseuilleflow.f90:224) and then the inline
+ * per-mode solve (poiseuilleflow.f90:242-394) and the (0,0)-mode solve
+ * (poiseuilleflow.f90:401-474).  A driver keeps its module arrays
+ * (paraandcons.f90:28-38) on the host and hands them to this library once;
+ * the library keeps them resident in device memory, advances them with
+ * hand-written sm_103a kernels and hands them back at output/restart steps.
+ *
+ * Array conventions (identical to the reference, one rank, nproc = 1):
+ *   field arrays  real*8 (0:nx,0:ny,0:nz), nx = nnx-1, ny = nny-1, nz = nnz,
+ *                 column-major; even x index = real part and odd x index =
+ *                 imaginary part of streamwise mode x/2 (poiseuilleflow.f90:8-12);
+ *                 Chebyshev coefficients in z for vnp1, omegaynp1, unp1, wnp1,
+ *                 omegaxnp1, omegaznp1 after a step; Gauss-Lobatto values for
+ *                 the nonlinear histories rhsvn, rhsomegayn (and unp1, wnp1
+ *                 between chf_getnonlinear and chf_solve).
+ *   mean arrays   real*8 (2,0:nz): clamb1n, clamb1nm1, clamb3n, clamb3nm1,
+ *                 au0, w0.
+ *
+ * Every entry point returns CHF_OK (0) or a negative CHF_E* status and never
+ * exits or aborts; chf_last_error() describes the last failure.  A handle is
+ * not re-entrant: calls on one handle must not overlap.  Different handles
+ * are independent.
+ */
+#ifndef CHFLOW_H
+#define CHFLOW_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CHF_OK 0
+#define CHF_E_INVALID (-1)   /* bad argument or configuration */
+#define CHF_E_CUDA (-2)      /* CUDA runtime error */
+#define CHF_E_NOMEM (-3)     /* device or host allocation failed */
+#define CHF_E_STATE (-4)     /* call out of order (e.g. step before upload) */
+#define CHF_E_NUMERIC (-5)   /* non-finite values detected */
+
+#define CHF_FP64 0           /* all arithmetic in FP64 */
+#define CHF_MIXED 1          /* FP32 transforms/products, FP64 solves */
+
+/* Runtime counterpart of the compile-time parameters of paraandcons.f90:4-25. */
+typedef struct chf_config {
+  int nnx;        /* streamwise points, paraandcons.f90:5  (multiple of 4) */
+  int nny;        /* spanwise points, paraandcons.f90:6    (multiple of 4) */
+  int nnz;        /* Chebyshev degree, paraandcons.f90:7   (even)          */
+  double aphi;    /* streamwise box 2*pi*aphi, paraandcons.f90:22 */
+  double beta;    /* spanwise box 2*pi*beta, paraandcons.f90:22   */
+  double dt;      /* time step, paraandcons.f90:23 */
+  double re;      /* Reynolds number (viscosity 1/re), paraandcons.f90:24 */
+  double re_p;    /* mean pressure gradient, paraandcons.f90:25 */
+  int precision;  /* CHF_FP64 or CHF_MIXED */
+  int zpad;       /* wall-normal intervals of the product grid; 0 = 2*nnz as
+                     in getlamb (poiseuilleflow.f90:1647-1648); any value with
+                     2*zpad > 3*nnz gives the same (exact) products */
+  int device;     /* CUDA device ordinal */
+} chf_config;
+
+typedef struct chf_handle chf_handle;
+
+/* Diagnostics of the current state (spectral, Parseval). */
+typedef struct chf_diag {
+  double energy;        /* 0.5 * sum over modes and z-coefficients of |u|^2+|v|^2+|w|^2,
+                           the spectral sum printed at poiseuilleflow.f90:2322-2336 */
+  double wall_shear_top;    /* d<u>/dz at z = +1 from au0 */
+  double wall_shear_bottom; /* d<u>/dz at z = -1 from au0 */
+  double max_abs;       /* max |value| over the prognostic fields */
+  int finite;           /* 1 if every value is finite */
+} chf_diag;
+
+/* Allocate device state and precompute the implicit operators.  Replaces the
+ * set-up of poiseuilleflow.f90:77-214 (allocation, FFT plans, wavenumbers,
+ * SCHEB and the zgetrf/zgetri explicit inverses). */
+int chf_create(const chf_config* cfg, chf_handle** out);
+int chf_destroy(chf_handle* h);
+
+/* Last error message of h, or of the last failed chf_create when h is NULL. */
+const char* chf_last_error(const chf_handle* h);
+
+/* Copy the module arrays paraandcons.f90:28-38 host -> device.  Any pointer
+ * may be NULL to leave that array unchanged. */
+int chf_upload_state(chf_handle* h,
+                     const double* vnp1, const double* omegaynp1,
+                     const double* unp1, const double* wnp1,
+                     const double* omegaxnp1, const double* omegaznp1,
+                     const double* rhsvn, const double* rhsomegayn,
+                     const double* clamb1n, const double* clamb1nm1,
+                     const double* clamb3n, const double* clamb3nm1,
+                     const double* au0, const double* w0);
+
+/* Copy the module arrays device -> host (blocking).  NULL pointers skipped. */
+int chf_download_state(chf_handle* h,
+                       double* vnp1, double* omegaynp1,
+                       double* unp1, double* wnp1,
+                       double* omegaxnp1, double* omegaznp1,
+                       double* rhsvn, double* rhsomegayn,
+                       double* clamb1n, double* clamb1nm1,
+                       double* clamb3n, double* clamb3nm1,
+                       double* au0, double* w0);
+
+/* getnonlinear (poiseuilleflow.f90:1380-1612): Lamb vector by dealiased
+ * products, its curl/projection, history swap, coefficients -> GL values. */
+int chf_getnonlinear(chf_handle* h);
+
+/* The per-mode solve loop (poiseuilleflow.f90:242-394) followed by the
+ * (0,0)-mode solve (poiseuilleflow.f90:401-474). */
+int chf_solve(chf_handle* h);
+
+/* nsteps iterations of the main loop body for istep > istepbegin
+ * (poiseuilleflow.f90:224 then 242-474).  Asynchronous on the handle's
+ * stream; chf_synchronize() waits. */
+int chf_step(chf_handle* h, int nsteps);
+
+int chf_synchronize(chf_handle* h);
+
+/* Diagnostics of the current state (synchronous). */
+int chf_diagnostics(chf_handle* h, chf_diag* out);
+
+/* Number of kernels launched per chf_step iteration (for instrumentation). */
+int chf_kernels_per_step(const chf_handle* h);
+
+/* Device address of one resident module array (0..7: vnp1, omegaynp1, unp1,
+ * wnp1, omegaxnp1, omegaznp1, rhsvn, rhsomegayn), for zero-copy access by
+ * device-side callers.  Valid until the next chf_* call on h. */
+int chf_device_field(chf_handle* h, int which, void** dptr);
+
+/* Run subsequent work of h on a caller-provided CUDA stream (a cudaStream_t
+ * passed as void*), e.g. the stream of a host framework; NULL restores the
+ * library's own stream.  The caller keeps the stream alive while h uses it. */
+int chf_set_stream(chf_handle* h, void* stream);
+
+/* Per-kernel timing with CUDA events recorded around every launch on the
+ * handle's stream (off by default; the reference's only instrumentation is
+ * the mpi_wtime prints at poiseuilleflow.f90:216-229, 481-486). */
+int chf_profile_enable(chf_handle* h, int on);
+int chf_profile_reset(chf_handle* h);
+/* Kernel idx (0-based): its name, launch count and total device time since
+ * the last reset (synchronises the stream).  CHF_E_INVALID past the end. */
+int chf_profile_read(chf_handle* h, int idx, const char** name, int* launches, double* total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHFLOW_H */

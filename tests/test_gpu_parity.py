@@ -1,0 +1,203 @@
+"""FP64 CUDA path vs the CPU oracle, through the C ABI.
+
+Tolerances: per-array relative L2 error.  One getnonlinear or one solve:
+1e-11.  N full steps: 1e-10 (the bar the FP64 path must meet against the
+reference algorithm).  The (0,0)-mode Lamb histories clamb* are plane
+averages with heavy cancellation; the oracle itself is 1e-11..1e-9 away from
+their extended-precision value, so they are held to 1e-7 here and, in
+test_mean_lamb_accuracy, the GPU must be at least as accurate as the oracle.  The GPU evaluates the same mathematics with a
+different operation order (6+3 instead of 12+6 transforms, even/odd block
+inverses, recurrence-based explicit terms), so agreement is to rounding, not
+bitwise.
+"""
+import numpy as np
+import pytest
+
+from channel_flow_gb300 import Channel, ChannelError, config, fields
+from channel_flow_gb300.fields import FIELD_NAMES, MEAN_NAMES
+from exact_mean import mean_h1
+from parity import check, compare, worst
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "small16": config.small(nnx=16, nny=8, nnz=16, aphi=1.0, beta=0.5, dt=5e-4, re=180.0, re_p=1.0),
+    "c1_32": config.CONFIGS["c1_poiseuille_32"],
+    "c2_os": config.CONFIGS["c2_orr_sommerfeld"],
+    "mixed_radix": config.small(nnx=24, nny=12, nnz=20, aphi=1.5, beta=0.75, dt=5e-4, re=300.0, re_p=1.0),
+}
+
+
+def make_state(cfg, seed=3):
+    return fields.reference_like_state(cfg, seed=seed, epsilon=0.3, noise=0.02, gamma=5.0)
+
+
+def pair(cfg, oracle_mod, st, zpad=0):
+    o = oracle_mod.Oracle.from_config(cfg)
+    o.setup()
+    o.set_state(st)
+    g = Channel(cfg, zpad=zpad)
+    g.upload_state(st)
+    return o, g
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_upload_download_roundtrip(chflow_lib, name):
+    cfg = CASES[name]
+    rng = np.random.default_rng(0)
+    st = {k: rng.standard_normal((cfg.nnz + 1, cfg.nny, cfg.nnx)) for k in FIELD_NAMES}
+    st.update({k: rng.standard_normal((cfg.nnz + 1, 2)) for k in MEAN_NAMES})
+    with Channel(cfg) as g:
+        g.upload_state(st)
+        back = g.download_state()
+    for k in st:
+        assert np.array_equal(back[k], st[k]), k
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_getnonlinear_matches_oracle(chflow_lib, oracle_mod, name):
+    cfg = CASES[name]
+    st = make_state(cfg)
+    o, g = pair(cfg, oracle_mod, st)
+    o.getnonlinear()
+    g.getnonlinear()
+    check(g.download_state(), o.get_state(), 1e-11, 1e-7)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_solve_matches_oracle(chflow_lib, oracle_mod, name):
+    cfg = CASES[name]
+    st = make_state(cfg, seed=5)
+    o, g = pair(cfg, oracle_mod, st)
+    o.getnonlinear()
+    mid = o.get_state()
+    g.upload_state(mid)
+    o.solve()
+    g.solve()
+    check(g.download_state(), o.get_state(), 1e-11, 1e-7)
+
+
+@pytest.mark.parametrize("name,nsteps", [("small16", 40), ("c1_32", 20), ("c2_os", 20), ("mixed_radix", 20)])
+def test_steps_match_oracle(chflow_lib, oracle_mod, name, nsteps):
+    cfg = CASES[name]
+    st = make_state(cfg, seed=7)
+    o, g = pair(cfg, oracle_mod, st)
+    # the reference's start-up: getnonlinear in initial(), then a solve-only step
+    o.getnonlinear(); o.solve()
+    g.getnonlinear(); g.solve()
+    o.step(nsteps)
+    g.step(nsteps)
+    check(g.download_state(), o.get_state(), 1e-10, 1e-7)
+
+
+def test_lowmode_c1_steps(chflow_lib, oracle_mod):
+    cfg = CASES["c1_32"]
+    st = fields.lowmode_state(cfg, seed=11, amp=1e-3)
+    o, g = pair(cfg, oracle_mod, st)
+    o.getnonlinear(); o.solve(); o.step(30)
+    g.getnonlinear(); g.solve(); g.step(30)
+    check(g.download_state(), o.get_state(), 1e-10, 1e-7)
+
+
+def test_zpad_equivalence(chflow_lib):
+    """Any product grid with 2*zpad > 3*nnz gives the same products."""
+    cfg = CASES["small16"]
+    st = make_state(cfg, seed=9)
+    outs = []
+    for zpad in (0, 25, 27, 40):
+        with Channel(cfg, zpad=zpad) as g:
+            g.upload_state(st)
+            g.getnonlinear(); g.solve(); g.step(5)
+            outs.append(g.download_state())
+    for other in outs[1:]:
+        k, e = worst(compare(other, outs[0]))
+        assert e < 1e-12, (k, e)
+
+
+def test_laminar_fixed_point(chflow_lib):
+    cfg = CASES["c1_32"]
+    st = fields.laminar_state(cfg)
+    with Channel(cfg) as g:
+        g.upload_state(st)
+        g.step(50)
+        out = g.download_state()
+    for k in ("au0", "unp1", "omegaznp1", "clamb1n", "clamb1nm1"):
+        err = np.abs(out[k] - st[k]).max() / max(np.abs(st[k]).max(), 1.0)
+        assert err < 1e-11, (k, err)
+
+
+def test_diagnostics_energy(chflow_lib):
+    cfg = CASES["c1_32"]
+    st = make_state(cfg)
+    with Channel(cfg) as g:
+        g.upload_state(st)
+        d = g.diagnostics()
+    e = 0.5 * sum((st[k] ** 2).sum() for k in ("unp1", "vnp1", "wnp1"))
+    assert d["finite"]
+    assert abs(d["energy"] - e) <= 1e-12 * e
+    mx = max(np.abs(st[k]).max() for k in FIELD_NAMES[:6])
+    assert d["max_abs"] == mx
+
+
+def test_nonfinite_state_is_reported(chflow_lib):
+    cfg = CASES["small16"]
+    st = make_state(cfg)
+    st["vnp1"][3, 2, 1] = np.nan
+    with Channel(cfg) as g:
+        g.upload_state(st)
+        d = g.diagnostics()
+    assert not d["finite"]
+
+
+def test_step_before_upload_is_an_error(chflow_lib):
+    with Channel(CASES["small16"]) as g:
+        with pytest.raises(ChannelError) as ei:
+            g.step(1)
+        assert ei.value.code == -4
+
+
+def test_divergence_free_after_steps(chflow_lib):
+    """i alpha u + Dv + i beta w = 0 for every solved mode (REF:2365-2377)."""
+    cfg = CASES["c1_32"]
+    st = make_state(cfg)
+    with Channel(cfg) as g:
+        g.upload_state(st)
+        g.getnonlinear(); g.solve(); g.step(5)
+        out = g.download_state()
+    ia, ib = fields.wavenumbers(cfg)
+    D = fields.cheb_derivative_matrix(cfg.nnz)
+    u = fields.as_complex(out["unp1"]); v = fields.as_complex(out["vnp1"]); w = fields.as_complex(out["wnp1"])
+    div = 1j * ia[None, None, :] * u + np.tensordot(D, v, axes=(1, 0)) + 1j * ib[None, :, None] * w
+    div[:, cfg.nny // 2, :] = 0
+    div[:, 0, 0] = 0
+    scale = np.abs(np.tensordot(D, v, axes=(1, 0))).max()
+    assert np.abs(div).max() < 1e-11 * scale
+
+
+def test_full_size_two_steps(chflow_lib, oracle_mod):
+    """128 x 129 x 128 (Re_tau 180 box): two full steps against the oracle."""
+    cfg = config.CONFIGS["c3_retau180_128"]
+    st = fields.reference_like_state(cfg, seed=1)
+    o, g = pair(cfg, oracle_mod, st)
+    o.getnonlinear(); o.solve(); o.step(1)
+    g.getnonlinear(); g.solve(); g.step(1)
+    check(g.download_state(), o.get_state(), 1e-10, 1e-6)
+
+
+@pytest.mark.parametrize("name", ["c1_32", "c2_os", "small16"])
+def test_mean_lamb_accuracy(chflow_lib, oracle_mod, name):
+    """H1(0,0) (left in omegaxnp1 by getnonlinear, REF:1489-1496) against its
+    extended-precision value: the GPU must be at least as accurate as the
+    reference algorithm."""
+    cfg = CASES[name]
+    st = make_state(cfg)
+    exact = mean_h1(cfg, st)
+    o, g = pair(cfg, oracle_mod, st)
+    o.getnonlinear()
+    g.getnonlinear()
+    got_o = o.field("omegaxnp1")[:, 0, 0] + 1j * o.field("omegaxnp1")[:, 0, 1]
+    out = g.download_state()["omegaxnp1"]
+    got_g = out[:, 0, 0] + 1j * out[:, 0, 1]
+    err_o = np.linalg.norm(got_o - exact) / np.linalg.norm(exact)
+    err_g = np.linalg.norm(got_g - exact) / np.linalg.norm(exact)
+    assert err_g <= max(2.0 * err_o, 1e-13), (err_g, err_o)
