@@ -38,7 +38,7 @@ namespace chf {
 
 namespace {
 
-constexpr int S_THREADS = 128;
+constexpr int S_THREADS = 256;
 constexpr int INV_THREADS = 256;
 
 // Offsets of the four blocks inside one k^2 entry of xinv.
@@ -171,7 +171,8 @@ __global__ void __launch_bounds__(INV_THREADS) k_invert(const double* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Per-group solve.
+// Per-group solve: one CTA per distinct k^2 (plus one for the (0,0) mode),
+// modes of the group processed CH at a time.
 // ---------------------------------------------------------------------------
 struct SolveArgs {
   cd *v, *oy, *u, *w, *ox, *oz;       // state (u, w hold the N^{n-1} histories on entry)
@@ -187,261 +188,299 @@ struct SolveArgs {
   int nk2;
 };
 
-// serial Chebyshev derivative of a strided real sequence (dz, REF:570-599)
-__device__ __forceinline__ void dser(const double* a, int as, double* b, int bs, int N) {
-  double bp1 = 0.0, bp2 = 0.0;
-  b[N * bs] = 0.0;
-  for (int k = N; k >= 1; --k) {
-    double bk1 = bp2 + 2.0 * (double)k * a[k * as];
-    if (k == 1) bk1 *= 0.5;
-    b[(k - 1) * bs] = bk1;
-    bp2 = bp1;
-    bp1 = bk1;
+constexpr int CH = 2;          // modes per chunk
+constexpr int S_WARPS = S_THREADS / 32;
+
+// Chebyshev derivative (dz, REF:570-599) of a real sequence a[0..N] (stride
+// as) into b (stride bs), by one warp: b_i = c_i sum_{j>i, j-i odd} 2 j a_j
+// (c_0 = 1/2) evaluated as suffix sums over each parity class, lane-local
+// then a warp scan.  Same sums as the serial recurrence, tree-ordered.
+__device__ __forceinline__ void warp_deriv(const double* a, int as, double* b, int bs, int N) {
+  const int lane = threadIdx.x & 31;
+  const int E = (N + 32) / 32;  // elements per lane (N + 1 <= 32 * E)
+  const int i0 = lane * E;
+  double te = 0.0, to = 0.0;    // lane totals of g_j over even / odd j
+  for (int q = 0; q < E; ++q) {
+    int j = i0 + q;
+    if (j <= N) {
+      double g = 2.0 * (double)j * a[j * as];
+      if (j & 1) to += g; else te += g;
+    }
   }
+  double se = te, so = to;      // inclusive suffix scan over lanes
+  for (int off = 1; off < 32; off <<= 1) {
+    double ue = __shfl_down_sync(0xffffffffu, se, off);
+    double uo = __shfl_down_sync(0xffffffffu, so, off);
+    if (lane + off < 32) { se += ue; so += uo; }
+  }
+  double re_ = se - te, ro = so - to;  // sums over lanes above this one
+  for (int q = E - 1; q >= 0; --q) {
+    int i = i0 + q;
+    if (i <= N) {
+      double bi = (i & 1) ? re_ : ro;  // sum over j > i of the opposite parity
+      if (i == 0) bi *= 0.5;
+      b[i * bs] = bi;
+      double g = 2.0 * (double)i * a[i * as];
+      if (i & 1) ro += g; else re_ += g;
+    }
+  }
+  __syncwarp();
 }
 
-struct SolveSmem {
-  cd* c;      // NZ coefficients of the current unknown
-  cd* r;      // NZ explicit AB2 terms at GL points
-  cd* fb;     // 2N FFT buffer
-  double* dr; // 4 x NZ derivative scratch (re)
-  double* di; // 4 x NZ derivative scratch (im)
-  cd* e;      // ne rhs (even)
-  cd* o;      // no rhs (odd)
-  cd* x;      // NZ solution
+struct ChunkSmem {
+  cd* cv;     // [CH][NZ] v coefficients  -> new v
+  cd* co;     // [CH][NZ] omega_y coeffs  -> new omega_y
+  cd* rv;     // [CH][NZ] AB2 explicit term of the v equation (GL values)
+  cd* rg;     // [CH][NZ] AB2 explicit term of the omega_y equation
+  cd* fb;     // [2 CH][2N] DFT lines
+  double* dd; // [CH][10][NZ] derivative scratch; also the even/odd rhs
 };
 
-// Values at the Gauss-Lobatto points of the series in s.fb[0..N] (already
-// written as coefficients): even extension with doubled ends, forward DFT,
-// halve.  Result in s.fb[p], p = 0..N.
-__device__ void gl_values(SolveSmem& s, const SolveArgs& a) {
-  const int N = a.d.N, L2 = 2 * N;
-  for (int n = threadIdx.x; n <= N; n += blockDim.x) {
-    cd v = s.fb[n];
-    if (n > 0 && n < N) s.fb[L2 - n] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s.fb[0] = cd{2.0 * s.fb[0].re, 2.0 * s.fb[0].im};
-    s.fb[N] = cd{2.0 * s.fb[N].re, 2.0 * s.fb[N].im};
-  }
-  __syncthreads();
-  smem_fft<double, -1, 2>(s.fb, 1, L2, a.pz2, a.tw2);
-  for (int n = threadIdx.x; n <= N; n += blockDim.x) s.fb[n] = cd{0.5 * s.fb[n].re, 0.5 * s.fb[n].im};
-  __syncthreads();
+__device__ __forceinline__ double* dslot(const ChunkSmem& s, int m, int q, int NZ) {
+  return s.dd + ((size_t)m * 10 + q) * NZ;
 }
 
-// Solve one CN collocation equation for the unknown whose current
-// coefficients are in s.c and whose explicit AB2 values are in s.r.
-// isv: v equation (4th order, BC rows v(+-1) = v'(+-1) = 0) else 2nd order.
-// On return the new coefficients are in s.x.
-__device__ void solve_eq(SolveSmem& s, const SolveArgs& a, double k2, const double* X, bool isv) {
-  const int N = a.d.N, NZ = N + 1;
-  const double dt = a.dt, re = a.re;
-  // derivatives: re by thread 0, im by thread 32 (different warps)
-  const int nder = isv ? 4 : 2;
-  if (threadIdx.x == 0 || threadIdx.x == 32) {
-    const bool im = threadIdx.x == 32;
-    const double* c = reinterpret_cast<const double*>(s.c) + (im ? 1 : 0);
-    double* dd = im ? s.di : s.dr;
-    dser(c, 2, dd, 1, N);
-    for (int q = 1; q < nder; ++q) dser(dd + (q - 1) * NZ, 1, dd + q * NZ, 1, N);
-  }
-  __syncthreads();
-  for (int n = threadIdx.x; n <= N; n += blockDim.x) {
-    cd c = s.c[n];
-    cd w;
-    if (isv) {
-      double c4 = dt * 0.5 / re, c2 = 1.0 - k2 * dt / re, c0 = -k2 * (1.0 - k2 * dt * 0.5 / re);
-      w.re = c4 * s.dr[3 * NZ + n] + c2 * s.dr[NZ + n] + c0 * c.re;
-      w.im = c4 * s.di[3 * NZ + n] + c2 * s.di[NZ + n] + c0 * c.im;
-    } else {
-      double c2 = dt * 0.5 / re, c0 = 1.0 - k2 * dt * 0.5 / re;
-      w.re = c2 * s.dr[NZ + n] + c0 * c.re;
-      w.im = c2 * s.di[NZ + n] + c0 * c.im;
-    }
-    s.fb[n] = w;
-  }
-  __syncthreads();
-  gl_values(s, a);
-  // right-hand side at the collocation points, folded into even/odd parts
-  const SolveLayout& sl = a.sl;
-  const int ne = isv ? sl.ne_v : sl.ne_w, no = isv ? sl.no_v : sl.no_w;
-  const int r0 = isv ? 2 : 1;  // first interior row of the blocks
-  for (int r = threadIdx.x; r < ne; r += blockDim.x) {
-    cd e{0.0, 0.0}, o{0.0, 0.0};
-    if (r >= r0) {
-      int p = r, q = N - r;
-      cd Rp{s.fb[p].re + s.r[p].re, s.fb[p].im + s.r[p].im};
-      cd Rq{s.fb[q].re + s.r[q].re, s.fb[q].im + s.r[q].im};
-      e = cd{0.5 * (Rp.re + Rq.re), 0.5 * (Rp.im + Rq.im)};
-      o = cd{0.5 * (Rp.re - Rq.re), 0.5 * (Rp.im - Rq.im)};
-    }
-    s.e[r] = e;
-    if (r < no) s.o[r] = o;
-  }
-  __syncthreads();
-  // matvecs: even rows then odd rows; X blocks column-major
-  BlockOffsets bo = block_offsets(sl);
-  const double* Xe = X + (isv ? bo.ve : bo.we);
-  const double* Xo = X + (isv ? bo.vo : bo.wo);
-  for (int t = threadIdx.x; t < ne + no; t += blockDim.x) {
-    const bool ev = t < ne;
-    const int row = ev ? t : t - ne, n = ev ? ne : no;
-    const double* Xb = ev ? Xe : Xo;
-    const cd* rhs = ev ? s.e : s.o;
-    double ar = 0.0, ai = 0.0;
-    for (int c = r0; c < n; ++c) {
-      double xv = __ldg(Xb + (size_t)c * n + row);
-      ar = fma(xv, rhs[c].re, ar);
-      ai = fma(xv, rhs[c].im, ai);
-    }
-    int j = ev ? 2 * row : 2 * row + 1;
-    s.x[j] = cd{ar, ai};
-  }
-  __syncthreads();
-}
-
-__global__ void __launch_bounds__(S_THREADS) k_solve(const __grid_constant__ SolveArgs a) {
+__global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ SolveArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Dims& d = a.d;
-  const int N = d.N, NZ = d.NZ;
+  const int N = d.N, NZ = d.NZ, L2 = 2 * N;
   const long modes = d.modes();
-  SolveSmem s;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  ChunkSmem s;
   {
     cd* p = reinterpret_cast<cd*>(smem_raw);
-    s.c = p; p += NZ;
-    s.r = p; p += NZ;
-    s.fb = p; p += 2 * N;
-    s.e = p; p += NZ;
-    s.o = p; p += NZ;
-    s.x = p; p += NZ;
-    double* q = reinterpret_cast<double*>(p);
-    s.dr = q; q += 4 * NZ;
-    s.di = q; q += 4 * NZ;
+    s.cv = p; p += CH * NZ;
+    s.co = p; p += CH * NZ;
+    s.rv = p; p += CH * NZ;
+    s.rg = p; p += CH * NZ;
+    s.fb = p; p += 2 * CH * L2;
+    s.dd = reinterpret_cast<double*>(p);
   }
   const int g = blockIdx.x;
-  const double dt = a.dt;
+  const bool mean = (g == a.nk2);
+  const double dt = a.dt, re = a.re;
+  const double k2 = mean ? 0.0 : a.k2vals[g];
   const double* X = a.xinv + (size_t)g * a.sl.stride;
-  if (g == a.nk2) {
-    // (0,0) mode: au0 with clamb1, then w0 with clamb3 (REF:401-474)
-    for (int comp = 0; comp < 2; ++comp) {
-      const double* cln = comp == 0 ? a.cl1n : a.cl3n;
-      const double* clm = comp == 0 ? a.cl1nm1 : a.cl3nm1;
-      double* am = comp == 0 ? a.au0 : a.w0;
-      for (int n = threadIdx.x; n <= N; n += blockDim.x) {
-        s.c[n] = cd{am[2 * n], am[2 * n + 1]};
-        s.r[n] = cd{-1.0 * dt / 2.0 * (3.0 * cln[2 * n] - clm[2 * n]),
-                    -1.0 * dt / 2.0 * (3.0 * cln[2 * n + 1] - clm[2 * n + 1])};
+  const SolveLayout& sl = a.sl;
+  BlockOffsets bo = block_offsets(sl);
+  const int gs = mean ? 0 : a.group_start[g], ge = mean ? 2 : a.group_start[g + 1];
+  const double c3 = 3.0 * dt / 2.0, c1 = dt / 2.0;
+  for (int base = gs; base < ge; base += CH) {
+    const int nm = min(CH, ge - base);
+    // ---- A: load coefficients and explicit AB2 terms
+    for (int t = tid; t < CH * NZ; t += blockDim.x) {
+      int m = t / NZ, n = t % NZ;
+      cd v{0.0, 0.0}, oy{0.0, 0.0}, rv{0.0, 0.0}, rg{0.0, 0.0};
+      if (m < nm) {
+        if (mean) {
+          const double* am = m == 0 ? a.au0 : a.w0;
+          const double* cln = m == 0 ? a.cl1n : a.cl3n;
+          const double* clm = m == 0 ? a.cl1nm1 : a.cl3nm1;
+          oy = cd{am[2 * n], am[2 * n + 1]};
+          rg = cd{-1.0 * dt / 2.0 * (3.0 * cln[2 * n] - clm[2 * n]),
+                  -1.0 * dt / 2.0 * (3.0 * cln[2 * n + 1] - clm[2 * n + 1])};
+        } else {
+          const int mode = a.group_modes[base + m];
+          size_t idx = (size_t)n * modes + mode;
+          v = a.v[idx];
+          oy = a.oy[idx];
+          cd x = a.rv[idx], y = a.u[idx];
+          rv = cd{(c3 * x.re - c1 * y.re) * 1.0, (c3 * x.im - c1 * y.im) * 1.0};
+          x = a.rg[idx];
+          y = a.w[idx];
+          rg = cd{(c3 * x.re - c1 * y.re) * 1.0, (c3 * x.im - c1 * y.im) * 1.0};
+        }
       }
-      __syncthreads();
-      solve_eq(s, a, 0.0, X, false);
-      cd* vel = comp == 0 ? a.u : a.w;
-      cd* vort = comp == 0 ? a.oz : a.ox;
-      const double sg = comp == 0 ? -1.0 : 1.0;
-      for (int n = threadIdx.x; n <= N; n += blockDim.x) {
-        cd x = s.x[n];
+      s.cv[t] = v;
+      s.co[t] = oy;
+      s.rv[t] = rv;
+      s.rg[t] = rg;
+    }
+    __syncthreads();
+    // ---- B: derivatives, one warp per chain.  task (m, comp): comp 0/1 =
+    // v re/im (D1..D4 into slots comp*4 + 0..3), comp 2/3 = omega_y re/im
+    // (D1 into this mode's omega DFT line, free until phase C; D2 into slot
+    // 8 + comp - 2)
+    for (int task = warp; task < CH * 4; task += S_WARPS) {
+      int m = task / 4, comp = task % 4;
+      if (m >= nm) continue;
+      if (comp < 2) {
+        if (mean) continue;
+        const double* src = reinterpret_cast<const double*>(s.cv + m * NZ) + comp;
+        double* o = dslot(s, m, comp * 4, NZ);
+        warp_deriv(src, 2, o, 1, N);
+        warp_deriv(o, 1, o + NZ, 1, N);
+        warp_deriv(o + NZ, 1, o + 2 * NZ, 1, N);
+        warp_deriv(o + 2 * NZ, 1, o + 3 * NZ, 1, N);
+      } else {
+        const int c = comp - 2;
+        const double* src = reinterpret_cast<const double*>(s.co + m * NZ) + c;
+        double* t1 = reinterpret_cast<double*>(s.fb + (2 * m + 1) * L2) + c * NZ;
+        warp_deriv(src, 2, t1, 1, N);
+        warp_deriv(t1, 1, dslot(s, m, 8 + c, NZ), 1, N);
+      }
+    }
+    __syncthreads();
+    // ---- C: explicit right-hand sides as Chebyshev series -> DFT lines
+    {
+      const double v4 = dt * 0.5 / re, v2 = 1.0 - k2 * dt / re, v0 = -k2 * (1.0 - k2 * dt * 0.5 / re);
+      const double w2 = dt * 0.5 / re, w0 = 1.0 - k2 * dt * 0.5 / re;
+      for (int t = tid; t < CH * NZ; t += blockDim.x) {
+        int m = t / NZ, n = t % NZ;
+        cd* lv = s.fb + (2 * m) * L2;
+        cd* lw = s.fb + (2 * m + 1) * L2;
+        cd cv = s.cv[t], co = s.co[t];
+        cd wv{0.0, 0.0}, ww{0.0, 0.0};
+        if (m < nm) {
+          if (!mean) {
+            wv.re = v4 * dslot(s, m, 3, NZ)[n] + v2 * dslot(s, m, 1, NZ)[n] + v0 * cv.re;
+            wv.im = v4 * dslot(s, m, 7, NZ)[n] + v2 * dslot(s, m, 5, NZ)[n] + v0 * cv.im;
+          }
+          ww.re = w2 * dslot(s, m, 8, NZ)[n] + w0 * co.re;
+          ww.im = w2 * dslot(s, m, 9, NZ)[n] + w0 * co.im;
+        }
+        double dbl = (n == 0 || n == N) ? 2.0 : 1.0;
+        // the omega line's first 2*NZ doubles held D1 scratch; all reads of
+        // it finished before the barrier above
+        lv[n] = cd{dbl * wv.re, dbl * wv.im};
+        lw[n] = cd{dbl * ww.re, dbl * ww.im};
+        if (n > 0 && n < N) {
+          lv[L2 - n] = wv;
+          lw[L2 - n] = ww;
+        }
+      }
+    }
+    __syncthreads();
+    smem_fft<double, -1, 2>(s.fb, 2 * CH, L2, a.pz2, a.tw2);
+    // ---- D: fold the collocation rows into even / odd right-hand sides.
+    // rhs storage reuses dd: [CH][4 blocks][NZ] complex (fits in 10*NZ doubles)
+    const int nev = sl.ne_v, nov = sl.no_v, new_ = sl.ne_w, now_ = sl.no_w;
+    cd* rhs = reinterpret_cast<cd*>(s.dd);  // rhs[(m*4 + b) * NZ + r]
+    for (int t = tid; t < CH * NZ; t += blockDim.x) {
+      int m = t / NZ, r = t % NZ;
+      const cd* lv = s.fb + (2 * m) * L2;
+      const cd* lw = s.fb + (2 * m + 1) * L2;
+      cd ev{0.0, 0.0}, ovv{0.0, 0.0}, ew{0.0, 0.0}, ow{0.0, 0.0};
+      if (m < nm && r <= N / 2) {
+        int p = r, q = N - r;
+        if (!mean && r >= 2) {
+          cd Rp{0.5 * lv[p].re + s.rv[m * NZ + p].re, 0.5 * lv[p].im + s.rv[m * NZ + p].im};
+          cd Rq{0.5 * lv[q].re + s.rv[m * NZ + q].re, 0.5 * lv[q].im + s.rv[m * NZ + q].im};
+          ev = cd{0.5 * (Rp.re + Rq.re), 0.5 * (Rp.im + Rq.im)};
+          ovv = cd{0.5 * (Rp.re - Rq.re), 0.5 * (Rp.im - Rq.im)};
+        }
+        if (r >= 1) {
+          cd Rp{0.5 * lw[p].re + s.rg[m * NZ + p].re, 0.5 * lw[p].im + s.rg[m * NZ + p].im};
+          cd Rq{0.5 * lw[q].re + s.rg[m * NZ + q].re, 0.5 * lw[q].im + s.rg[m * NZ + q].im};
+          ew = cd{0.5 * (Rp.re + Rq.re), 0.5 * (Rp.im + Rq.im)};
+          ow = cd{0.5 * (Rp.re - Rq.re), 0.5 * (Rp.im - Rq.im)};
+        }
+      }
+      if (r < nev) rhs[(m * 4 + 0) * NZ + r] = ev;
+      if (r < nov) rhs[(m * 4 + 1) * NZ + r] = ovv;
+      if (r < new_) rhs[(m * 4 + 2) * NZ + r] = ew;
+      if (r < now_) rhs[(m * 4 + 3) * NZ + r] = ow;
+    }
+    __syncthreads();
+    // ---- E: block matvecs, each inverse element used for every mode of the chunk
+    {
+      const int rows = nev + nov + new_ + now_;
+      for (int t = tid; t < rows; t += blockDim.x) {
+        int b, row, n, r0;
+        if (t < nev) { b = 0; row = t; n = nev; r0 = 2; }
+        else if (t < nev + nov) { b = 1; row = t - nev; n = nov; r0 = 2; }
+        else if (t < nev + nov + new_) { b = 2; row = t - nev - nov; n = new_; r0 = 1; }
+        else { b = 3; row = t - nev - nov - new_; n = now_; r0 = 1; }
+        if (mean && b < 2) continue;
+        const double* Xb = X + (b == 0 ? bo.ve : b == 1 ? bo.vo : b == 2 ? bo.we : bo.wo);
+        double acc[CH][2];
+#pragma unroll
+        for (int m = 0; m < CH; ++m) acc[m][0] = acc[m][1] = 0.0;
+#pragma unroll 4
+        for (int c = r0; c < n; ++c) {
+          double xv = __ldg(Xb + (size_t)c * n + row);
+#pragma unroll
+          for (int m = 0; m < CH; ++m) {
+            cd rr = rhs[(m * 4 + b) * NZ + c];
+            acc[m][0] = fma(xv, rr.re, acc[m][0]);
+            acc[m][1] = fma(xv, rr.im, acc[m][1]);
+          }
+        }
+        int j = (b == 0 || b == 2) ? 2 * row : 2 * row + 1;
+        cd* dst = b < 2 ? s.cv : s.co;
+#pragma unroll
+        for (int m = 0; m < CH; ++m)
+          if (m < nm) dst[m * NZ + j] = cd{acc[m][0], acc[m][1]};
+      }
+    }
+    __syncthreads();
+    // ---- F: store, then getvelocityandvorticity (REF:2347-2407)
+    if (mean) {
+      for (int t = tid; t < nm * NZ; t += blockDim.x) {
+        int m = t / NZ, n = t % NZ;
+        cd x = s.co[t];
+        double* am = m == 0 ? a.au0 : a.w0;
         am[2 * n] = x.re;
         am[2 * n + 1] = x.im;
-        vel[(size_t)n * modes] = x;
+        (m == 0 ? a.u : a.w)[(size_t)n * modes] = x;
       }
-      if (threadIdx.x == 0 || threadIdx.x == 32) {
-        const bool im = threadIdx.x == 32;
-        dser(reinterpret_cast<const double*>(s.x) + (im ? 1 : 0), 2, im ? s.di : s.dr, 1, N);
+      for (int task = warp; task < nm * 2; task += S_WARPS) {
+        int m = task / 2, comp = task % 2;
+        warp_deriv(reinterpret_cast<const double*>(s.co + m * NZ) + comp, 2, dslot(s, m, comp, NZ), 1, N);
       }
       __syncthreads();
-      for (int n = threadIdx.x; n <= N; n += blockDim.x)
-        vort[(size_t)n * modes] = cd{sg * s.dr[n], sg * s.di[n]};
+      for (int t = tid; t < nm * NZ; t += blockDim.x) {
+        int m = t / NZ, n = t % NZ;
+        const double sg = m == 0 ? -1.0 : 1.0;  // omega_z = -D au0, omega_x = D w0
+        (m == 0 ? a.oz : a.ox)[(size_t)n * modes] =
+            cd{sg * dslot(s, m, 0, NZ)[n], sg * dslot(s, m, 1, NZ)[n]};
+      }
       __syncthreads();
+      continue;
     }
-    return;
-  }
-  const double k2 = a.k2vals[g];
-  const double c3 = 3.0 * dt / 2.0, c1 = dt / 2.0;
-  for (int gi = a.group_start[g]; gi < a.group_start[g + 1]; ++gi) {
-    const int m = a.group_modes[gi];
-    const int kx = m % d.KX, ky = m / d.KX;
-    const double al = a.iapha[kx], be = a.ibeta[ky];
-    // ---- v equation (REF:253-330)
-    for (int n = threadIdx.x; n <= N; n += blockDim.x) {
-      size_t idx = (size_t)n * modes + m;
-      s.c[n] = a.v[idx];
-      cd rv = a.rv[idx], un = a.u[idx];
-      s.r[n] = cd{(c3 * rv.re - c1 * un.re) * 1.0, (c3 * rv.im - c1 * un.im) * 1.0};
+    for (int task = warp; task < nm * 2; task += S_WARPS) {  // Dv
+      int m = task / 2, comp = task % 2;
+      warp_deriv(reinterpret_cast<const double*>(s.cv + m * NZ) + comp, 2, dslot(s, m, comp, NZ), 1, N);
     }
     __syncthreads();
-    solve_eq(s, a, k2, X, true);
-    for (int n = threadIdx.x; n <= N; n += blockDim.x) a.v[(size_t)n * modes + m] = s.x[n];
-    // keep v^{n+1} for the recovery: Dv -> dr/di row 0 after the omega solve
-    for (int n = threadIdx.x; n <= N; n += blockDim.x) s.r[n] = s.x[n];
-    __syncthreads();
-    if (threadIdx.x == 0 || threadIdx.x == 32) {
-      const bool im = threadIdx.x == 32;
-      // Dv into derivative slot 3 (not used by the second-order solve)
-      dser(reinterpret_cast<const double*>(s.r) + (im ? 1 : 0), 2, (im ? s.di : s.dr) + 3 * NZ, 1, N);
+    // u, w into rv / rg (free now); v and omega_y stored
+    for (int t = tid; t < nm * NZ; t += blockDim.x) {
+      int m = t / NZ, n = t % NZ;
+      const int mode = a.group_modes[base + m];
+      const int kx = mode % d.KX, ky = mode / d.KX;
+      const double al = a.iapha[kx], be = a.ibeta[ky];
+      const double ik2 = 1.0 / k2;
+      cd vv = s.cv[t], oy = s.co[t];
+      cd dv{dslot(s, m, 0, NZ)[n], dslot(s, m, 1, NZ)[n]};
+      size_t idx = (size_t)n * modes + mode;
+      a.v[idx] = vv;
+      a.oy[idx] = oy;
+      cd u{(-1.0 * al * dv.im) * ik2 + (be * oy.im) * ik2, (al * dv.re) * ik2 - (be * oy.re) * ik2};
+      cd w{(-1.0 * dv.im * be) * ik2 - (1.0 * oy.im * al) * ik2, (be * dv.re) * ik2 + (al * oy.re) * ik2};
+      s.rv[t] = u;
+      s.rg[t] = w;
+      a.u[idx] = u;
+      a.w[idx] = w;
     }
     __syncthreads();
-    // park v^{n+1} and Dv in the even/odd rhs buffers' spare room is not
-    // possible in general, so keep them in registers of the owning threads:
-    // thread t owns coefficients n = t, t + blockDim.x, ...
-    cd vkeep[3], dvkeep[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      int n = threadIdx.x + q * blockDim.x;
-      if (n <= N) {
-        vkeep[q] = s.r[n];
-        dvkeep[q] = cd{s.dr[3 * NZ + n], s.di[3 * NZ + n]};
-      }
+    for (int task = warp; task < nm * 4; task += S_WARPS) {  // Du (re, im), Dw (re, im)
+      int m = task / 4, comp = task % 4;
+      const cd* src = (comp < 2) ? s.rv + m * NZ : s.rg + m * NZ;
+      warp_deriv(reinterpret_cast<const double*>(src) + (comp & 1), 2, dslot(s, m, 2 + comp, NZ), 1, N);
     }
     __syncthreads();
-    // ---- omega_y equation (REF:333-382)
-    for (int n = threadIdx.x; n <= N; n += blockDim.x) {
-      size_t idx = (size_t)n * modes + m;
-      s.c[n] = a.oy[idx];
-      cd rg = a.rg[idx], wn = a.w[idx];
-      s.r[n] = cd{(c3 * rg.re - c1 * wn.re) * 1.0, (c3 * rg.im - c1 * wn.im) * 1.0};
-    }
-    __syncthreads();
-    solve_eq(s, a, k2, X, false);
-    // ---- getvelocityandvorticity (REF:2347-2407)
-    // u = (i al Dv - i be oy) / k2, w = (i be Dv + i al oy) / k2
-    const double ik2 = 1.0 / k2;
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      int n = threadIdx.x + q * blockDim.x;
-      if (n <= N) {
-        cd oy = s.x[n];
-        cd dv = dvkeep[q];
-        a.oy[(size_t)n * modes + m] = oy;
-        cd u{(-1.0 * al * dv.im) * ik2 + (be * oy.im) * ik2, (al * dv.re) * ik2 - (be * oy.re) * ik2};
-        cd w{(-1.0 * dv.im * be) * ik2 - (1.0 * oy.im * al) * ik2, (be * dv.re) * ik2 + (al * oy.re) * ik2};
-        s.c[n] = u;   // u coefficients
-        s.e[n] = w;   // w coefficients (e has NZ room)
-      }
-    }
-    __syncthreads();
-    if (threadIdx.x < 64 && (threadIdx.x % 32) == 0) {
-      // thread 0: Du (re, im); thread 32: Dw (re, im)
-      const bool isw = threadIdx.x == 32;
-      const double* src = reinterpret_cast<const double*>(isw ? s.e : s.c);
-      double* dst_r = s.dr + (isw ? 1 : 0) * NZ;
-      double* dst_i = s.di + (isw ? 1 : 0) * NZ;
-      dser(src, 2, dst_r, 1, N);
-      dser(src + 1, 2, dst_i, 1, N);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      int n = threadIdx.x + q * blockDim.x;
-      if (n <= N) {
-        size_t idx = (size_t)n * modes + m;
-        cd v = vkeep[q];
-        a.u[idx] = s.c[n];
-        a.w[idx] = s.e[n];
-        // omega_x = Dw - i be v ; omega_z = -Du + i al v
-        a.ox[idx] = cd{s.dr[NZ + n] + be * v.im, s.di[NZ + n] - be * v.re};
-        a.oz[idx] = cd{-s.dr[n] - al * v.im, -s.di[n] + al * v.re};
-      }
+    for (int t = tid; t < nm * NZ; t += blockDim.x) {
+      int m = t / NZ, n = t % NZ;
+      const int mode = a.group_modes[base + m];
+      const int kx = mode % d.KX, ky = mode / d.KX;
+      const double al = a.iapha[kx], be = a.ibeta[ky];
+      cd vv = s.cv[t];
+      size_t idx = (size_t)n * modes + mode;
+      double dur = dslot(s, m, 2, NZ)[n], dui = dslot(s, m, 3, NZ)[n];
+      double dwr = dslot(s, m, 4, NZ)[n], dwi = dslot(s, m, 5, NZ)[n];
+      // omega_x = Dw - i be v ; omega_z = -Du + i al v
+      a.ox[idx] = cd{dwr + be * vv.im, dwi - be * vv.re};
+      a.oz[idx] = cd{-dur - al * vv.im, -dui + al * vv.re};
     }
     __syncthreads();
   }
@@ -454,10 +493,14 @@ __global__ void __launch_bounds__(S_THREADS) k_solve(const __grid_constant__ Sol
 __global__ void k_diag(const double* __restrict__ u, const double* __restrict__ v,
                        const double* __restrict__ w, const double* __restrict__ f4,
                        const double* __restrict__ f5, const double* __restrict__ f6, size_t n,
-                       double* out) {
+                       long modes, int KX, int NYQ, double* out) {
   double e = 0.0, mx = 0.0;
   unsigned long long bad = 0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    // the spanwise Nyquist slot is never part of the solution (it is zeroed
+    // before every transform, REF:739, 811, 1358); skip it
+    long mode = (long)((i >> 1) % (size_t)modes);
+    if (mode / KX == NYQ) continue;
     double a = u[i], b = v[i], c = w[i];
     e += 0.5 * (a * a) + 0.5 * (b * b) + 0.5 * (c * c);
     const double vals[6] = {a, b, c, f4[i], f5[i], f6[i]};
@@ -623,11 +666,12 @@ int launch_solve_fp64(Handle* h) {
   a.pz2 = h->pz2;
   a.tw2 = h->tw_z2;
   a.nk2 = h->nk2;
-  if (d.NZ > 3 * S_THREADS || !fft_fits(1, 2 * d.N, S_THREADS, 2)) {
+  if (d.N + 1 > 32 * 8 || !fft_fits(2 * CH, 2 * d.N, S_THREADS, 2)) {
     h->err = "k_solve: nnz too large for the launch shape";
     return CHF_E_INVALID;
   }
-  size_t smem = sizeof(cd) * (5 * (size_t)d.NZ + 2 * (size_t)d.N) + sizeof(double) * 8 * (size_t)d.NZ;
+  size_t smem = sizeof(cd) * (4 * (size_t)CH * d.NZ + 2 * (size_t)CH * 2 * d.N) +
+                sizeof(double) * 10 * (size_t)CH * d.NZ;
   if (smem > 48 * 1024 &&
       !cuda_ok(h, cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                "k_solve smem"))
@@ -649,7 +693,8 @@ int launch_diagnostics(Handle* h, chf_diag* out) {
   k_diag<<<4 * 152, 256, 0, h->stream>>>(
       reinterpret_cast<const double*>(h->f[F_U]), reinterpret_cast<const double*>(h->f[F_V]),
       reinterpret_cast<const double*>(h->f[F_W]), reinterpret_cast<const double*>(h->f[F_OX]),
-      reinterpret_cast<const double*>(h->f[F_OY]), reinterpret_cast<const double*>(h->f[F_OZ]), n, s);
+      reinterpret_cast<const double*>(h->f[F_OY]), reinterpret_cast<const double*>(h->f[F_OZ]), n,
+      d.modes(), d.KX, d.NYQ, s);
   if (!cuda_ok(h, cudaGetLastError(), "k_diag")) return CHF_E_CUDA;
   double host[3];
   std::vector<double> au0(2 * (size_t)d.NZ);

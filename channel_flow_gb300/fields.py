@@ -231,3 +231,75 @@ def lowmode_state(cfg: ChannelConfig, seed: int = 0, amp: float = 1e-3, nmodes: 
     st["omegaznp1"][1, 0, 0] = 2.0 * gamma
     _set_mean(cfg, st)
     return st
+
+
+def _cheb_values_matrix(n: int) -> np.ndarray:
+    k = np.arange(n + 1)
+    return np.cos(np.pi * np.outer(k, k) / n)  # [point, coefficient]
+
+
+def turbulent_start_state(cfg: ChannelConfig, seed: int = 0, u_centre: float = None,
+                          frac: float = 0.1, mode_frac: float = 0.25, deg_frac: float = 0.25) -> dict:
+    """Laminar profile u_centre (1 - z^2) plus a seeded divergence-free
+    perturbation whose rms velocity is ``frac * u_centre``.
+
+    The perturbation lives in the lowest ``mode_frac`` of the streamwise and
+    spanwise modes; its wall-normal profiles are (1 - z^2)^2 P(z) for v and
+    (1 - z^2) Q(z) for omega_y with random Chebyshev series P, Q of degree
+    ``deg_frac * nnz`` (decaying spectrum), so every wall condition holds;
+    u, w, omega_x, omega_z follow from getvelocityandvorticity.  The default
+    u_centre is the laminar centreline re*re_p/2 when that is O(1) (channels
+    scaled by the laminar centreline speed) and otherwise the turbulent
+    centreline 2.5 ln(Re_tau) + 5.5 in wall units (u_tau = sqrt(re_p))."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    n = cfg.nnz
+    z = zpoints(n)
+    if u_centre is None:
+        lam = cfg.re * cfg.re_p / 2.0
+        if lam <= 2.0:
+            u_centre = lam
+        else:
+            re_tau = cfg.re * np.sqrt(cfg.re_p)
+            u_centre = 2.5 * np.log(re_tau) + 5.5
+    st = empty_state(cfg)
+    M = _dct1_matrix(n)
+    deg = max(2, min(int(deg_frac * n), n - 4))
+    nkx = max(1, int(mode_frac * cfg.kx))
+    nky = max(1, int(mode_frac * cfg.nny / 2))
+    v = as_complex(st["vnp1"])
+    oy = as_complex(st["omegaynp1"])
+    damp = np.exp(-np.arange(deg + 1) / max(1.0, deg / 3.0))
+    wv = (1.0 - z * z) ** 2
+    wo = 1.0 - z * z
+    for i in range(nkx):
+        for jj in range(-(nky - 1), nky):
+            if i == 0 and jj <= 0:
+                continue  # kx = 0: fill jj > 0, mirror below
+            j = jj % cfg.nny
+            cv = (rng.standard_normal(deg + 1) + 1j * rng.standard_normal(deg + 1)) * damp
+            co = (rng.standard_normal(deg + 1) + 1j * rng.standard_normal(deg + 1)) * damp
+            v[:, j, i] = M @ (wv * np.polynomial.chebyshev.chebval(z, cv))
+            oy[:, j, i] = M @ (wo * np.polynomial.chebyshev.chebval(z, co))
+    for jj in range(1, nky):
+        v[:, (-jj) % cfg.nny, 0] = np.conj(v[:, jj, 0])
+        oy[:, (-jj) % cfg.nny, 0] = np.conj(oy[:, jj, 0])
+    recover_velocity(cfg, st)
+    # physical mean square of the perturbation velocity (Parseval in x, y;
+    # kx > 0 modes stand for their conjugate partners too)
+    T = _cheb_values_matrix(n)
+    ms = 0.0
+    for name in ("unp1", "vnp1", "wnp1"):
+        vals = np.tensordot(T, as_complex(st[name]), axes=(1, 0))
+        p = np.abs(vals) ** 2
+        p[:, :, 1:] *= 2.0
+        ms += p.sum(axis=(1, 2)).mean()
+    scale = frac * u_centre / np.sqrt(ms / 3.0) if ms > 0 else 0.0
+    for name in ("vnp1", "omegaynp1", "unp1", "wnp1", "omegaxnp1", "omegaznp1"):
+        st[name] *= scale
+    st["unp1"][:, 0, :2] = 0.0
+    st["omegaznp1"][:, 0, :2] = 0.0
+    st["unp1"][0, 0, 0] = 0.5 * u_centre
+    st["unp1"][2, 0, 0] = -0.5 * u_centre
+    st["omegaznp1"][1, 0, 0] = 2.0 * u_centre
+    _set_mean(cfg, st)
+    return st

@@ -65,11 +65,12 @@ typedef struct chf_handle chf_handle;
 
 /* Diagnostics of the current state (spectral, Parseval). */
 typedef struct chf_diag {
-  double energy;        /* 0.5 * sum over modes and z-coefficients of |u|^2+|v|^2+|w|^2,
-                           the spectral sum printed at poiseuilleflow.f90:2322-2336 */
+  double energy;        /* 0.5 * sum over the spectral arrays of u^2 + v^2 + w^2 (the sum
+                           printed at poiseuilleflow.f90:2322-2336), spanwise Nyquist
+                           slot excluded */
   double wall_shear_top;    /* d<u>/dz at z = +1 from au0 */
   double wall_shear_bottom; /* d<u>/dz at z = -1 from au0 */
-  double max_abs;       /* max |value| over the prognostic fields */
+  double max_abs;       /* max |value| over the six velocity/vorticity fields (no Nyquist slot) */
   int finite;           /* 1 if every value is finite */
 } chf_diag;
 
