@@ -309,6 +309,37 @@ def main():
            "d2h_bytes_per_step": sum(a.nbytes for a in out.values()),
            "what": "chf_upload_state (all module arrays, pinned host) + chf_step(1) + chf_download_state"}
     ch.close()
+    # accuracy of the mixed form: the same start advanced by the FP64 path
+    accuracy = None
+    if args.precision == "mixed":
+        total = 1 + max(3, args.warmup) + args.steps
+        ref = Channel(cfg, precision="fp64", zpad=args.zpad, device=local)
+        ref.upload_state(st)
+        ref.getnonlinear()
+        ref.solve()
+        ref.profile(True)
+        ref.profile_reset()
+        ref.step(total - 1)
+        fp64_prof = ref.profile_report()
+        a = ref.download_state()
+        ref.close()
+        mix = Channel(cfg, precision="mixed", zpad=args.zpad, device=local)
+        mix.upload_state(st)
+        mix.getnonlinear()
+        mix.solve()
+        mix.step(total - 1)
+        b = mix.download_state()
+        mix.close()
+        nyq = cfg.nny // 2
+        errs = {}
+        for k in ("unp1", "vnp1", "wnp1", "omegaynp1"):
+            pa = np.delete(a[k], nyq, axis=1)
+            pb = np.delete(b[k], nyq, axis=1)
+            errs[k] = float(np.linalg.norm(pb - pa) / np.linalg.norm(pa))
+        fp64_ms = sum(v[1] for v in fp64_prof.values()) / max(1, total - 1)
+        accuracy = {"steps": total, "rel_l2_vs_fp64": errs, "max_rel_l2": max(errs.values()),
+                    "fp64_steps_per_s": 1e3 / fp64_ms if fp64_ms > 0 else None,
+                    "fp64_ms_per_step_kernels": fp64_ms}
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -340,7 +371,7 @@ def main():
         "metric": "steps/s", "value": value, "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32+bf16x2 transforms, f64 solves",
+        "dtype": "f64" if args.precision == "fp64" else "f32 FFTs/products + bf16x3 tcgen05 GEMMs (f32 accum) + f64 solves",
         "data": "synthetic (seeded laminar profile + 10% divergence-free perturbation)",
         "config": {"workload": workload_name(cfg, args.precision, args.zpad),
                    "grid_points": cfg.points, "precision": args.precision,
@@ -354,6 +385,8 @@ def main():
         "kernels": kernels,
         "energy_after": diag["energy"],
     }
+    if accuracy is not None:
+        line["accuracy"] = accuracy
     if world == 1 and not args.no_cpu_baseline:
         rate, threads, steps, el = cpu_reference_rate(cfg, args.cpu_seconds)
         line["cpu_baseline"] = {

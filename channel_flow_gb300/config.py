@@ -58,8 +58,11 @@ CONFIGS = {
     "c1_poiseuille_32": ChannelConfig(32, 32, 32, 1.0, 0.5, 1e-3, 2000.0, _laminar_rep(2000.0)),
     # 16 x 65 x 4, box 2pi x 2 x 2pi, Re_c = 7500, dt = 1e-3.
     "c2_orr_sommerfeld": ChannelConfig(16, 4, 64, 1.0, 1.0, 1e-3, 7500.0, _laminar_rep(7500.0)),
-    # 128 x 129 x 128, box 4pi x 2 x 4pi/3, Re_tau = 180 (re = 180, re_p = 1), dt = 5e-4.
-    "c3_retau180_128": ChannelConfig(128, 128, 128, 2.0, 2.0 / 3.0, 5e-4, 180.0, 1.0),
+    # 128 x 129 x 128, box 4pi x 2 x 4pi/3, Re_tau = 180 (re = 180, re_p = 1).  dt = 2e-4 as in
+    # the reference's own run (paraandcons.f90:23): at dt = 5e-4 the reference algorithm
+    # diverges within ~45 steps from a 10% perturbation at this resolution (the highest
+    # streamwise, spanwise and Chebyshev modes grow about tenfold per step).
+    "c3_retau180_128": ChannelConfig(128, 128, 128, 2.0, 2.0 / 3.0, 2e-4, 180.0, 1.0),
     # 384 x 193 x 384, box 2pi x 2 x pi, Re_tau = 550, dt = 2e-4.
     "c4_retau550_384": ChannelConfig(384, 384, 192, 1.0, 0.5, 2e-4, 550.0, 1.0),
 }

@@ -47,8 +47,10 @@ static std::vector<cd> twiddles(int L) {
   return t;
 }
 
-const char* const kKernelNames[K_COUNT] = {"k_zc2v", "k_yinv", "k_xprod", "k_yfwd",
-                                           "k_zcurl", "k_solve", "k_diag"};
+const char* const kKernelNames[K_COUNT] = {
+    "k_zc2v", "k_yinv", "k_xprod", "k_yfwd", "k_zcurl", "k_solve", "k_diag",
+    "k_tc_split_z1", "k_tc_gemm_z1", "k_tc_split_z2", "k_tc_gemm_z2", "k_curl32", "k_tc_gemm_gl",
+    "k_meanfix"};
 
 static cudaEvent_t take_event(Handle* h) {
   if (!h->event_pool.empty()) {
@@ -123,7 +125,8 @@ static void release(chf_handle* h) {
   for (auto& p : h->mean) cudaFree(p);
   void* ptrs[] = {h->iapha, h->ibeta, h->t0, h->t2, h->t4, h->k2vals, h->xinv, h->xmean,
                   h->group_start, h->group_modes, h->tw_py, h->tw_px, h->tw_z2, h->tw_zm,
-                  h->twf_py, h->twf_px, h->wz, h->wy, h->scratch};
+                  h->twf_py, h->twf_px, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
+                  h->agl, h->bimg, h->wz32, h->wy32, h->lc32};
   for (void* p : ptrs) cudaFree(p);
   for (auto& p : h->pending) {
     cudaEventDestroy(p.a);
@@ -144,10 +147,6 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
   std::string why = validate(cfg);
   if (!why.empty()) {
     g_create_error = why;
-    return CHF_E_INVALID;
-  }
-  if (cfg->precision == CHF_MIXED) {
-    g_create_error = "CHF_MIXED is not available in this build";
     return CHF_E_INVALID;
   }
   chf_handle* h = new (std::nothrow) chf_handle();
@@ -199,10 +198,15 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
       return fail(CHF_E_NOMEM);
     cudaMemsetAsync(h->mean[i], 0, sizeof(double) * 2 * d.NZ, h->stream);
   }
-  const size_t wz_elems = (size_t)6 * d.MP * d.modes();
-  const size_t wy_elems = (size_t)6 * d.MP * d.PY * d.KX;
-  if (!cuda_ok(h, cudaMalloc((void**)&h->wz, sizeof(cd) * wz_elems), "work alloc") ||
-      !cuda_ok(h, cudaMalloc((void**)&h->wy, sizeof(cd) * wy_elems), "work alloc"))
+  if (cfg->precision == CHF_FP64) {
+    const size_t wz_elems = (size_t)6 * d.MP * d.modes();
+    const size_t wy_elems = (size_t)6 * d.MP * d.PY * d.KX;
+    if (!cuda_ok(h, cudaMalloc((void**)&h->wz, sizeof(cd) * wz_elems), "work alloc") ||
+        !cuda_ok(h, cudaMalloc((void**)&h->wy, sizeof(cd) * wy_elems), "work alloc"))
+      return fail(CHF_E_NOMEM);
+  }
+  if (!cuda_ok(h, cudaMalloc((void**)&h->dev_status, sizeof(int)), "status alloc") ||
+      !cuda_ok(h, cudaMemsetAsync(h->dev_status, 0, sizeof(int), h->stream), "status init"))
     return fail(CHF_E_NOMEM);
   h->scratch_bytes = 4096;
   if (!cuda_ok(h, cudaMalloc(&h->scratch, h->scratch_bytes), "scratch alloc")) return fail(CHF_E_NOMEM);
@@ -223,7 +227,11 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
   }
   int rc = setup_solver(h);
   if (rc != CHF_OK) return fail(rc);
-  h->kernels_per_step = 6;
+  if (cfg->precision == CHF_MIXED) {
+    rc = setup_mixed(h);
+    if (rc != CHF_OK) return fail(rc);
+  }
+  h->kernels_per_step = cfg->precision == CHF_MIXED ? 11 : 6;
   if (!cuda_ok(h, cudaStreamSynchronize(h->stream), "create sync")) return fail(CHF_E_CUDA);
   *out = h;
   return CHF_OK;
@@ -292,7 +300,7 @@ int chf_getnonlinear(chf_handle* h) {
     return CHF_E_STATE;
   }
   if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
-  return launch_nonlinear_fp64(h);
+  return h->cfg.precision == CHF_MIXED ? launch_nonlinear_mixed(h) : launch_nonlinear_fp64(h);
 }
 
 int chf_solve(chf_handle* h) {
@@ -320,12 +328,27 @@ int chf_step(chf_handle* h, int nsteps) {
   return CHF_OK;
 }
 
+// Device-side error word: tensor-core kernels record a bounded-wait timeout
+// there (11: operand copy, 12: MMA completion) instead of hanging.
+static int check_status(chf_handle* h) {
+  int st = 0;
+  if (!cuda_ok(h, cudaMemcpyAsync(&st, h->dev_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream),
+               "status read") ||
+      !cuda_ok(h, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))
+    return CHF_E_CUDA;
+  if (st != 0) {
+    h->err = "tensor-core pipeline wait timed out (code " + std::to_string(st) + ")";
+    return CHF_E_CUDA;
+  }
+  return CHF_OK;
+}
+
 int chf_synchronize(chf_handle* h) {
   if (!h) return CHF_E_INVALID;
   if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice") ||
       !cuda_ok(h, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))
     return CHF_E_CUDA;
-  return CHF_OK;
+  return check_status(h);
 }
 
 int chf_diagnostics(chf_handle* h, chf_diag* out) {
@@ -333,6 +356,7 @@ int chf_diagnostics(chf_handle* h, chf_diag* out) {
   if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
   int rc = launch_diagnostics(h, out);
   if (rc == CHF_E_NUMERIC) h->err = "non-finite values in the state";
+  if (rc == CHF_OK) rc = check_status(h);
   return rc;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <string>
 #include <vector>
 
@@ -30,6 +31,23 @@ struct Dims {
   int MP;   // product-grid points = MZ + 1
   __host__ __device__ long modes() const { return (long)KX * KY; }
   __host__ __device__ size_t field_elems() const { return (size_t)NZ * KY * KX; }  // complex elements
+};
+
+// Tensor-core GEMM plan (k_tcgemm.cu): 128 x 128 output tiles, K in chunks
+// of at most TC_KC, operands split into TC_SPLITS bf16 planes.
+constexpr int TC_KC = 64;
+constexpr int TC_SPLITS = 3;
+struct TcPlan {
+  int mvalid, mtiles, kpad, ntiles, nchunks;
+  long ncols;
+  int kc[16];
+  size_t chunk_off[16];
+  size_t tile_bytes;  // bytes of one 128-row/column tile image (all chunks and planes)
+};
+
+template <typename T>
+struct Ptr8 {
+  T* p[8];
 };
 
 // Even/odd split of the collocation operators (see k_solve.cu).
@@ -77,6 +95,16 @@ struct Handle {
   void* scratch = nullptr;  // reduction scratch (diagnostics)
   size_t scratch_bytes = 0;
 
+  // mixed-precision path (k_mixed.cu): FP32 transforms, tcgen05 GEMMs
+  int* dev_status = nullptr;  // device error word (tensor-core pipeline timeouts)
+  TcPlan tz1{}, tz2{}, tgl{};
+  uint8_t *az1 = nullptr, *az2 = nullptr, *agl = nullptr;  // constant A images
+  uint8_t* bimg = nullptr;    // per-step B images
+  size_t bimg_bytes = 0;
+  cf* wz32 = nullptr;         // 6 x [MP][KY][KX]
+  cf* wy32 = nullptr;         // 6 x [MP][PY][KX]
+  float* lc32 = nullptr;      // 3 x [NZ][2 modes] Lamb-vector coefficients
+
   // statistics
   int kernels_per_step = 0;
   cudaStream_t own_stream = nullptr;
@@ -98,7 +126,10 @@ struct Handle {
 };
 
 // Kernel ids for profiling.
-enum KernelId { K_ZC2V = 0, K_YINV, K_XPROD, K_YFWD, K_ZCURL, K_SOLVE, K_DIAG, K_COUNT };
+enum KernelId {
+  K_ZC2V = 0, K_YINV, K_XPROD, K_YFWD, K_ZCURL, K_SOLVE, K_DIAG,
+  K_SPLIT_Z1, K_GEMM_Z1, K_SPLIT_Z2, K_GEMM_Z2, K_CURL32, K_GEMM_GL, K_MEANFIX, K_COUNT
+};
 extern const char* const kKernelNames[K_COUNT];
 
 // Bracket one launch with events when profiling is on.
@@ -109,6 +140,19 @@ bool cuda_ok(Handle* h, cudaError_t e, const char* what);
 
 // launchers (k_nonlinear.cu)
 int launch_nonlinear_fp64(Handle* h);
+template <typename T>
+int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const cplx<T>* tw_px);
+// launchers (k_tcgemm.cu, k_mixed.cu)
+TcPlan make_tc_plan(int mvalid, int kvalid, long ncols);
+std::vector<uint8_t> make_a_image(const TcPlan& p, const std::vector<double>& a, int M, int K);
+template <typename OutT>
+int launch_tc_gemm(Handle* h, const TcPlan& p, const uint8_t* aimg, const uint8_t* bimg,
+                   size_t bfield_stride, const Ptr8<OutT>& outs, int nfields, size_t ldc, int kid);
+template <typename InT>
+int launch_tc_split(Handle* h, const TcPlan& p, const Ptr8<const InT>& ins, int kvalid, uint8_t* bimg,
+                    size_t bfield_stride, int nfields, int kid);
+int setup_mixed(Handle* h);
+int launch_nonlinear_mixed(Handle* h);
 // launchers (k_solve.cu)
 int setup_solver(Handle* h);
 int launch_solve_fp64(Handle* h);

@@ -94,17 +94,17 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zc2v(SixPtr in, cd* __restrict__
 // y inverse: per (field, plane p, group of kxb streamwise modes).
 // grid (KX / kxb, MP, 6)
 // ---------------------------------------------------------------------------
-template <int MB2>
-__global__ void __launch_bounds__(Y_THREADS) k_yinv(const cd* __restrict__ wz, cd* __restrict__ wy,
+template <typename T, int MB2>
+__global__ void __launch_bounds__(Y_THREADS) k_yinv(const cplx<T>* __restrict__ wz, cplx<T>* __restrict__ wy,
                                                     Dims d, int kxb, const __grid_constant__ FftPlan py,
-                                                    const cd* __restrict__ tw) {
+                                                    const cplx<T>* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cd* s = reinterpret_cast<cd*>(smem_raw);
+  cplx<T>* s = reinterpret_cast<cplx<T>*>(smem_raw);
   const int ls = d.PY + 1;
   const int f = blockIdx.z, p = blockIdx.y, kx0 = blockIdx.x * kxb;
   const long modes = d.modes();
-  const cd* __restrict__ src = wz + ((size_t)f * d.MP + p) * modes;
-  for (int t = threadIdx.x; t < kxb * ls; t += blockDim.x) s[t] = cd{0.0, 0.0};
+  const cplx<T>* __restrict__ src = wz + ((size_t)f * d.MP + p) * modes;
+  for (int t = threadIdx.x; t < kxb * ls; t += blockDim.x) s[t] = cplx<T>{(T)0, (T)0};
   __syncthreads();
   for (int t = threadIdx.x; t < kxb * d.KY; t += blockDim.x) {
     int l = t % kxb, ky = t / kxb;
@@ -113,8 +113,8 @@ __global__ void __launch_bounds__(Y_THREADS) k_yinv(const cd* __restrict__ wz, c
     s[l * ls + slot] = src[(size_t)ky * d.KX + kx0 + l];
   }
   __syncthreads();
-  smem_fft<double, +1, MB2>(s, kxb, ls, py, tw);
-  cd* __restrict__ dst = wy + ((size_t)f * d.MP + p) * (size_t)d.PY * d.KX;
+  smem_fft<T, +1, MB2>(s, kxb, ls, py, tw);
+  cplx<T>* __restrict__ dst = wy + ((size_t)f * d.MP + p) * (size_t)d.PY * d.KX;
   for (int t = threadIdx.x; t < kxb * d.PY; t += blockDim.x) {
     int l = t % kxb, yp = t / kxb;
     dst[(size_t)yp * d.KX + kx0 + l] = s[l * ls + yp];
@@ -126,61 +126,62 @@ __global__ void __launch_bounds__(Y_THREADS) k_yinv(const cd* __restrict__ wz, c
 // of six fields (u, v, w, ox, oy, oz), written back in place as H1, H2, H3
 // into field slots 0, 1, 2.  grid (ceil(MP * PY / X_ROWS))
 // ---------------------------------------------------------------------------
-template <int MB2>
-__global__ void __launch_bounds__(X_THREADS) k_xprod(cd* __restrict__ wy, Dims d, double re_p,
-                                                     const __grid_constant__ FftPlan px, const cd* __restrict__ tw) {
+template <typename T, int MB2>
+__global__ void __launch_bounds__(X_THREADS) k_xprod(cplx<T>* __restrict__ wy, Dims d, T re_p,
+                                                     const __grid_constant__ FftPlan px, const cplx<T>* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cd* s = reinterpret_cast<cd*>(smem_raw);
+  using C = cplx<T>;
+  C* s = reinterpret_cast<C*>(smem_raw);
   const int PX = d.PX, KX = d.KX, ls = PX + 1;
   const long nrows = (long)d.MP * d.PY;
   const long r0 = (long)blockIdx.x * X_ROWS;
   const size_t fstride = (size_t)d.MP * d.PY * KX;
   // lines: row q, pair c (0: u+iv, 1: w+i ox, 2: oy+i oz) at (c*X_ROWS + q) * ls
-  for (int t = threadIdx.x; t < X_ROWS * 3 * ls; t += blockDim.x) s[t] = cd{0.0, 0.0};
+  for (int t = threadIdx.x; t < X_ROWS * 3 * ls; t += blockDim.x) s[t] = C{(T)0, (T)0};
   __syncthreads();
   for (int t = threadIdx.x; t < X_ROWS * 3 * KX; t += blockDim.x) {
     int k = t % KX, c = (t / KX) % 3, q = t / (3 * KX);
     long r = r0 + q;
     if (r >= nrows) continue;
-    cd F = wy[(size_t)(2 * c) * fstride + (size_t)r * KX + k];
-    cd G = wy[(size_t)(2 * c + 1) * fstride + (size_t)r * KX + k];
-    cd* line = s + (c * X_ROWS + q) * ls;
+    C F = wy[(size_t)(2 * c) * fstride + (size_t)r * KX + k];
+    C G = wy[(size_t)(2 * c + 1) * fstride + (size_t)r * KX + k];
+    C* line = s + (c * X_ROWS + q) * ls;
     if (k == 0) {
-      line[0] = cd{F.re, G.re};  // imaginary part of the streamwise mean dropped
+      line[0] = C{F.re, G.re};  // imaginary part of the streamwise mean dropped
     } else {
-      line[k] = cd{F.re - G.im, F.im + G.re};        // F + i G
-      line[PX - k] = cd{F.re + G.im, G.re - F.im};   // conj(F) + i conj(G)
+      line[k] = C{F.re - G.im, F.im + G.re};        // F + i G
+      line[PX - k] = C{F.re + G.im, G.re - F.im};   // conj(F) + i conj(G)
     }
   }
   __syncthreads();
-  smem_fft<double, +1, MB2>(s, X_ROWS * 3, ls, px, tw);
+  smem_fft<T, +1, MB2>(s, X_ROWS * 3, ls, px, tw);
   // products at every physical point; write (H1 + i H2) to pair 0, (H3 + 0i) to pair 1
   for (int t = threadIdx.x; t < X_ROWS * PX; t += blockDim.x) {
     int x = t % PX, q = t / PX;
-    cd a = s[(0 * X_ROWS + q) * ls + x];  // u, v
-    cd b = s[(1 * X_ROWS + q) * ls + x];  // w, ox
-    cd c = s[(2 * X_ROWS + q) * ls + x];  // oy, oz
-    double u = a.re, v = a.im, w = b.re, ox = b.im, oy = c.re, oz = c.im;
-    double h1 = (oy * w - re_p) - oz * v;
-    double h2 = oz * u - ox * w;
-    double h3 = ox * v - oy * u;
-    s[(0 * X_ROWS + q) * ls + x] = cd{h1, h2};
-    s[(1 * X_ROWS + q) * ls + x] = cd{h3, 0.0};
+    C a = s[(0 * X_ROWS + q) * ls + x];  // u, v
+    C b = s[(1 * X_ROWS + q) * ls + x];  // w, ox
+    C c = s[(2 * X_ROWS + q) * ls + x];  // oy, oz
+    T u = a.re, v = a.im, w = b.re, ox = b.im, oy = c.re, oz = c.im;
+    T h1 = (oy * w - re_p) - oz * v;
+    T h2 = oz * u - ox * w;
+    T h3 = ox * v - oy * u;
+    s[(0 * X_ROWS + q) * ls + x] = C{h1, h2};
+    s[(1 * X_ROWS + q) * ls + x] = C{h3, (T)0};
   }
   __syncthreads();
   // forward DFT of the 2 * X_ROWS lines holding (H1 + i H2) and H3
-  smem_fft<double, -1, MB2>(s, X_ROWS * 2, ls, px, tw);
+  smem_fft<T, -1, MB2>(s, X_ROWS * 2, ls, px, tw);
   for (int t = threadIdx.x; t < X_ROWS * KX; t += blockDim.x) {
     int k = t % KX, q = t / KX;
     long r = r0 + q;
     if (r >= nrows) continue;
-    const cd* z = s + (0 * X_ROWS + q) * ls;
-    cd A = z[k];
-    cd B = z[k == 0 ? 0 : PX - k];
+    const C* z = s + (0 * X_ROWS + q) * ls;
+    C A = z[k];
+    C B = z[k == 0 ? 0 : PX - k];
     B.im = -B.im;  // conj(Z[-k])
-    cd H1{0.5 * (A.re + B.re), 0.5 * (A.im + B.im)};
-    cd H2{0.5 * (A.im - B.im), -0.5 * (A.re - B.re)};
-    cd H3 = s[(1 * X_ROWS + q) * ls + k];
+    C H1{(T)0.5 * (A.re + B.re), (T)0.5 * (A.im + B.im)};
+    C H2{(T)0.5 * (A.im - B.im), (T)-0.5 * (A.re - B.re)};
+    C H3 = s[(1 * X_ROWS + q) * ls + k];
     wy[(size_t)0 * fstride + (size_t)r * KX + k] = H1;
     wy[(size_t)1 * fstride + (size_t)r * KX + k] = H2;
     wy[(size_t)2 * fstride + (size_t)r * KX + k] = H3;
@@ -192,28 +193,28 @@ __global__ void __launch_bounds__(X_THREADS) k_xprod(cd* __restrict__ wy, Dims d
 // slot receives padded mode +NYQ as in expand(-1), REF:751-761) and the
 // negative modes, scaled by 1/(PX PY).  grid (KX / kxb, MP, 3)
 // ---------------------------------------------------------------------------
-template <int MB2>
-__global__ void __launch_bounds__(Y_THREADS) k_yfwd(const cd* __restrict__ wy, cd* __restrict__ wz,
+template <typename T, int MB2>
+__global__ void __launch_bounds__(Y_THREADS) k_yfwd(const cplx<T>* __restrict__ wy, cplx<T>* __restrict__ wz,
                                                     Dims d, int kxb, const __grid_constant__ FftPlan py,
-                                                    const cd* __restrict__ tw, double scale) {
+                                                    const cplx<T>* __restrict__ tw, T scale) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cd* s = reinterpret_cast<cd*>(smem_raw);
+  cplx<T>* s = reinterpret_cast<cplx<T>*>(smem_raw);
   const int ls = d.PY + 1;
   const int f = blockIdx.z, p = blockIdx.y, kx0 = blockIdx.x * kxb;
   const long modes = d.modes();
-  const cd* __restrict__ src = wy + ((size_t)f * d.MP + p) * (size_t)d.PY * d.KX;
+  const cplx<T>* __restrict__ src = wy + ((size_t)f * d.MP + p) * (size_t)d.PY * d.KX;
   for (int t = threadIdx.x; t < kxb * d.PY; t += blockDim.x) {
     int l = t % kxb, yp = t / kxb;
     s[l * ls + yp] = src[(size_t)yp * d.KX + kx0 + l];
   }
   __syncthreads();
-  smem_fft<double, -1, MB2>(s, kxb, ls, py, tw);
-  cd* __restrict__ dst = wz + ((size_t)f * d.MP + p) * modes;
+  smem_fft<T, -1, MB2>(s, kxb, ls, py, tw);
+  cplx<T>* __restrict__ dst = wz + ((size_t)f * d.MP + p) * modes;
   for (int t = threadIdx.x; t < kxb * d.KY; t += blockDim.x) {
     int l = t % kxb, ky = t / kxb;
     int slot = ky <= d.NYQ ? ky : d.PY - d.KY + ky;
-    cd v = s[l * ls + slot];
-    dst[(size_t)ky * d.KX + kx0 + l] = cd{v.re * scale, v.im * scale};
+    cplx<T> v = s[l * ls + slot];
+    dst[(size_t)ky * d.KX + kx0 + l] = cplx<T>{v.re * scale, v.im * scale};
   }
 }
 
@@ -373,6 +374,57 @@ int pick_kxb(int KX) {
 
 }  // namespace
 
+template <typename T>
+int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const cplx<T>* tw_px) {
+  const Dims& d = h->d;
+  cudaStream_t st = h->stream;
+  const int kxb = pick_kxb(d.KX);
+  {
+    if (!fft_fits(kxb, d.PY, Y_THREADS, 6)) {
+      h->err = "k_yinv: FFT length too large for the launch shape";
+      return CHF_E_INVALID;
+    }
+    size_t smem = sizeof(cplx<T>) * kxb * (d.PY + 1);
+    if (!set_smem(h, k_yinv<T, 6>, smem)) return CHF_E_CUDA;
+    dim3 grid(d.KX / kxb, d.MP, 6);
+    cudaEvent_t ev;
+    prof_begin(h, K_YINV, &ev);
+    k_yinv<T, 6><<<grid, Y_THREADS, smem, st>>>(wz, wy, d, kxb, h->py, tw_py);
+    prof_end(h, K_YINV, ev);
+    if (!cuda_ok(h, cudaGetLastError(), "k_yinv")) return CHF_E_CUDA;
+  }
+  {
+    if (!fft_fits(X_ROWS * 3, d.PX, X_THREADS, 5)) {
+      h->err = "k_xprod: FFT length too large for the launch shape";
+      return CHF_E_INVALID;
+    }
+    size_t smem = sizeof(cplx<T>) * X_ROWS * 3 * (d.PX + 1);
+    if (!set_smem(h, k_xprod<T, 5>, smem)) return CHF_E_CUDA;
+    long nrows = (long)d.MP * d.PY;
+    dim3 grid((unsigned)((nrows + X_ROWS - 1) / X_ROWS));
+    cudaEvent_t ev;
+    prof_begin(h, K_XPROD, &ev);
+    k_xprod<T, 5><<<grid, X_THREADS, smem, st>>>(wy, d, (T)h->cfg.re_p, h->px, tw_px);
+    prof_end(h, K_XPROD, ev);
+    if (!cuda_ok(h, cudaGetLastError(), "k_xprod")) return CHF_E_CUDA;
+  }
+  {
+    size_t smem = sizeof(cplx<T>) * kxb * (d.PY + 1);
+    if (!set_smem(h, k_yfwd<T, 6>, smem)) return CHF_E_CUDA;
+    dim3 grid(d.KX / kxb, d.MP, 3);
+    T scale = (T)(1.0 / ((double)d.PX * (double)d.PY));
+    cudaEvent_t ev;
+    prof_begin(h, K_YFWD, &ev);
+    k_yfwd<T, 6><<<grid, Y_THREADS, smem, st>>>(wy, wz, d, kxb, h->py, tw_py, scale);
+    prof_end(h, K_YFWD, ev);
+    if (!cuda_ok(h, cudaGetLastError(), "k_yfwd")) return CHF_E_CUDA;
+  }
+  return CHF_OK;
+}
+
+template int launch_xy<double>(Handle*, cd*, cd*, const cd*, const cd*);
+template int launch_xy<float>(Handle*, cf*, cf*, const cf*, const cf*);
+
 int launch_nonlinear_fp64(Handle* h) {
   const Dims& d = h->d;
   cudaStream_t st = h->stream;
@@ -394,46 +446,9 @@ int launch_nonlinear_fp64(Handle* h) {
     prof_end(h, K_ZC2V, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_zc2v")) return CHF_E_CUDA;
   }
-  const int kxb = pick_kxb(d.KX);
   {
-    if (!fft_fits(kxb, d.PY, Y_THREADS, 6)) {
-      h->err = "k_yinv: FFT length too large for the launch shape";
-      return CHF_E_INVALID;
-    }
-    size_t smem = sizeof(cd) * kxb * (d.PY + 1);
-    if (!set_smem(h, k_yinv<6>, smem)) return CHF_E_CUDA;
-    dim3 grid(d.KX / kxb, d.MP, 6);
-    cudaEvent_t ev;
-    prof_begin(h, K_YINV, &ev);
-    k_yinv<6><<<grid, Y_THREADS, smem, st>>>(h->wz, h->wy, d, kxb, h->py, h->tw_py);
-    prof_end(h, K_YINV, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_yinv")) return CHF_E_CUDA;
-  }
-  {
-    if (!fft_fits(X_ROWS * 3, d.PX, X_THREADS, 5)) {
-      h->err = "k_xprod: FFT length too large for the launch shape";
-      return CHF_E_INVALID;
-    }
-    size_t smem = sizeof(cd) * X_ROWS * 3 * (d.PX + 1);
-    if (!set_smem(h, k_xprod<5>, smem)) return CHF_E_CUDA;
-    long nrows = (long)d.MP * d.PY;
-    dim3 grid((unsigned)((nrows + X_ROWS - 1) / X_ROWS));
-    cudaEvent_t ev;
-    prof_begin(h, K_XPROD, &ev);
-    k_xprod<5><<<grid, X_THREADS, smem, st>>>(h->wy, d, h->cfg.re_p, h->px, h->tw_px);
-    prof_end(h, K_XPROD, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_xprod")) return CHF_E_CUDA;
-  }
-  {
-    size_t smem = sizeof(cd) * kxb * (d.PY + 1);
-    if (!set_smem(h, k_yfwd<6>, smem)) return CHF_E_CUDA;
-    dim3 grid(d.KX / kxb, d.MP, 3);
-    double scale = 1.0 / ((double)d.PX * (double)d.PY);
-    cudaEvent_t ev;
-    prof_begin(h, K_YFWD, &ev);
-    k_yfwd<6><<<grid, Y_THREADS, smem, st>>>(h->wy, h->wz, d, kxb, h->py, h->tw_py, scale);
-    prof_end(h, K_YFWD, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_yfwd")) return CHF_E_CUDA;
+    int rc = launch_xy<double>(h, h->wz, h->wy, h->tw_py, h->tw_px);
+    if (rc != CHF_OK) return rc;
   }
   {
     const int L = 2 * d.MZ;

@@ -1,0 +1,96 @@
+"""Mixed-precision path (FP32 transforms and products, bf16x3 tcgen05 GEMMs
+for the wall-normal transforms, FP64 implicit solves) against the FP64 path
+and the oracle.  Bar: velocity rel-L2 <= 1e-5 against FP64 (the accuracy the
+mixed form must hold); the nonlinear term itself to 1e-5 after one call."""
+import numpy as np
+import pytest
+
+from channel_flow_gb300 import Channel, config, fields
+from parity import compare, rel_l2, split
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "small16": config.small(nnx=16, nny=8, nnz=16, aphi=1.0, beta=0.5, dt=5e-4, re=180.0, re_p=1.0),
+    "c1_32": config.CONFIGS["c1_poiseuille_32"],
+    "c2_os": config.CONFIGS["c2_orr_sommerfeld"],
+    "mixed_radix": config.small(nnx=24, nny=12, nnz=20, aphi=1.5, beta=0.75, dt=5e-4, re=300.0, re_p=1.0),
+}
+VEL = ("unp1", "vnp1", "wnp1")
+
+
+def vel_err(a, b):
+    out = {}
+    for k in VEL:
+        pa, pb = split(a[k], k)[k], split(b[k], k)[k]
+        out[k] = rel_l2(pa, pb)
+    return out
+
+
+def run(cfg, st, precision, nsteps, zpad=0):
+    with Channel(cfg, precision=precision, zpad=zpad) as g:
+        g.upload_state(st)
+        g.getnonlinear()
+        g.solve()
+        g.step(nsteps)
+        g.synchronize()
+        return g.download_state()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_mixed_nonlinear_term(chflow_lib, name):
+    cfg = CASES[name]
+    st = fields.turbulent_start_state(cfg, seed=2)
+    outs = {}
+    for prec in ("fp64", "mixed"):
+        with Channel(cfg, precision=prec) as g:
+            g.upload_state(st)
+            g.getnonlinear()
+            g.synchronize()
+            outs[prec] = g.download_state()
+    for k in ("rhsvn", "rhsomegayn"):
+        e = rel_l2(split(outs["mixed"][k], k)[k], split(outs["fp64"][k], k)[k])
+        assert e < 1e-5, (k, e)
+    for k in ("clamb1n", "clamb3n"):
+        e = np.linalg.norm(outs["mixed"][k] - outs["fp64"][k]) / max(np.linalg.norm(outs["fp64"][k]), 1e-30)
+        assert e < 1e-4, (k, e)
+
+
+@pytest.mark.parametrize("name,nsteps", [("small16", 50), ("c1_32", 50), ("c2_os", 50), ("mixed_radix", 30)])
+def test_mixed_steps_vs_fp64(chflow_lib, name, nsteps):
+    cfg = CASES[name]
+    st = fields.turbulent_start_state(cfg, seed=4)
+    a = run(cfg, st, "fp64", nsteps)
+    b = run(cfg, st, "mixed", nsteps)
+    errs = vel_err(b, a)
+    assert max(errs.values()) < 1e-5, errs
+
+
+def test_mixed_steps_vs_oracle(chflow_lib, oracle_mod):
+    cfg = CASES["c1_32"]
+    st = fields.lowmode_state(cfg, seed=5, amp=1e-2)
+    o = oracle_mod.Oracle.from_config(cfg)
+    o.setup()
+    o.set_state(st)
+    o.getnonlinear(); o.solve(); o.step(40)
+    b = run(cfg, st, "mixed", 40)
+    errs = vel_err(b, o.get_state())
+    assert max(errs.values()) < 1e-5, errs
+
+
+def test_mixed_zpad_auto_matches_default(chflow_lib):
+    cfg = CASES["small16"]
+    st = fields.turbulent_start_state(cfg, seed=6)
+    a = run(cfg, st, "mixed", 10, zpad=0)
+    b = run(cfg, st, "mixed", 10, zpad=25)
+    errs = vel_err(b, a)
+    assert max(errs.values()) < 1e-6, errs
+
+
+def test_mixed_full_size(chflow_lib):
+    cfg = config.CONFIGS["c3_retau180_128"]
+    st = fields.turbulent_start_state(cfg, seed=1)
+    a = run(cfg, st, "fp64", 20, zpad=200)
+    b = run(cfg, st, "mixed", 20, zpad=200)
+    errs = vel_err(b, a)
+    assert max(errs.values()) < 1e-5, errs
