@@ -15,8 +15,9 @@ import pytest
 
 from channel_flow_gb300 import Channel, ChannelError, config, fields
 from channel_flow_gb300.fields import FIELD_NAMES, MEAN_NAMES
+from exact_lamb import lamb
 from exact_mean import mean_h1
-from parity import check, compare, worst
+from parity import PROG, check, compare, worst
 
 pytestmark = pytest.mark.gpu
 
@@ -65,7 +66,35 @@ def test_getnonlinear_matches_oracle(chflow_lib, oracle_mod, name):
     o, g = pair(cfg, oracle_mod, st)
     o.getnonlinear()
     g.getnonlinear()
-    check(g.download_state(), o.get_state(), 1e-10, 1e-7)
+    gs, os_ = g.download_state(), o.get_state()
+    # omega_x / omega_z now hold H1 / H3, whose accuracy is pinned against
+    # extended precision in test_lamb_accuracy; every other array here
+    for k in ("omegaxnp1", "omegaznp1"):
+        gs.pop(k)
+        os_.pop(k)
+    errs = compare(gs, os_, names=tuple(k for k in os_))
+    bad = {k: e for k, e in errs.items() if e >= (1e-10 if k in PROG else 1e-7)}
+    assert not bad, (bad, errs)
+
+
+@pytest.mark.parametrize("name", ["small16", "c2_os", "mixed_radix"])
+def test_lamb_accuracy(chflow_lib, oracle_mod, name):
+    """H1, H3 (left in omega_x, omega_z by getnonlinear, REF:1489-1496)
+    against an extended-precision evaluation of the dealiased products: the
+    GPU must be at least as accurate as the reference algorithm (the oracle
+    is 2e-10 off for the Orr-Sommerfeld box, whose H1 is a near-cancelling
+    sum)."""
+    cfg = CASES[name]
+    st = make_state(cfg)
+    h1, h2, h3 = lamb(cfg, st)
+    o, g = pair(cfg, oracle_mod, st)
+    o.getnonlinear()
+    g.getnonlinear()
+    out = g.download_state()
+    for key, ex in (("omegaxnp1", h1), ("omegaznp1", h3)):
+        e_o = np.linalg.norm(o.field(key) - ex) / np.linalg.norm(ex)
+        e_g = np.linalg.norm(out[key] - ex) / np.linalg.norm(ex)
+        assert e_g <= max(2.0 * e_o, 1e-13), (key, e_g, e_o)
 
 
 @pytest.mark.parametrize("name", list(CASES))
