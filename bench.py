@@ -28,7 +28,6 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FP64_PEAK_TFLOPS = 1.199  # measured FP64 FMA throughput of this machine's GB300 (profiles/fp64_peak_probe.md)
 
 
 def parse_args():
@@ -356,6 +355,7 @@ def main():
     except Exception:
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    fp64_peak = fp64_peak_tflops(torch, f"cuda:{local}")
     achieved_gbs = nbytes / (avg_ms / 1e3) / 1e9
     traffic = read_traffic(kname)
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved_gbs, "peak": hbm_peak,
@@ -363,8 +363,9 @@ def main():
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback",
                 "traffic": traffic, "algorithmic_bytes": nbytes, "avg_launch_ms": avg_ms,
                 "fp64_tflops_achieved": nflops / (avg_ms / 1e3) / 1e12,
-                "fp64_tflops_peak": FP64_PEAK_TFLOPS,
-                "fp64_frac": nflops / (avg_ms / 1e3) / 1e12 / FP64_PEAK_TFLOPS}
+                "fp64_tflops_peak": fp64_peak,
+                "fp64_peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                "fp64_frac": nflops / (avg_ms / 1e3) / 1e12 / fp64_peak}
     kernels = {k: {"launches": v[0], "ms_total": v[1], "share": v[1] / max(1e-9, sum(x[1] for x in prof.values()))}
                for k, v in prof.items() if v[0] > 0}
     line = {
@@ -397,6 +398,26 @@ def main():
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def fp64_peak_tflops(torch, device):
+    """FP64 throughput of this GPU, measured now: best of three cuBLAS DGEMMs
+    of size 4096 (2 n^3 flops each)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=device)
+    b = torch.randn(n, n, dtype=torch.float64, device=device)
+    torch.matmul(a, b)
+    torch.cuda.synchronize(device)
+    best = 0.0
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize(device)
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    return best
 
 
 def ch_kernels(steps, prof):

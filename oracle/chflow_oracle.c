@@ -12,7 +12,7 @@
  * Parity is UNPINNED against the reference itself (no tests, fixtures or
  * buildable toolchain exist for it); see chflow_oracle.h.
  *
- * Build: oracle/Makefile (gcc -O2 -ffp-contract=off -fopenmp), so that x86
+ * Build: oracle/build_oracle.py (gcc -O2 -ffp-contract=off -fopenmp), so that x86
  * and Arm hosts round identically (no FMA contraction).
  */
 #include "chflow_oracle.h"
@@ -457,7 +457,18 @@ void orc_setup(orc* o) {
   o->ready = 1;
 }
 
+static void ensure_scheb(orc* o) {
+  if (o->t0) return;
+  const int Z = o->Z;
+  o->t0 = (double*)calloc((size_t)Z * Z, sizeof(double));
+  o->t1 = (double*)calloc((size_t)Z * Z, sizeof(double));
+  o->t2 = (double*)calloc((size_t)Z * Z, sizeof(double));
+  o->t4 = (double*)calloc((size_t)Z * Z, sizeof(double));
+  scheb(o->nz, o->t0, o->t1, o->t2, o->t4);
+}
+
 void orc_matrices(orc* o, double kmn, double* av, double* ae, double* xv, double* xe) {
+  ensure_scheb(o);
   const int Z = o->Z;
   int* ipiv = (int*)malloc(sizeof(int) * (size_t)Z);
   double* work = (double*)malloc(sizeof(double) * (size_t)Z);
