@@ -22,7 +22,8 @@ STATUS = {0: "CHF_OK", -1: "CHF_E_INVALID", -2: "CHF_E_CUDA", -3: "CHF_E_NOMEM",
 EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
            "chf_download_state", "chf_getnonlinear", "chf_solve", "chf_step",
            "chf_synchronize", "chf_diagnostics", "chf_kernels_per_step", "chf_device_field",
-           "chf_set_stream", "chf_profile_enable", "chf_profile_reset", "chf_profile_read")
+           "chf_set_stream", "chf_profile_enable", "chf_profile_reset", "chf_profile_read",
+           "chf_diagnostics_static")
 
 
 class ChannelError(RuntimeError):
@@ -75,6 +76,7 @@ def load_library(path: str = None):
     L.chf_profile_reset.argtypes = [vp]
     L.chf_profile_read.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
                                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    L.chf_diagnostics_static.argtypes = [ctypes.c_int] * 3 + [vp] * 6 + [dp, ctypes.POINTER(CDiag), vp]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     L.chf_last_error.restype = ctypes.c_char_p

@@ -144,6 +144,27 @@ int chf_profile_reset(chf_handle* h);
  * the last reset (synchronises the stream).  CHF_E_INVALID past the end. */
 int chf_profile_read(chf_handle* h, int idx, const char** name, int* launches, double* total_ms);
 
+/* Allocation-free diagnostics.  No counterpart in the reference: an addition
+ * for callers that cannot allocate device memory (their device memory is
+ * owned by another runtime's pool, or fully committed to the resident state,
+ * or their time loop must avoid the synchronisation of cudaMalloc/cudaFree).
+ * It computes the energy, max |value| and finiteness of chf_diagnostics
+ * (wall shear is reported as 0) on the caller's own device arrays in the
+ * field layout above, plus the energy of every wall-normal plane k in
+ * energy_profile[k] (k = 0..nnz, may be NULL), with no handle and no
+ * allocation: its scratch is a fixed __device__ array inside the library.
+ * nnz + 1 must not exceed CHF_STATIC_MAX_PLANES (else CHF_E_INVALID).  The
+ * first call on a device looks up the array's address with that device
+ * current (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU race
+ * and must be serialised by the caller.  stream: a cudaStream_t or NULL. */
+#define CHF_STATIC_MAX_PLANES 1025
+int chf_diagnostics_static(int nnx, int nny, int nnz,
+                           const double* d_unp1, const double* d_vnp1, const double* d_wnp1,
+                           const double* d_omegaxnp1, const double* d_omegaynp1,
+                           const double* d_omegaznp1, double* energy_profile, chf_diag* out,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -70,3 +70,14 @@ def test_python_layer_raises_channel_error(chflow_lib):
     from channel_flow_gb300 import Channel
     with pytest.raises(ChannelError):
         Channel(config.small(nnx=16, nny=8, nnz=16))
+
+
+def test_static_diagnostics_rejects_oversized_grid(chflow_lib):
+    """The allocation-free entry point checks the plane count against its
+    fixed scratch before touching the GPU."""
+    from channel_flow_gb300.channel import CDiag
+    d = CDiag()
+    one = ctypes.c_void_p(16)  # never dereferenced: the size check comes first
+    rc = chflow_lib.chf_diagnostics_static(16, 8, 1025, one, one, one, one, one, one, None,
+                                           ctypes.byref(d), None)
+    assert rc == -1
