@@ -150,9 +150,12 @@ class Channel:
             arrs.append(a)
         self._check(self.L.chf_upload_state(self.h, *[_dptr(a) for a in arrs]))
 
-    def download_state(self) -> dict:
-        out = {k: np.empty(self.shape) for k in FIELD_NAMES}
-        out.update({k: np.empty((self.cfg.nnz + 1, 2)) for k in MEAN_NAMES})
+    def download_state(self, out: dict = None) -> dict:
+        """Copy the module arrays device -> host, into ``out`` (C-contiguous
+        float64 arrays, e.g. pinned buffers) when given."""
+        if out is None:
+            out = {k: np.empty(self.shape) for k in FIELD_NAMES}
+            out.update({k: np.empty((self.cfg.nnz + 1, 2)) for k in MEAN_NAMES})
         self._check(self.L.chf_download_state(
             self.h, *[_dptr(out[k]) for k in FIELD_NAMES], *[_dptr(out[k]) for k in MEAN_NAMES]))
         return out

@@ -195,16 +195,22 @@ constexpr int S_WARPS = S_THREADS / 32;
 // as) into b (stride bs), by one warp: b_i = c_i sum_{j>i, j-i odd} 2 j a_j
 // (c_0 = 1/2) evaluated as suffix sums over each parity class, lane-local
 // then a warp scan.  Same sums as the serial recurrence, tree-ordered.
-__device__ __forceinline__ void warp_deriv(const double* a, int as, double* b, int bs, int N) {
+// tj[j] = 2 j (a per-CTA table, so no int-to-double conversion per element).
+constexpr int WD_EMAX = 8;  // elements per lane: N + 1 <= 256
+__device__ __forceinline__ void warp_deriv(const double* a, int as, double* b, int bs, int N,
+                                           const double* __restrict__ tj) {
   const int lane = threadIdx.x & 31;
   const int E = (N + 32) / 32;  // elements per lane (N + 1 <= 32 * E)
   const int i0 = lane * E;
+  double g[WD_EMAX];
   double te = 0.0, to = 0.0;    // lane totals of g_j over even / odd j
-  for (int q = 0; q < E; ++q) {
-    int j = i0 + q;
-    if (j <= N) {
-      double g = 2.0 * (double)j * a[j * as];
-      if (j & 1) to += g; else te += g;
+#pragma unroll
+  for (int q = 0; q < WD_EMAX; ++q) {
+    const int j = i0 + q;
+    g[q] = 0.0;
+    if (q < E && j <= N) {
+      g[q] = tj[j] * a[j * as];
+      if (j & 1) to += g[q]; else te += g[q];
     }
   }
   double se = te, so = to;      // inclusive suffix scan over lanes
@@ -214,20 +220,21 @@ __device__ __forceinline__ void warp_deriv(const double* a, int as, double* b, i
     if (lane + off < 32) { se += ue; so += uo; }
   }
   double re_ = se - te, ro = so - to;  // sums over lanes above this one
-  for (int q = E - 1; q >= 0; --q) {
-    int i = i0 + q;
-    if (i <= N) {
+#pragma unroll
+  for (int q = WD_EMAX - 1; q >= 0; --q) {
+    const int i = i0 + q;
+    if (q < E && i <= N) {
       double bi = (i & 1) ? re_ : ro;  // sum over j > i of the opposite parity
       if (i == 0) bi *= 0.5;
       b[i * bs] = bi;
-      double g = 2.0 * (double)i * a[i * as];
-      if (i & 1) ro += g; else re_ += g;
+      if (i & 1) ro += g[q]; else re_ += g[q];
     }
   }
   __syncwarp();
 }
 
 struct ChunkSmem {
+  double* tj; // [NZ] 2 j
   cd* cv;     // [CH][NZ] v coefficients  -> new v
   cd* co;     // [CH][NZ] omega_y coeffs  -> new omega_y
   cd* rv;     // [CH][NZ] AB2 explicit term of the v equation (GL values)
@@ -255,7 +262,10 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
     s.rg = p; p += CH * NZ;
     s.fb = p; p += 2 * CH * L2;
     s.dd = reinterpret_cast<double*>(p);
+    s.tj = s.dd + (size_t)CH * 10 * NZ;
   }
+  for (int j = threadIdx.x; j < NZ; j += blockDim.x) s.tj[j] = 2.0 * (double)j;
+  __syncthreads();
   const int g = blockIdx.x;
   const bool mean = (g == a.nk2);
   const double dt = a.dt, re = a.re;
@@ -308,16 +318,16 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
         if (mean) continue;
         const double* src = reinterpret_cast<const double*>(s.cv + m * NZ) + comp;
         double* o = dslot(s, m, comp * 4, NZ);
-        warp_deriv(src, 2, o, 1, N);
-        warp_deriv(o, 1, o + NZ, 1, N);
-        warp_deriv(o + NZ, 1, o + 2 * NZ, 1, N);
-        warp_deriv(o + 2 * NZ, 1, o + 3 * NZ, 1, N);
+        warp_deriv(src, 2, o, 1, N, s.tj);
+        warp_deriv(o, 1, o + NZ, 1, N, s.tj);
+        warp_deriv(o + NZ, 1, o + 2 * NZ, 1, N, s.tj);
+        warp_deriv(o + 2 * NZ, 1, o + 3 * NZ, 1, N, s.tj);
       } else {
         const int c = comp - 2;
         const double* src = reinterpret_cast<const double*>(s.co + m * NZ) + c;
         double* t1 = reinterpret_cast<double*>(s.fb + (2 * m + 1) * L2) + c * NZ;
-        warp_deriv(src, 2, t1, 1, N);
-        warp_deriv(t1, 1, dslot(s, m, 8 + c, NZ), 1, N);
+        warp_deriv(src, 2, t1, 1, N, s.tj);
+        warp_deriv(t1, 1, dslot(s, m, 8 + c, NZ), 1, N, s.tj);
       }
     }
     __syncthreads();
@@ -426,7 +436,7 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
       }
       for (int task = warp; task < nm * 2; task += S_WARPS) {
         int m = task / 2, comp = task % 2;
-        warp_deriv(reinterpret_cast<const double*>(s.co + m * NZ) + comp, 2, dslot(s, m, comp, NZ), 1, N);
+        warp_deriv(reinterpret_cast<const double*>(s.co + m * NZ) + comp, 2, dslot(s, m, comp, NZ), 1, N, s.tj);
       }
       __syncthreads();
       for (int t = tid; t < nm * NZ; t += blockDim.x) {
@@ -440,7 +450,7 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
     }
     for (int task = warp; task < nm * 2; task += S_WARPS) {  // Dv
       int m = task / 2, comp = task % 2;
-      warp_deriv(reinterpret_cast<const double*>(s.cv + m * NZ) + comp, 2, dslot(s, m, comp, NZ), 1, N);
+      warp_deriv(reinterpret_cast<const double*>(s.cv + m * NZ) + comp, 2, dslot(s, m, comp, NZ), 1, N, s.tj);
     }
     __syncthreads();
     // u, w into rv / rg (free now); v and omega_y stored
@@ -466,7 +476,7 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
     for (int task = warp; task < nm * 4; task += S_WARPS) {  // Du (re, im), Dw (re, im)
       int m = task / 4, comp = task % 4;
       const cd* src = (comp < 2) ? s.rv + m * NZ : s.rg + m * NZ;
-      warp_deriv(reinterpret_cast<const double*>(src) + (comp & 1), 2, dslot(s, m, 2 + comp, NZ), 1, N);
+      warp_deriv(reinterpret_cast<const double*>(src) + (comp & 1), 2, dslot(s, m, 2 + comp, NZ), 1, N, s.tj);
     }
     __syncthreads();
     for (int t = tid; t < nm * NZ; t += blockDim.x) {
@@ -671,7 +681,7 @@ int launch_solve_fp64(Handle* h) {
     return CHF_E_INVALID;
   }
   size_t smem = sizeof(cd) * (4 * (size_t)CH * d.NZ + 2 * (size_t)CH * 2 * d.N) +
-                sizeof(double) * 10 * (size_t)CH * d.NZ;
+                sizeof(double) * (10 * (size_t)CH + 1) * d.NZ;
   if (smem > 48 * 1024 &&
       !cuda_ok(h, cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                "k_solve smem"))
