@@ -32,6 +32,7 @@
 #include <cstdio>
 
 #include "chf_internal.h"
+#include "fft_warp.cuh"
 
 namespace chf {
 
@@ -357,6 +358,163 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zcurl(
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Length-192 specialisations (3/2-padded 128-point directions), one warp per
+// line with the register FFT of fft_warp.cuh.  Rows written by k_yinv_w and
+// read by k_xprod_w / k_yfwd_w are in the permuted order 32 k1 + lane of that
+// header; every consumer is row-wise, so the order never matters.
+// ---------------------------------------------------------------------------
+constexpr int W_WARPS = 8;    // warps (lines) per CTA in the x kernel
+// kx columns (one warp each) per CTA in the y kernels: 16 for FP32, 8 for FP64
+// (the [192][cols+1] tile stays under the 48 KB static shared-memory limit)
+template <typename T>
+struct YCols {
+  static constexpr int value = sizeof(T) == 4 ? 16 : 8;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_tw192(cplx<T>* s_tw, const cplx<T>* __restrict__ tw) {
+  for (int t = threadIdx.x; t < 192; t += blockDim.x) s_tw[t] = tw[t];
+}
+
+// x: c2r (three packed pairs), Lamb products, r2c; KX = 64, PX = 192.
+// grid ceil(nrows / W_WARPS), W_WARPS * 32 threads.
+template <typename T>
+__global__ void __launch_bounds__(W_WARPS * 32) k_xprod_w(cplx<T>* __restrict__ wy, long nrows,
+                                                         size_t fstride, T re_p,
+                                                         const cplx<T>* __restrict__ tw) {
+  using C = cplx<T>;
+  __shared__ C s_tw[192];
+  load_tw192(s_tw, tw);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long r = (long)blockIdx.x * W_WARPS + (threadIdx.x >> 5);
+  if (r >= nrows) return;
+  C pk[3][6];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const C* F = wy + (size_t)(2 * c) * fstride + (size_t)r * 64;
+    const C* G = wy + (size_t)(2 * c + 1) * fstride + (size_t)r * 64;
+    C f0 = F[lane], f1 = F[32 + lane], g0 = G[lane], g1 = G[32 + lane];
+    // Hermitian partners: positions 128 + l -> mode 64 - l, 160 + l -> mode 32 - l
+    const int src = (32 - lane) & 31;
+    C f1s = shfl_i(f1, src), g1s = shfl_i(g1, src);
+    C f0s = shfl_i(f0, src), g0s = shfl_i(g0, src);
+    C f32 = shfl_i(f1, 0), g32 = shfl_i(g1, 0);  // mode 32 (for lane 0)
+    C* v = pk[c];
+    v[0] = lane == 0 ? C{f0.re, g0.re} : C{f0.re - g0.im, f0.im + g0.re};  // F + iG (mean: real parts)
+    v[1] = C{f1.re - g1.im, f1.im + g1.re};
+    v[2] = C{(T)0, (T)0};
+    v[3] = C{(T)0, (T)0};
+    v[4] = lane == 0 ? C{(T)0, (T)0} : C{f1s.re + g1s.im, g1s.re - f1s.im};  // conj F + i conj G
+    v[5] = lane == 0 ? C{f32.re + g32.im, g32.re - f32.im} : C{f0s.re + g0s.im, g0s.re - f0s.im};
+    fft192_natural_to_perm<T, +1>(v, s_tw);
+  }
+  C z1[6], z2[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const T u = pk[0][k].re, v = pk[0][k].im, w = pk[1][k].re, ox = pk[1][k].im;
+    const T oy = pk[2][k].re, oz = pk[2][k].im;
+    z1[k] = C{(oy * w - re_p) - oz * v, oz * u - ox * w};
+    z2[k] = C{ox * v - oy * u, (T)0};
+  }
+  fft192_perm_to_natural<T, -1>(z1, s_tw);
+  fft192_perm_to_natural<T, -1>(z2, s_tw);
+  // unpack H1, H2 from Z = FFT(H1 + i H2): Z[-k] for k = l (reg 0) and 32 + l (reg 1)
+  const int src = (32 - lane) & 31;
+  C m5 = shfl_i(z1[5], src), m4 = shfl_i(z1[4], src), m50 = shfl_i(z1[5], 0);
+  C A0 = z1[0], B0 = lane == 0 ? z1[0] : m5;   // Z[192 - l]
+  C A1 = z1[1], B1 = lane == 0 ? m50 : m4;     // Z[160 - l]
+  C* o0 = wy + (size_t)r * 64;
+  C* o1 = wy + fstride + (size_t)r * 64;
+  C* o2 = wy + 2 * fstride + (size_t)r * 64;
+  const T h = (T)0.5;
+  o0[lane] = C{h * (A0.re + B0.re), h * (A0.im - B0.im)};
+  o1[lane] = C{h * (A0.im + B0.im), -h * (A0.re - B0.re)};
+  o0[32 + lane] = C{h * (A1.re + B1.re), h * (A1.im - B1.im)};
+  o1[32 + lane] = C{h * (A1.im + B1.im), -h * (A1.re - B1.re)};
+  o2[lane] = z2[0];
+  o2[32 + lane] = z2[1];
+}
+
+// y inverse: per (field, plane, 16 kx columns); KY = 128, PY = 192.
+// grid (KX / 16, MP, 6), 512 threads.
+template <typename T, int YW_COLS = YCols<T>::value>
+__global__ void __launch_bounds__(YW_COLS * 32) k_yinv_w(const cplx<T>* __restrict__ wz,
+                                                        cplx<T>* __restrict__ wy, Dims d,
+                                                        const cplx<T>* __restrict__ tw) {
+  using C = cplx<T>;
+  __shared__ C s_tw[192];
+  __shared__ C tile[192][YW_COLS + 1];
+  load_tw192(s_tw, tw);
+  const int f = blockIdx.z, p = blockIdx.y, kx0 = blockIdx.x * YW_COLS;
+  const long modes = d.modes();
+  const C* src = wz + ((size_t)f * d.MP + p) * modes;
+  for (int t = threadIdx.x; t < 128 * YW_COLS; t += blockDim.x) {
+    const int c = t % YW_COLS, ky = t / YW_COLS;
+    tile[ky][c] = src[(size_t)ky * d.KX + kx0 + c];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
+  C v[6];
+  const C z{(T)0, (T)0};
+  v[0] = tile[lane][c];                          // ky = l
+  v[1] = tile[32 + lane][c];                     // ky = 32 + l
+  v[2] = z;                                      // ky = 64 (Nyquist, zeroed) and padding
+  v[3] = z;
+  v[4] = lane == 0 ? z : tile[64 + lane][c];     // ky = 64 + l (negative modes)
+  v[5] = tile[96 + lane][c];                     // ky = 96 + l
+  fft192_natural_to_perm<T, +1>(v, s_tw);
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 6; ++k) tile[32 * k + lane][c] = v[k];
+  __syncthreads();
+  C* dst = wy + ((size_t)f * d.MP + p) * (size_t)192 * d.KX;
+  for (int t = threadIdx.x; t < 192 * YW_COLS; t += blockDim.x) {
+    const int cc = t % YW_COLS, q = t / YW_COLS;
+    dst[(size_t)q * d.KX + kx0 + cc] = tile[q][cc];
+  }
+}
+
+// y forward: per (component, plane, 16 kx columns); keeps ky = 0..64 and
+// the negative modes, scaled by 1/(PX PY).  grid (KX / 16, MP, 3), 512 threads.
+template <typename T, int YW_COLS = YCols<T>::value>
+__global__ void __launch_bounds__(YW_COLS * 32) k_yfwd_w(const cplx<T>* __restrict__ wy,
+                                                        cplx<T>* __restrict__ wz, Dims d,
+                                                        const cplx<T>* __restrict__ tw, T scale) {
+  using C = cplx<T>;
+  __shared__ C s_tw[192];
+  __shared__ C tile[192][YW_COLS + 1];
+  load_tw192(s_tw, tw);
+  const int f = blockIdx.z, p = blockIdx.y, kx0 = blockIdx.x * YW_COLS;
+  const long modes = d.modes();
+  const C* src = wy + ((size_t)f * d.MP + p) * (size_t)192 * d.KX;
+  for (int t = threadIdx.x; t < 192 * YW_COLS; t += blockDim.x) {
+    const int c = t % YW_COLS, q = t / YW_COLS;
+    tile[q][c] = src[(size_t)q * d.KX + kx0 + c];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
+  C v[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) v[k] = tile[32 * k + lane][c];
+  fft192_perm_to_natural<T, -1>(v, s_tw);
+  __syncthreads();
+  // natural spectral position 32 j + l -> ky slot
+  tile[lane][c] = C{v[0].re * scale, v[0].im * scale};                 // ky = l
+  tile[32 + lane][c] = C{v[1].re * scale, v[1].im * scale};            // ky = 32 + l
+  if (lane == 0) tile[64][c] = C{v[2].re * scale, v[2].im * scale};    // ky = 64 <- padded mode +64
+  if (lane > 0) tile[64 + lane][c] = C{v[4].re * scale, v[4].im * scale};  // ky = 64 + l
+  tile[96 + lane][c] = C{v[5].re * scale, v[5].im * scale};            // ky = 96 + l
+  __syncthreads();
+  C* dst = wz + ((size_t)f * d.MP + p) * modes;
+  for (int t = threadIdx.x; t < 128 * YW_COLS; t += blockDim.x) {
+    const int cc = t % YW_COLS, ky = t / YW_COLS;
+    dst[(size_t)ky * d.KX + kx0 + cc] = tile[ky][cc];
+  }
+}
+
 template <typename K>
 bool set_smem(Handle* h, K kernel, size_t bytes) {
   if (bytes > 48 * 1024)
@@ -378,6 +536,29 @@ template <typename T>
 int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const cplx<T>* tw_px) {
   const Dims& d = h->d;
   cudaStream_t st = h->stream;
+  if (sizeof(T) == 4 && d.PX == 192 && d.PY == 192 && d.KX % YCols<T>::value == 0) {
+    // register-FFT specialisation of the 128-point directions, FP32 only: in
+    // FP64 (the FP64 pipe is the bound) the cross-lane radix-2 network costs
+    // more FP64 instructions than the radix-4 shared-memory stages below
+    cudaEvent_t ev;
+    prof_begin(h, K_YINV, &ev);
+    constexpr int YC = YCols<T>::value;
+    k_yinv_w<T><<<dim3(d.KX / YC, d.MP, 6), YC * 32, 0, st>>>(wz, wy, d, tw_py);
+    prof_end(h, K_YINV, ev);
+    if (!cuda_ok(h, cudaGetLastError(), "k_yinv_w")) return CHF_E_CUDA;
+    const long nrows = (long)d.MP * d.PY;
+    prof_begin(h, K_XPROD, &ev);
+    k_xprod_w<T><<<(unsigned)((nrows + W_WARPS - 1) / W_WARPS), W_WARPS * 32, 0, st>>>(
+        wy, nrows, (size_t)d.MP * d.PY * d.KX, (T)h->cfg.re_p, tw_px);
+    prof_end(h, K_XPROD, ev);
+    if (!cuda_ok(h, cudaGetLastError(), "k_xprod_w")) return CHF_E_CUDA;
+    const T scale = (T)(1.0 / ((double)d.PX * (double)d.PY));
+    prof_begin(h, K_YFWD, &ev);
+    k_yfwd_w<T><<<dim3(d.KX / YC, d.MP, 3), YC * 32, 0, st>>>(wy, wz, d, tw_py, scale);
+    prof_end(h, K_YFWD, ev);
+    if (!cuda_ok(h, cudaGetLastError(), "k_yfwd_w")) return CHF_E_CUDA;
+    return CHF_OK;
+  }
   const int kxb = pick_kxb(d.KX);
   {
     if (!fft_fits(kxb, d.PY, Y_THREADS, 6)) {

@@ -15,6 +15,7 @@ CASES = {
     "c1_32": config.CONFIGS["c1_poiseuille_32"],
     "c2_os": config.CONFIGS["c2_orr_sommerfeld"],
     "mixed_radix": config.small(nnx=24, nny=12, nnz=20, aphi=1.5, beta=0.75, dt=5e-4, re=300.0, re_p=1.0),
+    "warp192": config.small(nnx=128, nny=128, nnz=16, aphi=2.0, beta=2.0 / 3.0, dt=2e-4, re=180.0, re_p=1.0),
 }
 VEL = ("unp1", "vnp1", "wnp1")
 
@@ -56,7 +57,8 @@ def test_mixed_nonlinear_term(chflow_lib, name):
         assert e < 1e-4, (k, e)
 
 
-@pytest.mark.parametrize("name,nsteps", [("small16", 50), ("c1_32", 50), ("c2_os", 50), ("mixed_radix", 30)])
+@pytest.mark.parametrize("name,nsteps", [("small16", 50), ("c1_32", 50), ("c2_os", 50), ("mixed_radix", 30),
+                                          ("warp192", 30)])
 def test_mixed_steps_vs_fp64(chflow_lib, name, nsteps):
     cfg = CASES[name]
     st = fields.turbulent_start_state(cfg, seed=4)

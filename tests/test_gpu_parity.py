@@ -26,6 +26,8 @@ CASES = {
     "c1_32": config.CONFIGS["c1_poiseuille_32"],
     "c2_os": config.CONFIGS["c2_orr_sommerfeld"],
     "mixed_radix": config.small(nnx=24, nny=12, nnz=20, aphi=1.5, beta=0.75, dt=5e-4, re=300.0, re_p=1.0),
+    # 3/2-padded lengths of 192: the register-FFT kernels of the 128-point directions
+    "warp192": config.small(nnx=128, nny=128, nnz=16, aphi=2.0, beta=2.0 / 3.0, dt=2e-4, re=180.0, re_p=1.0),
 }
 
 
@@ -110,7 +112,8 @@ def test_solve_matches_oracle(chflow_lib, oracle_mod, name):
     check(g.download_state(), o.get_state(), 1e-10, 1e-7)
 
 
-@pytest.mark.parametrize("name,nsteps", [("small16", 40), ("c1_32", 20), ("c2_os", 20), ("mixed_radix", 20)])
+@pytest.mark.parametrize("name,nsteps", [("small16", 40), ("c1_32", 20), ("c2_os", 20), ("mixed_radix", 20),
+                                          ("warp192", 10)])
 def test_steps_match_oracle(chflow_lib, oracle_mod, name, nsteps):
     cfg = CASES[name]
     st = make_state(cfg, seed=7)
