@@ -303,3 +303,62 @@ def turbulent_start_state(cfg: ChannelConfig, seed: int = 0, u_centre: float = N
     st["omegaznp1"][1, 0, 0] = 2.0 * u_centre
     _set_mean(cfg, st)
     return st
+
+
+def collocation_matrices(n: int):
+    """T0, T2, T4 at the Gauss-Lobatto points (the SCHEB matrices,
+    poiseuilleflow.f90:3272-3342), from exact Chebyshev calculus."""
+    T0 = _cheb_values_matrix(n)
+    D = cheb_derivative_matrix(n)
+    D2 = D @ D
+    return T0, T0 @ D2, T0 @ D2 @ D2
+
+
+def orr_sommerfeld_mode(cfg: ChannelConfig, kx: int = 1, U=None):
+    """Least-stable Orr-Sommerfeld eigenpair of v about U(z) (default
+    U = 1 - z^2) for streamwise mode kx (alpha = kx/aphi, beta = 0), in the
+    reference's collocation discretisation: the equation
+        d/dt (D^2 - a^2) v = -i a U (D^2 - a^2) v + i a U'' v + (1/re) (D^2 - a^2)^2 v
+    at the interior points 2..N-2 plus the four wall conditions v = v' = 0
+    (the rows of get_coef_v, poiseuilleflow.f90:3348-3381).  Returns
+    (sigma, coefficients): v(t) ~ exp(sigma t)."""
+    import scipy.linalg
+    n = cfg.nnz
+    a = kx / cfg.aphi
+    z = zpoints(n)
+    T0, T2, T4 = collocation_matrices(n)
+    if U is None:
+        Uz, Upp = 1.0 - z * z, -2.0 * np.ones_like(z)
+    else:
+        Uz, Upp = U
+    rows = np.arange(2, n - 1)
+    lap = T2[rows] - a * a * T0[rows]
+    bih = T4[rows] - 2 * a * a * T2[rows] + a ** 4 * T0[rows]
+    Lmat = np.zeros((n + 1, n + 1), dtype=complex)
+    Mmat = np.zeros((n + 1, n + 1), dtype=complex)
+    j = np.arange(n + 1)
+    Lmat[0] = 1.0
+    Lmat[1] = (-1.0) ** j
+    Lmat[2] = j ** 2
+    Lmat[3] = -((-1.0) ** j) * j ** 2
+    Lmat[4:] = -1j * a * Uz[rows, None] * lap + 1j * a * Upp[rows, None] * T0[rows] + bih / cfg.re
+    Mmat[4:] = lap
+    w, V = scipy.linalg.eig(Lmat, Mmat)
+    ok = np.isfinite(w)
+    w, V = w[ok], V[:, ok]
+    i = int(np.argmax(w.real))
+    return w[i], V[:, i]
+
+
+def orr_sommerfeld_state(cfg: ChannelConfig, amp: float = 1e-6, kx: int = 1) -> dict:
+    """Laminar Poiseuille flow U = 1 - z^2 (with steady mean histories) plus
+    the least-stable two-dimensional Orr-Sommerfeld mode of streamwise mode kx
+    at amplitude amp (max |v| coefficient); u, omega_z follow from
+    getvelocityandvorticity (omega_y = w = 0 for a 2D mode)."""
+    sigma, vec = orr_sommerfeld_mode(cfg, kx)
+    st = laminar_state(cfg, gamma=1.0)  # the fixed point needs re * re_p = 2
+    vec = vec / np.abs(vec).max() * amp
+    v = as_complex(st["vnp1"])
+    v[:, 0, kx] = vec
+    recover_velocity(cfg, st)  # k^2 != 0 modes only: the (0,0) mode stays laminar
+    return st
