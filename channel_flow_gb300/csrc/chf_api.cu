@@ -133,7 +133,56 @@ static void release(chf_handle* h) {
     cudaEventDestroy(p.b);
   }
   for (auto e : h->event_pool) cudaEventDestroy(e);
+  for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+static int step_once(chf_handle* h) {
+  int rc = h->cfg.precision == CHF_MIXED ? launch_nonlinear_mixed(h) : launch_nonlinear_fp64(h);
+  return rc == CHF_OK ? launch_solve_fp64(h) : rc;
+}
+
+// The graph of a pair of steps for the current history arrangement, captured
+// on first use; *out = nullptr when steps must be launched directly: with
+// per-kernel profiling on (its events are host-side bookkeeping), when the
+// stream is already being captured by the caller (the direct launches then
+// become part of the caller's graph), or after a capture failed.
+static int pair_graph(chf_handle* h, cudaGraphExec_t* out) {
+  *out = nullptr;
+  if (h->graphs_off || h->profiling) return CHF_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (!cuda_ok(h, cudaStreamIsCapturing(h->stream, &cs), "cudaStreamIsCapturing")) return CHF_E_CUDA;
+  if (cs != cudaStreamCaptureStatusNone) return CHF_OK;
+  for (auto& g : h->graphs)
+    if (std::memcmp(g.f, h->f, sizeof g.f) == 0) {
+      *out = g.exec;
+      return CHF_OK;
+    }
+  Handle::StepGraph sg{};
+  std::memcpy(sg.f, h->f, sizeof sg.f);
+  if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    cudaGetLastError();
+    h->graphs_off = true;
+    return CHF_OK;
+  }
+  int rc = step_once(h);
+  if (rc == CHF_OK) rc = step_once(h);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+  bool ok = rc == CHF_OK && e == cudaSuccess && graph &&
+            cudaGraphInstantiate(&sg.exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  // the captured launches did not run; put the arrangement back either way
+  std::memcpy(h->f, sg.f, sizeof sg.f);
+  if (!ok) {
+    cudaGetLastError();
+    h->err.clear();
+    h->graphs_off = true;
+    return CHF_OK;
+  }
+  h->graphs.push_back(sg);
+  *out = sg.exec;
+  return CHF_OK;
 }
 
 extern "C" {
@@ -319,10 +368,22 @@ int chf_step(chf_handle* h, int nsteps) {
     h->err = "nsteps must be >= 0";
     return CHF_E_INVALID;
   }
-  for (int s = 0; s < nsteps; ++s) {
-    int rc = chf_getnonlinear(h);
+  if (!h->uploaded) {
+    h->err = "chf_step before chf_upload_state";
+    return CHF_E_STATE;
+  }
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
+  int s = 0;
+  if (nsteps >= 2) {
+    cudaGraphExec_t g = nullptr;
+    int rc = pair_graph(h, &g);
     if (rc != CHF_OK) return rc;
-    rc = chf_solve(h);
+    if (g)
+      for (; s + 2 <= nsteps; s += 2)
+        if (!cuda_ok(h, cudaGraphLaunch(g, h->stream), "cudaGraphLaunch")) return CHF_E_CUDA;
+  }
+  for (; s < nsteps; ++s) {
+    int rc = step_once(h);
     if (rc != CHF_OK) return rc;
   }
   return CHF_OK;

@@ -109,6 +109,17 @@ struct Handle {
   int kernels_per_step = 0;
   cudaStream_t own_stream = nullptr;
 
+  // chf_step replays a CUDA graph of two steps.  Each step exchanges the
+  // history buffers by pointer (f[F_U] <-> f[F_RV], f[F_W] <-> f[F_RG]), so
+  // a pair of steps restores the arrangement and one graph, keyed by the
+  // arrangement it was captured in, serves every later pair.
+  struct StepGraph {
+    cd* f[F_COUNT];
+    cudaGraphExec_t exec;
+  };
+  std::vector<StepGraph> graphs;
+  bool graphs_off = false;  // capture failed once: launch directly from then on
+
   // per-kernel event timing (chf_profile_*)
   struct ProfRec {
     const char* name;

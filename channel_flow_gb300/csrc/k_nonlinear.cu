@@ -38,10 +38,12 @@ namespace chf {
 
 namespace {
 
-constexpr int ZC_LINES = 8;      // modes per CTA in the z kernels
+// Modes per CTA in the z kernels (ZL) and (plane, y) rows per CTA in k_xprod
+// (XR) are template parameters: the launchers take the largest of 8, 4, 2
+// (and 1 for XR) whose FFT work fits the per-thread butterfly bound, so long
+// lines (600-point z lines, 576-point x rows) run with fewer lines per CTA.
 constexpr int ZC_THREADS = 512;
 constexpr int Y_THREADS = 256;
-constexpr int X_ROWS = 8;        // (plane, y) rows per CTA in k_xprod
 constexpr int X_THREADS = 512;
 
 struct SixPtr {
@@ -52,22 +54,22 @@ struct SixPtr {
 // z: coefficients -> values at z'_p = cos(pi p / MZ), p = 0..MZ.
 // Even extension of length 2 MZ with doubled first entry, forward DFT, /2
 // (the packed evaluation of getlamb, REF:1672-1683, applied per field).
-// grid (ceil(modes / ZC_LINES), 6)
+// ZL modes per CTA, grid (ceil(modes / ZL), 6)
 // ---------------------------------------------------------------------------
-template <int MB2>
+template <int MB2, int ZL>
 __global__ void __launch_bounds__(ZC_THREADS) k_zc2v(SixPtr in, cd* __restrict__ out, Dims d,
                                                      const __grid_constant__ FftPlan pz, const cd* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cd* s = reinterpret_cast<cd*>(smem_raw);
   const int L = 2 * d.MZ, ls = L;
   const long modes = d.modes();
-  const long m0 = (long)blockIdx.x * ZC_LINES;
+  const long m0 = (long)blockIdx.x * ZL;
   const int f = blockIdx.y;
   const cd* __restrict__ src = in.p[f];
-  for (int t = threadIdx.x; t < ZC_LINES * L; t += blockDim.x) s[t] = cd{0.0, 0.0};
+  for (int t = threadIdx.x; t < ZL * L; t += blockDim.x) s[t] = cd{0.0, 0.0};
   __syncthreads();
-  for (int t = threadIdx.x; t < ZC_LINES * d.NZ; t += blockDim.x) {
-    int l = t % ZC_LINES, n = t / ZC_LINES;
+  for (int t = threadIdx.x; t < ZL * d.NZ; t += blockDim.x) {
+    int l = t % ZL, n = t / ZL;
     long m = m0 + l;
     cd c{0.0, 0.0};
     if (m < modes) c = src[(size_t)n * modes + m];
@@ -79,10 +81,10 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zc2v(SixPtr in, cd* __restrict__
     }
   }
   __syncthreads();
-  smem_fft<double, -1, MB2>(s, ZC_LINES, ls, pz, tw);
+  smem_fft<double, -1, MB2>(s, ZL, ls, pz, tw);
   cd* __restrict__ dst = out + (size_t)f * d.MP * modes;
-  for (int t = threadIdx.x; t < ZC_LINES * d.MP; t += blockDim.x) {
-    int l = t % ZC_LINES, p = t / ZC_LINES;
+  for (int t = threadIdx.x; t < ZL * d.MP; t += blockDim.x) {
+    int l = t % ZL, p = t / ZL;
     long m = m0 + l;
     if (m < modes) {
       cd v = s[l * ls + p];
@@ -125,9 +127,9 @@ __global__ void __launch_bounds__(Y_THREADS) k_yinv(const cplx<T>* __restrict__ 
 // ---------------------------------------------------------------------------
 // x: fused c2r, products, r2c.  Rows r = p * PY + yp; each row holds KX modes
 // of six fields (u, v, w, ox, oy, oz), written back in place as H1, H2, H3
-// into field slots 0, 1, 2.  grid (ceil(MP * PY / X_ROWS))
+// into field slots 0, 1, 2.  XR rows per CTA, grid (ceil(MP * PY / XR))
 // ---------------------------------------------------------------------------
-template <typename T, int MB2>
+template <typename T, int MB2, int XR>
 __global__ void __launch_bounds__(X_THREADS) k_xprod(cplx<T>* __restrict__ wy, Dims d, T re_p,
                                                      const __grid_constant__ FftPlan px, const cplx<T>* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -135,18 +137,18 @@ __global__ void __launch_bounds__(X_THREADS) k_xprod(cplx<T>* __restrict__ wy, D
   C* s = reinterpret_cast<C*>(smem_raw);
   const int PX = d.PX, KX = d.KX, ls = PX + 1;
   const long nrows = (long)d.MP * d.PY;
-  const long r0 = (long)blockIdx.x * X_ROWS;
+  const long r0 = (long)blockIdx.x * XR;
   const size_t fstride = (size_t)d.MP * d.PY * KX;
-  // lines: row q, pair c (0: u+iv, 1: w+i ox, 2: oy+i oz) at (c*X_ROWS + q) * ls
-  for (int t = threadIdx.x; t < X_ROWS * 3 * ls; t += blockDim.x) s[t] = C{(T)0, (T)0};
+  // lines: row q, pair c (0: u+iv, 1: w+i ox, 2: oy+i oz) at (c*XR + q) * ls
+  for (int t = threadIdx.x; t < XR * 3 * ls; t += blockDim.x) s[t] = C{(T)0, (T)0};
   __syncthreads();
-  for (int t = threadIdx.x; t < X_ROWS * 3 * KX; t += blockDim.x) {
+  for (int t = threadIdx.x; t < XR * 3 * KX; t += blockDim.x) {
     int k = t % KX, c = (t / KX) % 3, q = t / (3 * KX);
     long r = r0 + q;
     if (r >= nrows) continue;
     C F = wy[(size_t)(2 * c) * fstride + (size_t)r * KX + k];
     C G = wy[(size_t)(2 * c + 1) * fstride + (size_t)r * KX + k];
-    C* line = s + (c * X_ROWS + q) * ls;
+    C* line = s + (c * XR + q) * ls;
     if (k == 0) {
       line[0] = C{F.re, G.re};  // imaginary part of the streamwise mean dropped
     } else {
@@ -155,34 +157,34 @@ __global__ void __launch_bounds__(X_THREADS) k_xprod(cplx<T>* __restrict__ wy, D
     }
   }
   __syncthreads();
-  smem_fft<T, +1, MB2>(s, X_ROWS * 3, ls, px, tw);
+  smem_fft<T, +1, MB2>(s, XR * 3, ls, px, tw);
   // products at every physical point; write (H1 + i H2) to pair 0, (H3 + 0i) to pair 1
-  for (int t = threadIdx.x; t < X_ROWS * PX; t += blockDim.x) {
+  for (int t = threadIdx.x; t < XR * PX; t += blockDim.x) {
     int x = t % PX, q = t / PX;
-    C a = s[(0 * X_ROWS + q) * ls + x];  // u, v
-    C b = s[(1 * X_ROWS + q) * ls + x];  // w, ox
-    C c = s[(2 * X_ROWS + q) * ls + x];  // oy, oz
+    C a = s[(0 * XR + q) * ls + x];  // u, v
+    C b = s[(1 * XR + q) * ls + x];  // w, ox
+    C c = s[(2 * XR + q) * ls + x];  // oy, oz
     T u = a.re, v = a.im, w = b.re, ox = b.im, oy = c.re, oz = c.im;
     T h1 = (oy * w - re_p) - oz * v;
     T h2 = oz * u - ox * w;
     T h3 = ox * v - oy * u;
-    s[(0 * X_ROWS + q) * ls + x] = C{h1, h2};
-    s[(1 * X_ROWS + q) * ls + x] = C{h3, (T)0};
+    s[(0 * XR + q) * ls + x] = C{h1, h2};
+    s[(1 * XR + q) * ls + x] = C{h3, (T)0};
   }
   __syncthreads();
-  // forward DFT of the 2 * X_ROWS lines holding (H1 + i H2) and H3
-  smem_fft<T, -1, MB2>(s, X_ROWS * 2, ls, px, tw);
-  for (int t = threadIdx.x; t < X_ROWS * KX; t += blockDim.x) {
+  // forward DFT of the 2 * XR lines holding (H1 + i H2) and H3
+  smem_fft<T, -1, MB2>(s, XR * 2, ls, px, tw);
+  for (int t = threadIdx.x; t < XR * KX; t += blockDim.x) {
     int k = t % KX, q = t / KX;
     long r = r0 + q;
     if (r >= nrows) continue;
-    const C* z = s + (0 * X_ROWS + q) * ls;
+    const C* z = s + (0 * XR + q) * ls;
     C A = z[k];
     C B = z[k == 0 ? 0 : PX - k];
     B.im = -B.im;  // conj(Z[-k])
     C H1{(T)0.5 * (A.re + B.re), (T)0.5 * (A.im + B.im)};
     C H2{(T)0.5 * (A.im - B.im), (T)-0.5 * (A.re - B.re)};
-    C H3 = s[(1 * X_ROWS + q) * ls + k];
+    C H3 = s[(1 * XR + q) * ls + k];
     wy[(size_t)0 * fstride + (size_t)r * KX + k] = H1;
     wy[(size_t)1 * fstride + (size_t)r * KX + k] = H2;
     wy[(size_t)2 * fstride + (size_t)r * KX + k] = H3;
@@ -236,11 +238,11 @@ __device__ __forceinline__ void cheb_deriv_serial(const double* a, int as, doubl
 
 // ---------------------------------------------------------------------------
 // z: values -> coefficients, curl, histories, coefficients -> GL values.
-// grid (ceil(modes / ZC_LINES))
-// shared: FFT buffer ZC_LINES x 2MZ, coefficient store 3 x ZC_LINES x NZ,
-//         derivative store 2 x ZC_LINES x NZ
+// ZL modes per CTA, grid (ceil(modes / ZL))
+// shared: FFT buffer max(ZL x 2MZ, 2 ZL x 2N), coefficient store 3 x ZL x NZ,
+//         derivative store 4 x ZL x NZ (doubles)
 // ---------------------------------------------------------------------------
-template <int MB2>
+template <int MB2, int ZL>
 __global__ void __launch_bounds__(ZC_THREADS) k_zcurl(
     const cd* __restrict__ wz, cd* __restrict__ out_hv, cd* __restrict__ out_hg,
     cd* __restrict__ ox_out, cd* __restrict__ oz_out, double* __restrict__ cl1n,
@@ -252,16 +254,16 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zcurl(
   const int NZ = d.NZ, N = d.N;
   cd* s = reinterpret_cast<cd*>(smem_raw);
   const int L2 = 2 * N;
-  const int fb = max(ZC_LINES * ls, 2 * ZC_LINES * L2);  // FFT buffer elements
-  cd* coef = s + fb;                     // [3][ZC_LINES][NZ]
-  double* der = reinterpret_cast<double*>(coef + 3 * ZC_LINES * NZ);  // [4][ZC_LINES][NZ]
+  const int fb = max(ZL * ls, 2 * ZL * L2);  // FFT buffer elements
+  cd* coef = s + fb;                     // [3][ZL][NZ]
+  double* der = reinterpret_cast<double*>(coef + 3 * ZL * NZ);  // [4][ZL][NZ]
   const long modes = d.modes();
-  const long m0 = (long)blockIdx.x * ZC_LINES;
+  const long m0 = (long)blockIdx.x * ZL;
   const double inv_mz = 1.0 / (double)d.MZ;
   for (int f = 0; f < 3; ++f) {
     const cd* __restrict__ src = wz + (size_t)f * d.MP * modes;
-    for (int t = threadIdx.x; t < ZC_LINES * d.MP; t += blockDim.x) {
-      int l = t % ZC_LINES, p = t / ZC_LINES;
+    for (int t = threadIdx.x; t < ZL * d.MP; t += blockDim.x) {
+      int l = t % ZL, p = t / ZL;
       long m = m0 + l;
       cd v{0.0, 0.0};
       if (m < modes) v = src[(size_t)p * modes + m];
@@ -269,29 +271,29 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zcurl(
       if (p > 0 && p < d.MZ) s[l * ls + L - p] = v;
     }
     __syncthreads();
-    smem_fft<double, -1, MB2>(s, ZC_LINES, ls, pzm, twm);
-    for (int t = threadIdx.x; t < ZC_LINES * NZ; t += blockDim.x) {
-      int l = t % ZC_LINES, n = t / ZC_LINES;
+    smem_fft<double, -1, MB2>(s, ZL, ls, pzm, twm);
+    for (int t = threadIdx.x; t < ZL * NZ; t += blockDim.x) {
+      int l = t % ZL, n = t / ZL;
       cd v = s[l * ls + n];
       double sc = (n == 0) ? 0.5 * inv_mz : inv_mz;
-      coef[(f * ZC_LINES + l) * NZ + n] = cd{v.re * sc, v.im * sc};
+      coef[(f * ZL + l) * NZ + n] = cd{v.re * sc, v.im * sc};
     }
     __syncthreads();
   }
   // omega_x <- H1, omega_z <- H3 (the reference leaves them there, REF:1489-1496)
-  for (int t = threadIdx.x; t < ZC_LINES * NZ; t += blockDim.x) {
-    int l = t % ZC_LINES, n = t / ZC_LINES;
+  for (int t = threadIdx.x; t < ZL * NZ; t += blockDim.x) {
+    int l = t % ZL, n = t / ZL;
     long m = m0 + l;
     if (m >= modes) continue;
-    ox_out[(size_t)n * modes + m] = coef[(0 * ZC_LINES + l) * NZ + n];
-    oz_out[(size_t)n * modes + m] = coef[(2 * ZC_LINES + l) * NZ + n];
+    ox_out[(size_t)n * modes + m] = coef[(0 * ZL + l) * NZ + n];
+    oz_out[(size_t)n * modes + m] = coef[(2 * ZL + l) * NZ + n];
   }
   // derivatives of H1 and H3 (re, im): 4 serial recurrences per line
-  if (threadIdx.x < 4 * ZC_LINES) {
-    int l = threadIdx.x % ZC_LINES, which = threadIdx.x / ZC_LINES;  // 0:H1re 1:H1im 2:H3re 3:H3im
-    const cd* c = coef + ((which < 2 ? 0 : 2) * ZC_LINES + l) * NZ;
+  if (threadIdx.x < 4 * ZL) {
+    int l = threadIdx.x % ZL, which = threadIdx.x / ZL;  // 0:H1re 1:H1im 2:H3re 3:H3im
+    const cd* c = coef + ((which < 2 ? 0 : 2) * ZL + l) * NZ;
     const double* a = reinterpret_cast<const double*>(c) + (which & 1);
-    cheb_deriv_serial(a, 2, der + (which * ZC_LINES + l) * NZ, 1, N);
+    cheb_deriv_serial(a, 2, der + (which * ZL + l) * NZ, 1, N);
   }
   __syncthreads();
   // (0,0)-mode histories: nm1 <- old n (the swap of REF:1560-1569), n <- new
@@ -305,18 +307,18 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zcurl(
   }
   // h_v, h_g in coefficient space -> FFT buffer lines 2l (h_v) and 2l+1 (h_g)
   // of length 2N (even extension with doubled end points, REF:1573-1581)
-  for (int t = threadIdx.x; t < ZC_LINES * NZ; t += blockDim.x) {
-    int l = t % ZC_LINES, n = t / ZC_LINES;
+  for (int t = threadIdx.x; t < ZL * NZ; t += blockDim.x) {
+    int l = t % ZL, n = t / ZL;
     long m = m0 + l;
     int kx = (int)(m % d.KX), ky = (int)(m / d.KX);
     double a = 0.0, b = 0.0;
     if (m < modes) { a = iapha[kx]; b = ibeta[ky]; }
     double k2 = a * a + b * b;
-    cd h1 = coef[(0 * ZC_LINES + l) * NZ + n];
-    cd h2 = coef[(1 * ZC_LINES + l) * NZ + n];
-    cd h3 = coef[(2 * ZC_LINES + l) * NZ + n];
-    double d1r = der[(0 * ZC_LINES + l) * NZ + n], d1i = der[(1 * ZC_LINES + l) * NZ + n];
-    double d3r = der[(2 * ZC_LINES + l) * NZ + n], d3i = der[(3 * ZC_LINES + l) * NZ + n];
+    cd h1 = coef[(0 * ZL + l) * NZ + n];
+    cd h2 = coef[(1 * ZL + l) * NZ + n];
+    cd h3 = coef[(2 * ZL + l) * NZ + n];
+    double d1r = der[(0 * ZL + l) * NZ + n], d1i = der[(1 * ZL + l) * NZ + n];
+    double d3r = der[(2 * ZL + l) * NZ + n], d3i = der[(3 * ZL + l) * NZ + n];
     // h_v = k2 H2 + i a D H1 + i b D H3
     cd hv{k2 * h2.re - a * d1i - b * d3i, k2 * h2.im + a * d1r + b * d3r};
     // h_g = i a H3 - i b H1
@@ -336,9 +338,9 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zcurl(
     }
   }
   __syncthreads();
-  smem_fft<double, -1, MB2>(s, ZC_LINES * 2, L2, pz2, tw2);
-  for (int t = threadIdx.x; t < ZC_LINES * NZ; t += blockDim.x) {
-    int l = t % ZC_LINES, n = t / ZC_LINES;
+  smem_fft<double, -1, MB2>(s, ZL * 2, L2, pz2, tw2);
+  for (int t = threadIdx.x; t < ZL * NZ; t += blockDim.x) {
+    int l = t % ZL, n = t / ZL;
     long m = m0 + l;
     if (m >= modes) continue;
     cd v = s[(2 * l) * L2 + n];
@@ -524,10 +526,94 @@ bool set_smem(Handle* h, K kernel, size_t bytes) {
   return true;
 }
 
-int pick_kxb(int KX) {
-  for (int b = 16; b > 1; b /= 2)
-    if (KX % b == 0) return b;
-  return 1;
+constexpr size_t kMaxSmem = 227 * 1024;  // dynamic shared memory per CTA
+
+// streamwise modes per CTA in the generic y kernels: the largest power of two
+// up to 16 that divides KX and whose lines fit the butterfly bound and smem
+template <typename T>
+int pick_kxb(const Dims& d) {
+  for (int b = 16; b >= 1; b /= 2)
+    if (d.KX % b == 0 && fft_fits(b, d.PY, Y_THREADS, 6) &&
+        sizeof(cplx<T>) * b * (d.PY + 1) <= kMaxSmem)
+      return b;
+  return 0;
+}
+
+template <typename T>
+size_t xprod_smem(const Dims& d, int xr) { return sizeof(cplx<T>) * xr * 3 * (d.PX + 1); }
+
+template <typename T>
+int pick_xr(const Dims& d) {
+  for (int r = 8; r >= 1; r /= 2)
+    if (fft_fits(r * 3, d.PX, X_THREADS, 5) && xprod_smem<T>(d, r) <= kMaxSmem) return r;
+  return 0;
+}
+
+size_t zc2v_smem(const Dims& d, int zl) { return sizeof(cd) * zl * 2 * d.MZ; }
+
+size_t zcurl_smem(const Dims& d, int zl) {
+  const size_t fb = (size_t)std::max(zl * 2 * d.MZ, 2 * zl * 2 * d.N);
+  return sizeof(cd) * fb + sizeof(cd) * 3 * zl * d.NZ + sizeof(double) * 4 * zl * d.NZ;
+}
+
+int pick_zl_c2v(const Dims& d) {
+  for (int l = 8; l >= 2; l /= 2)
+    if (fft_fits(l, 2 * d.MZ, ZC_THREADS, 4) && zc2v_smem(d, l) <= kMaxSmem) return l;
+  return 0;
+}
+
+int pick_zl_curl(const Dims& d) {
+  for (int l = 8; l >= 2; l /= 2)
+    if (fft_fits(l, 2 * d.MZ, ZC_THREADS, 4) && fft_fits(2 * l, 2 * d.N, ZC_THREADS, 4) &&
+        zcurl_smem(d, l) <= kMaxSmem)
+      return l;
+  return 0;
+}
+
+template <typename T, int XR>
+int run_xprod(Handle* h, cplx<T>* wy, const cplx<T>* tw_px) {
+  const Dims& d = h->d;
+  const size_t smem = xprod_smem<T>(d, XR);
+  if (!set_smem(h, k_xprod<T, 5, XR>, smem)) return CHF_E_CUDA;
+  const long nrows = (long)d.MP * d.PY;
+  dim3 grid((unsigned)((nrows + XR - 1) / XR));
+  cudaEvent_t ev;
+  prof_begin(h, K_XPROD, &ev);
+  k_xprod<T, 5, XR><<<grid, X_THREADS, smem, h->stream>>>(wy, d, (T)h->cfg.re_p, h->px, tw_px);
+  prof_end(h, K_XPROD, ev);
+  return cuda_ok(h, cudaGetLastError(), "k_xprod") ? CHF_OK : CHF_E_CUDA;
+}
+
+template <int ZL>
+int run_zc2v(Handle* h) {
+  const Dims& d = h->d;
+  SixPtr in{{h->f[F_U], h->f[F_V], h->f[F_W], h->f[F_OX], h->f[F_OY], h->f[F_OZ]}};
+  const size_t smem = zc2v_smem(d, ZL);
+  if (!set_smem(h, k_zc2v<4, ZL>, smem)) return CHF_E_CUDA;
+  dim3 grid((unsigned)((d.modes() + ZL - 1) / ZL), 6);
+  cudaEvent_t ev;
+  prof_begin(h, K_ZC2V, &ev);
+  k_zc2v<4, ZL><<<grid, ZC_THREADS, smem, h->stream>>>(in, h->wz, d, h->pzm, h->tw_zm);
+  prof_end(h, K_ZC2V, ev);
+  return cuda_ok(h, cudaGetLastError(), "k_zc2v") ? CHF_OK : CHF_E_CUDA;
+}
+
+template <int ZL>
+int run_zcurl(Handle* h) {
+  const Dims& d = h->d;
+  const size_t smem = zcurl_smem(d, ZL);
+  if (!set_smem(h, k_zcurl<4, ZL>, smem)) return CHF_E_CUDA;
+  dim3 grid((unsigned)((d.modes() + ZL - 1) / ZL));
+  // h_v -> the unp1 buffer, h_g -> the wnp1 buffer; swapped with rhsvn /
+  // rhsomegayn by the caller (REF:1542-1558)
+  cudaEvent_t ev;
+  prof_begin(h, K_ZCURL, &ev);
+  k_zcurl<4, ZL><<<grid, ZC_THREADS, smem, h->stream>>>(
+      h->wz, h->f[F_U], h->f[F_W], h->f[F_OX], h->f[F_OZ], h->mean[M_CL1N], h->mean[M_CL1NM1],
+      h->mean[M_CL3N], h->mean[M_CL3NM1], h->iapha, h->ibeta, d, h->pzm, h->tw_zm, h->pz2,
+      h->tw_z2);
+  prof_end(h, K_ZCURL, ev);
+  return cuda_ok(h, cudaGetLastError(), "k_zcurl") ? CHF_OK : CHF_E_CUDA;
 }
 
 }  // namespace
@@ -559,12 +645,13 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     if (!cuda_ok(h, cudaGetLastError(), "k_yfwd_w")) return CHF_E_CUDA;
     return CHF_OK;
   }
-  const int kxb = pick_kxb(d.KX);
+  const int kxb = pick_kxb<T>(d);
+  const int xr = pick_xr<T>(d);
+  if (!kxb || !xr) {
+    h->err = "x/y transforms: FFT length too large for the launch shapes";
+    return CHF_E_INVALID;
+  }
   {
-    if (!fft_fits(kxb, d.PY, Y_THREADS, 6)) {
-      h->err = "k_yinv: FFT length too large for the launch shape";
-      return CHF_E_INVALID;
-    }
     size_t smem = sizeof(cplx<T>) * kxb * (d.PY + 1);
     if (!set_smem(h, k_yinv<T, 6>, smem)) return CHF_E_CUDA;
     dim3 grid(d.KX / kxb, d.MP, 6);
@@ -575,19 +662,11 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     if (!cuda_ok(h, cudaGetLastError(), "k_yinv")) return CHF_E_CUDA;
   }
   {
-    if (!fft_fits(X_ROWS * 3, d.PX, X_THREADS, 5)) {
-      h->err = "k_xprod: FFT length too large for the launch shape";
-      return CHF_E_INVALID;
-    }
-    size_t smem = sizeof(cplx<T>) * X_ROWS * 3 * (d.PX + 1);
-    if (!set_smem(h, k_xprod<T, 5>, smem)) return CHF_E_CUDA;
-    long nrows = (long)d.MP * d.PY;
-    dim3 grid((unsigned)((nrows + X_ROWS - 1) / X_ROWS));
-    cudaEvent_t ev;
-    prof_begin(h, K_XPROD, &ev);
-    k_xprod<T, 5><<<grid, X_THREADS, smem, st>>>(wy, d, (T)h->cfg.re_p, h->px, tw_px);
-    prof_end(h, K_XPROD, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_xprod")) return CHF_E_CUDA;
+    int rc = xr == 8 ? run_xprod<T, 8>(h, wy, tw_px)
+           : xr == 4 ? run_xprod<T, 4>(h, wy, tw_px)
+           : xr == 2 ? run_xprod<T, 2>(h, wy, tw_px)
+                     : run_xprod<T, 1>(h, wy, tw_px);
+    if (rc != CHF_OK) return rc;
   }
   {
     size_t smem = sizeof(cplx<T>) * kxb * (d.PY + 1);
@@ -608,51 +687,19 @@ template int launch_xy<float>(Handle*, cf*, cf*, const cf*, const cf*);
 
 int launch_nonlinear_fp64(Handle* h) {
   const Dims& d = h->d;
-  cudaStream_t st = h->stream;
-  const long modes = d.modes();
-  // z inverse, six fields: u, v, w, ox, oy, oz
-  {
-    SixPtr in{{h->f[F_U], h->f[F_V], h->f[F_W], h->f[F_OX], h->f[F_OY], h->f[F_OZ]}};
-    const int L = 2 * d.MZ;
-    if (!fft_fits(ZC_LINES, L, ZC_THREADS, 4)) {
-      h->err = "k_zc2v: FFT length too large for the launch shape";
-      return CHF_E_INVALID;
-    }
-    size_t smem = sizeof(cd) * ZC_LINES * L;
-    if (!set_smem(h, k_zc2v<4>, smem)) return CHF_E_CUDA;
-    dim3 grid((unsigned)((modes + ZC_LINES - 1) / ZC_LINES), 6);
-    cudaEvent_t ev;
-    prof_begin(h, K_ZC2V, &ev);
-    k_zc2v<4><<<grid, ZC_THREADS, smem, st>>>(in, h->wz, d, h->pzm, h->tw_zm);
-    prof_end(h, K_ZC2V, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_zc2v")) return CHF_E_CUDA;
+  // z inverse of the six fields u, v, w, ox, oy, oz
+  const int zl = pick_zl_c2v(d);
+  const int zc = pick_zl_curl(d);
+  if (!zl || !zc) {
+    h->err = "z transforms: FFT length too large for the launch shapes";
+    return CHF_E_INVALID;
   }
-  {
-    int rc = launch_xy<double>(h, h->wz, h->wy, h->tw_py, h->tw_px);
-    if (rc != CHF_OK) return rc;
-  }
-  {
-    const int L = 2 * d.MZ;
-    if (!fft_fits(ZC_LINES, L, ZC_THREADS, 4) || !fft_fits(2 * ZC_LINES, 2 * d.N, ZC_THREADS, 4)) {
-      h->err = "k_zcurl: FFT length too large for the launch shape";
-      return CHF_E_INVALID;
-    }
-    size_t fb = (size_t)std::max(ZC_LINES * L, 2 * ZC_LINES * 2 * d.N);
-    size_t smem = sizeof(cd) * fb + sizeof(cd) * 3 * ZC_LINES * d.NZ +
-                  sizeof(double) * 4 * ZC_LINES * d.NZ;
-    if (!set_smem(h, k_zcurl<4>, smem)) return CHF_E_CUDA;
-    dim3 grid((unsigned)((modes + ZC_LINES - 1) / ZC_LINES));
-    // h_v -> the unp1 buffer, h_g -> the wnp1 buffer; swapped with rhsvn /
-    // rhsomegayn below (REF:1542-1558)
-    cudaEvent_t ev;
-    prof_begin(h, K_ZCURL, &ev);
-    k_zcurl<4><<<grid, ZC_THREADS, smem, st>>>(
-        h->wz, h->f[F_U], h->f[F_W], h->f[F_OX], h->f[F_OZ], h->mean[M_CL1N], h->mean[M_CL1NM1],
-        h->mean[M_CL3N], h->mean[M_CL3NM1], h->iapha, h->ibeta, d, h->pzm, h->tw_zm, h->pz2,
-        h->tw_z2);
-    prof_end(h, K_ZCURL, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_zcurl")) return CHF_E_CUDA;
-  }
+  int rc = zl == 8 ? run_zc2v<8>(h) : zl == 4 ? run_zc2v<4>(h) : run_zc2v<2>(h);
+  if (rc != CHF_OK) return rc;
+  rc = launch_xy<double>(h, h->wz, h->wy, h->tw_py, h->tw_px);
+  if (rc != CHF_OK) return rc;
+  rc = zc == 8 ? run_zcurl<8>(h) : zc == 4 ? run_zcurl<4>(h) : run_zcurl<2>(h);
+  if (rc != CHF_OK) return rc;
   std::swap(h->f[F_U], h->f[F_RV]);
   std::swap(h->f[F_W], h->f[F_RG]);
   return CHF_OK;

@@ -247,6 +247,9 @@ __device__ __forceinline__ double* dslot(const ChunkSmem& s, int m, int q, int N
   return s.dd + ((size_t)m * 10 + q) * NZ;
 }
 
+// MB2 bounds the radix-2 butterflies per thread of the 2N-point DFTs (2 up
+// to nnz = 128, 4 up to nnz = 256)
+template <int MB2>
 __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ SolveArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Dims& d = a.d;
@@ -361,7 +364,7 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
       }
     }
     __syncthreads();
-    smem_fft<double, -1, 2>(s.fb, 2 * CH, L2, a.pz2, a.tw2);
+    smem_fft<double, -1, MB2>(s.fb, 2 * CH, L2, a.pz2, a.tw2);
     // ---- D: fold the collocation rows into even / odd right-hand sides.
     // rhs storage reuses dd: [CH][4 blocks][NZ] complex (fits in 10*NZ doubles)
     const int nev = sl.ne_v, nov = sl.no_v, new_ = sl.ne_w, now_ = sl.no_w;
@@ -676,19 +679,21 @@ int launch_solve_fp64(Handle* h) {
   a.pz2 = h->pz2;
   a.tw2 = h->tw_z2;
   a.nk2 = h->nk2;
-  if (d.N + 1 > 32 * 8 || !fft_fits(2 * CH, 2 * d.N, S_THREADS, 2)) {
+  const int mb2 = fft_fits(2 * CH, 2 * d.N, S_THREADS, 2) ? 2 : 4;
+  if (d.N + 1 > 32 * WD_EMAX || !fft_fits(2 * CH, 2 * d.N, S_THREADS, mb2)) {
     h->err = "k_solve: nnz too large for the launch shape";
     return CHF_E_INVALID;
   }
   size_t smem = sizeof(cd) * (4 * (size_t)CH * d.NZ + 2 * (size_t)CH * 2 * d.N) +
                 sizeof(double) * (10 * (size_t)CH + 1) * d.NZ;
+  auto kern = mb2 == 2 ? k_solve<2> : k_solve<4>;
   if (smem > 48 * 1024 &&
-      !cuda_ok(h, cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+      !cuda_ok(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                "k_solve smem"))
     return CHF_E_CUDA;
   cudaEvent_t ev;
   prof_begin(h, K_SOLVE, &ev);
-  k_solve<<<h->nk2 + 1, S_THREADS, smem, h->stream>>>(a);
+  kern<<<h->nk2 + 1, S_THREADS, smem, h->stream>>>(a);
   prof_end(h, K_SOLVE, ev);
   if (!cuda_ok(h, cudaGetLastError(), "k_solve")) return CHF_E_CUDA;
   return CHF_OK;

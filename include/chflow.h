@@ -114,7 +114,11 @@ int chf_solve(chf_handle* h);
 
 /* nsteps iterations of the main loop body for istep > istepbegin
  * (poiseuilleflow.f90:224 then 242-474).  Asynchronous on the handle's
- * stream; chf_synchronize() waits. */
+ * stream; chf_synchronize() waits.  Pairs of steps replay a CUDA graph
+ * captured on the first call (one launch per pair instead of one per
+ * kernel); the kernels and results are those of chf_getnonlinear +
+ * chf_solve.  Steps launch directly instead while per-kernel profiling is
+ * on, or when the stream is already under capture by the caller. */
 int chf_step(chf_handle* h, int nsteps);
 
 int chf_synchronize(chf_handle* h);

@@ -59,10 +59,45 @@ def worst(errs):
     return k, errs[k]
 
 
-def check(gpu, ref, prog_tol, hist_tol):
+def oracle_sensitivity(oracle_mod, cfg, st, run, names=ALL, eps=2.2e-16, seed=1):
+    """Per-part relative change of the oracle's result when every input value
+    is multiplied by (1 + eps * N(0,1)): the rounding-level conditioning
+    floor of that result.  run(oracle) performs the calls under test."""
+    rng = np.random.default_rng(seed)
+    pert = {k: v * (1.0 + eps * rng.standard_normal(v.shape)) for k, v in st.items()}
+    outs = []
+    for s in (st, pert):
+        o = oracle_mod.Oracle.from_config(cfg)
+        o.setup()
+        o.set_state(s)
+        run(o)
+        outs.append(o.get_state())
+    return compare(outs[1], outs[0], names=names)
+
+
+def bad_parts(errs, prog_tol, hist_tol, floor=None, factor=4.0):
+    """Parts above their bar: prog_tol for prognostic arrays, hist_tol for the
+    rest, each raised to factor x the conditioning floor where one is given."""
+    bad = {}
+    for k, e in errs.items():
+        tol = prog_tol if k in PROG else hist_tol
+        if floor is not None:
+            tol = max(tol, factor * floor.get(k, 0.0))
+        if e >= tol:
+            bad[k] = e
+    return bad
+
+
+def check(gpu, ref, prog_tol, hist_tol, sensitivity=None):
     """Prognostic physical modes to prog_tol; histories, Nyquist slots and the
-    (0,0) plane averages to hist_tol."""
+    (0,0) plane averages to hist_tol.  If a part misses its bar and
+    sensitivity() (the oracle's conditioning floor, oracle_sensitivity) is
+    given, the bar of that part becomes 4x its floor."""
     errs = compare(gpu, ref)
-    bad = {k: e for k, e in errs.items() if e >= (prog_tol if k in PROG else hist_tol)}
+    bad = bad_parts(errs, prog_tol, hist_tol)
+    if bad and sensitivity is not None:
+        floor = sensitivity()
+        bad = bad_parts(errs, prog_tol, hist_tol, floor)
+        assert not bad, (bad, errs, {k: floor.get(k) for k in bad})
     assert not bad, (bad, errs)
     return errs

@@ -16,6 +16,8 @@ CASES = {
     "c2_os": config.CONFIGS["c2_orr_sommerfeld"],
     "mixed_radix": config.small(nnx=24, nny=12, nnz=20, aphi=1.5, beta=0.75, dt=5e-4, re=300.0, re_p=1.0),
     "warp192": config.small(nnx=128, nny=128, nnz=16, aphi=2.0, beta=2.0 / 3.0, dt=2e-4, re=180.0, re_p=1.0),
+    "long_xz": config.small(nnx=384, nny=8, nnz=192, aphi=1.0, beta=0.5, dt=2e-4, re=550.0, re_p=1.0),
+    "long_y": config.small(nnx=8, nny=384, nnz=16, aphi=1.0, beta=0.5, dt=2e-4, re=550.0, re_p=1.0),
 }
 VEL = ("unp1", "vnp1", "wnp1")
 
@@ -58,7 +60,7 @@ def test_mixed_nonlinear_term(chflow_lib, name):
 
 
 @pytest.mark.parametrize("name,nsteps", [("small16", 50), ("c1_32", 50), ("c2_os", 50), ("mixed_radix", 30),
-                                          ("warp192", 30)])
+                                          ("warp192", 30), ("long_xz", 10), ("long_y", 20)])
 def test_mixed_steps_vs_fp64(chflow_lib, name, nsteps):
     cfg = CASES[name]
     st = fields.turbulent_start_state(cfg, seed=4)
@@ -94,5 +96,17 @@ def test_mixed_full_size(chflow_lib):
     st = fields.turbulent_start_state(cfg, seed=1)
     a = run(cfg, st, "fp64", 20, zpad=200)
     b = run(cfg, st, "mixed", 20, zpad=200)
+    errs = vel_err(b, a)
+    assert max(errs.values()) < 1e-5, errs
+
+
+def test_mixed_retau550_full_size(chflow_lib):
+    """The Re_tau 550 box, 384 x 193 x 384 on the exact 300-interval product
+    grid (2 * 300 > 3 * 192): both paths run it, and agree."""
+    cfg = config.CONFIGS["c4_retau550_384"]
+    st = fields.turbulent_start_state(cfg, seed=1)
+    a = run(cfg, st, "fp64", 5, zpad=300)
+    assert all(np.isfinite(a[k]).all() for k in VEL)
+    b = run(cfg, st, "mixed", 5, zpad=300)
     errs = vel_err(b, a)
     assert max(errs.values()) < 1e-5, errs

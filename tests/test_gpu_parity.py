@@ -17,7 +17,7 @@ from channel_flow_gb300 import Channel, ChannelError, config, fields
 from channel_flow_gb300.fields import FIELD_NAMES, MEAN_NAMES
 from exact_lamb import lamb
 from exact_mean import mean_h1
-from parity import PROG, check, compare, worst
+from parity import PROG, bad_parts, check, compare, oracle_sensitivity, worst
 
 pytestmark = pytest.mark.gpu
 
@@ -28,6 +28,10 @@ CASES = {
     "mixed_radix": config.small(nnx=24, nny=12, nnz=20, aphi=1.5, beta=0.75, dt=5e-4, re=300.0, re_p=1.0),
     # 3/2-padded lengths of 192: the register-FFT kernels of the 128-point directions
     "warp192": config.small(nnx=128, nny=128, nnz=16, aphi=2.0, beta=2.0 / 3.0, dt=2e-4, re=180.0, re_p=1.0),
+    # the long lines of the Re_tau 550 box (384 x 193 x 384): 576-point x rows
+    # and 768-point z lines (fewer lines per CTA), and 576-point y lines
+    "long_xz": config.small(nnx=384, nny=8, nnz=192, aphi=1.0, beta=0.5, dt=2e-4, re=550.0, re_p=1.0),
+    "long_y": config.small(nnx=8, nny=384, nnz=16, aphi=1.0, beta=0.5, dt=2e-4, re=550.0, re_p=1.0),
 }
 
 
@@ -74,8 +78,14 @@ def test_getnonlinear_matches_oracle(chflow_lib, oracle_mod, name):
     for k in ("omegaxnp1", "omegaznp1"):
         gs.pop(k)
         os_.pop(k)
-    errs = compare(gs, os_, names=tuple(k for k in os_))
-    bad = {k: e for k, e in errs.items() if e >= (1e-10 if k in PROG else 1e-7)}
+    names = tuple(k for k in os_)
+    errs = compare(gs, os_, names=names)
+    bad = bad_parts(errs, 1e-10, 1e-7)
+    if bad:
+        # e.g. 384-point x rows: h_g mixes alpha up to 191 with small H, a
+        # condition of ~5e5 (one-ulp input noise moves the oracle by 1e-10)
+        floor = oracle_sensitivity(oracle_mod, cfg, st, lambda o: o.getnonlinear(), names=names)
+        bad = bad_parts(errs, 1e-10, 1e-7, floor)
     assert not bad, (bad, errs)
 
 
@@ -113,7 +123,7 @@ def test_solve_matches_oracle(chflow_lib, oracle_mod, name):
 
 
 @pytest.mark.parametrize("name,nsteps", [("small16", 40), ("c1_32", 20), ("c2_os", 20), ("mixed_radix", 20),
-                                          ("warp192", 10)])
+                                          ("warp192", 10), ("long_xz", 3), ("long_y", 5)])
 def test_steps_match_oracle(chflow_lib, oracle_mod, name, nsteps):
     cfg = CASES[name]
     st = make_state(cfg, seed=7)
@@ -123,7 +133,14 @@ def test_steps_match_oracle(chflow_lib, oracle_mod, name, nsteps):
     g.getnonlinear(); g.solve()
     o.step(nsteps)
     g.step(nsteps)
-    check(g.download_state(), o.get_state(), 1e-10, 1e-7)
+
+    def run(o):
+        o.getnonlinear()
+        o.solve()
+        o.step(nsteps)
+
+    check(g.download_state(), o.get_state(), 1e-10, 1e-7,
+          sensitivity=lambda: oracle_sensitivity(oracle_mod, cfg, st, run))
 
 
 def test_lowmode_c1_steps(chflow_lib, oracle_mod):
@@ -238,3 +255,26 @@ def test_mean_lamb_accuracy(chflow_lib, oracle_mod, name):
     err_o = np.linalg.norm(got_o - exact) / np.linalg.norm(exact)
     err_g = np.linalg.norm(got_g - exact) / np.linalg.norm(exact)
     assert err_g <= max(2.0 * err_o, 1e-13), (err_g, err_o)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_step_graph_matches_direct_launches(chflow_lib, precision):
+    """chf_step replays a captured graph for pairs of steps; the state after
+    7 steps (3 replays and one direct step) is bit-identical to 7 direct
+    getnonlinear + solve calls, and to a second handle stepping 3 + 4."""
+    cfg = CASES["mixed_radix"]
+    st = make_state(cfg, seed=9)
+    with Channel(cfg, precision=precision) as a, Channel(cfg, precision=precision) as b, \
+            Channel(cfg, precision=precision) as c:
+        for g in (a, b, c):
+            g.upload_state(st)
+        a.step(7)
+        for _ in range(7):
+            b.getnonlinear()
+            b.solve()
+        c.step(3)
+        c.step(4)
+        outs = [g.download_state() for g in (a, b, c)]
+    for k in FIELD_NAMES + MEAN_NAMES:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+        assert np.array_equal(outs[0][k], outs[2][k]), k
