@@ -49,7 +49,7 @@ static std::vector<cd> twiddles(int L) {
 
 const char* const kKernelNames[K_COUNT] = {
     "k_zc2v", "k_yinv", "k_xprod", "k_yfwd", "k_zcurl", "k_solve", "k_diag",
-    "k_tc_split_z1", "k_tc_gemm_z1", "k_tc_split_z2", "k_tc_gemm_z2", "k_curl32", "k_tc_gemm_gl",
+    "k_tc_split_z1", "k_tc_gemm_z1", "k_tc_split_z2", "k_tc_gemm_z2", "k_curl", "k_tc_gemm_gl",
     "k_meanfix"};
 
 static cudaEvent_t take_event(Handle* h) {
@@ -126,7 +126,7 @@ static void release(chf_handle* h) {
   void* ptrs[] = {h->iapha, h->ibeta, h->t0, h->t2, h->t4, h->k2vals, h->xinv, h->xmean,
                   h->group_start, h->group_modes, h->tw_py, h->tw_px, h->tw_z2, h->tw_zm,
                   h->twf_py, h->twf_px, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
-                  h->agl, h->bimg, h->wz32, h->wy32, h->lc32};
+                  h->agl, h->bimg, h->wz32, h->wy32, h->lc64, h->aexp1, h->aexp2, h->aexp3, h->bexp};
   for (void* p : ptrs) cudaFree(p);
   for (auto& p : h->pending) {
     cudaEventDestroy(p.a);

@@ -33,16 +33,18 @@ struct Dims {
   __host__ __device__ size_t field_elems() const { return (size_t)NZ * KY * KX; }  // complex elements
 };
 
-// Tensor-core GEMM plan (k_tcgemm.cu): 128 x 128 output tiles, K in chunks
-// of at most TC_KC, operands split into TC_SPLITS bf16 planes.
+// Tensor-core GEMM plans (k_tcgemm.cu): K in chunks of at most TC_KC.
 constexpr int TC_KC = 64;
-constexpr int TC_SPLITS = 3;
-struct TcPlan {
+constexpr int FX_PLANES = 4;     // digit planes per operand
+constexpr int FX_NT = 64;        // columns per B tile
+struct FxPlan {
   int mvalid, mtiles, kpad, ntiles, nchunks;
   long ncols;
   int kc[16];
-  size_t chunk_off[16];
-  size_t tile_bytes;  // bytes of one 128-row/column tile image (all chunks and planes)
+  size_t a_chunk_off[16], b_chunk_off[16];
+  size_t a_tile_bytes, b_tile_bytes;  // one 128-row A tile / one 64-column B tile
+  __host__ __device__ size_t b_field_bytes() const { return (size_t)ntiles * b_tile_bytes; }
+  __host__ __device__ size_t bexp_stride() const { return (size_t)ntiles * FX_NT; }
 };
 
 template <typename T>
@@ -97,13 +99,15 @@ struct Handle {
 
   // mixed-precision path (k_mixed.cu): FP32 transforms, tcgen05 GEMMs
   int* dev_status = nullptr;  // device error word (tensor-core pipeline timeouts)
-  TcPlan tz1{}, tz2{}, tgl{};
+  FxPlan tz1{}, tz2{}, tgl{};
   uint8_t *az1 = nullptr, *az2 = nullptr, *agl = nullptr;  // constant A images
   uint8_t* bimg = nullptr;    // per-step B images
+  int *aexp1 = nullptr, *aexp2 = nullptr, *aexp3 = nullptr;  // row exponents of the A images
+  int* bexp = nullptr;        // per-step column exponents of the fixed-point B images
   size_t bimg_bytes = 0;
   cf* wz32 = nullptr;         // 6 x [MP][KY][KX]
   cf* wy32 = nullptr;         // 6 x [MP][PY][KX]
-  float* lc32 = nullptr;      // 3 x [NZ][2 modes] Lamb-vector coefficients
+  double* lc64 = nullptr;     // 3 x [NZ][2 modes] Lamb-vector coefficients (exact z transform)
 
   // statistics
   int kernels_per_step = 0;
@@ -154,14 +158,19 @@ int launch_nonlinear_fp64(Handle* h);
 template <typename T>
 int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const cplx<T>* tw_px);
 // launchers (k_tcgemm.cu, k_mixed.cu)
-TcPlan make_tc_plan(int mvalid, int kvalid, long ncols);
-std::vector<uint8_t> make_a_image(const TcPlan& p, const std::vector<double>& a, int M, int K);
+// Wall-normal transforms as tcgen05 GEMMs (k_tcgemm.cu): operands as FX_PLANES planes of
+// signed 7-bit integer digits below a per-row (A) / per-column (B) power of
+// two, products of digits accumulated exactly per level i + j <= 3.
+// 128-row A tiles, 64-column B tiles (two CTAs per SM fit in TMEM).
+FxPlan make_fx_plan(int mvalid, int kvalid, long ncols);
+std::vector<uint8_t> make_a_image_fx(const FxPlan& p, const std::vector<double>& a, int M, int K,
+                                     std::vector<int>& row_exp);
 template <typename OutT>
-int launch_tc_gemm(Handle* h, const TcPlan& p, const uint8_t* aimg, const uint8_t* bimg,
-                   size_t bfield_stride, const Ptr8<OutT>& outs, int nfields, size_t ldc, int kid);
+int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int* aexp, const uint8_t* bimg,
+                      const int* bexp, const Ptr8<OutT>& outs, int nfields, size_t ldc, int kid);
 template <typename InT>
-int launch_tc_split(Handle* h, const TcPlan& p, const Ptr8<const InT>& ins, int kvalid, uint8_t* bimg,
-                    size_t bfield_stride, int nfields, int kid);
+int launch_tc_split_fx(Handle* h, const FxPlan& p, const Ptr8<const InT>& ins, int kvalid, uint8_t* bimg,
+                       int* bexp, int nfields, int kid);
 int setup_mixed(Handle* h);
 int launch_nonlinear_mixed(Handle* h);
 // launchers (k_solve.cu)

@@ -2,15 +2,16 @@
 //
 // The state and the implicit solves stay FP64 (k_solve.cu).  The nonlinear
 // term is formed with FP32 FFTs/products and tcgen05 tensor-core GEMMs for
-// the wall-normal Chebyshev transforms (k_tcgemm.cu):
+// the wall-normal Chebyshev transforms, accumulated exactly on fixed-point
+// digits (k_tcgemm.cu):
 //
-//   k_tc_split_z1   six FP64 fields [NZ][2 modes] -> bf16x3 tile images
+//   k_tc_split_z1   six FP64 fields [NZ][2 modes] -> fixed-point digit images
 //   k_tc_gemm_z1    values on the product grid: V = T1 C, T1[p][n] = cos(pi n p / MZ)
 //   k_yinv/xprod/yfwd (FP32)   as in the FP64 path (k_nonlinear.cu)
-//   k_tc_split_z2   the three Lamb components [MP][2 modes] -> tile images
-//   k_tc_gemm_z2    Chebyshev coefficients: L = W V, W = DCT-I weights on the
-//                   product grid, rows 0..N (truncation, REF:1686-1704)
-//   k_curl32        dz of H1, H3 by warp scans, h_v = k^2 H2 + i a D H1 + i b D H3,
+//   k_tc_split_z2   the three Lamb components [MP][2 modes] -> digit images
+//   k_tc_gemm_z2    Chebyshev coefficients in FP64: L = W V, W = DCT-I weights
+//                   on the product grid, rows 0..N (truncation, REF:1686-1704)
+//   k_curl          dz of H1, H3 by FP64 warp scans, h_v = k^2 H2 + i a D H1 + i b D H3,
 //                   h_g = i a H3 - i b H1 (REF:1502-1540), written as tile images
 //   k_tc_gemm_gl    Gauss-Lobatto values T0 h (REF:1573-1609) into the FP64
 //                   history buffers
@@ -26,140 +27,156 @@
 #include <vector>
 
 #include "chf_internal.h"
+#include "tc_dev.cuh"
 
 namespace chf {
 
 namespace {
 
-constexpr int CM = 16;          // modes per CTA in k_curl32
+constexpr int CM = 8;           // modes per CTA in k_curl
 constexpr int CURL_THREADS = 256;
 
-// dz by one warp on FP32 data (suffix sums per parity class, see k_solve.cu)
-__device__ __forceinline__ void warp_deriv_f(const float* a, int as, float* b, int bs, int N) {
+// dz (REF:570-599) of a[0..N] (stride as) into b (stride bs) by one warp, in
+// FP64: suffix sums per parity class, lane-local then a warp scan (the scheme
+// of k_solve.cu)
+__device__ __forceinline__ void warp_deriv_d(const double* a, int as, double* b, int bs, int N) {
   const int lane = threadIdx.x & 31;
   const int E = (N + 32) / 32;
   const int i0 = lane * E;
-  float te = 0.f, to = 0.f;
+  double te = 0.0, to = 0.0;
   for (int q = 0; q < E; ++q) {
     int j = i0 + q;
     if (j <= N) {
-      float g = 2.0f * (float)j * a[j * as];
+      double g = 2.0 * (double)j * a[j * as];
       if (j & 1) to += g; else te += g;
     }
   }
-  float se = te, so = to;
+  double se = te, so = to;
   for (int off = 1; off < 32; off <<= 1) {
-    float ue = __shfl_down_sync(0xffffffffu, se, off);
-    float uo = __shfl_down_sync(0xffffffffu, so, off);
+    double ue = __shfl_down_sync(0xffffffffu, se, off);
+    double uo = __shfl_down_sync(0xffffffffu, so, off);
     if (lane + off < 32) { se += ue; so += uo; }
   }
-  float re_ = se - te, ro = so - to;
+  double re_ = se - te, ro = so - to;
   for (int q = E - 1; q >= 0; --q) {
     int i = i0 + q;
     if (i <= N) {
-      float bi = (i & 1) ? re_ : ro;
-      if (i == 0) bi *= 0.5f;
+      double bi = (i & 1) ? re_ : ro;
+      if (i == 0) bi *= 0.5;
       b[i * bs] = bi;
-      float g = 2.0f * (float)i * a[i * as];
+      double g = 2.0 * (double)i * a[i * as];
       if (i & 1) ro += g; else re_ += g;
     }
   }
   __syncwarp();
 }
 
-__device__ __forceinline__ void split3(float x, uint16_t* h) {
-  __nv_bfloat16 b0 = __float2bfloat16_rn(x);
-  float r1 = x - __bfloat162float(b0);
-  __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
-  float r2 = r1 - __bfloat162float(b1);
-  __nv_bfloat16 b2 = __float2bfloat16_rn(r2);
-  h[0] = __bfloat16_as_ushort(b0);
-  h[1] = __bfloat16_as_ushort(b1);
-  h[2] = __bfloat16_as_ushort(b2);
-}
-
 // grid (ceil(modes / CM)), CURL_THREADS threads.
-// lc: 3 fields [NZ][ncols] FP32 (H1, H2, H3 coefficients); out: tile images
-// for the GL GEMM, field 0 = h_v, field 1 = h_g (mode (0,0) carries H1, H3).
-__global__ void __launch_bounds__(CURL_THREADS) k_curl32(const float* __restrict__ lc,
-                                                         const double* __restrict__ iapha,
-                                                         const double* __restrict__ ibeta, Dims d,
-                                                         const __grid_constant__ TcPlan plan,
-                                                         uint8_t* __restrict__ bimg, size_t bfield_stride) {
+// lc: 3 fields [NZ][ncols] FP64 (H1, H2, H3 coefficients from the exact z
+// transform); out: fixed-point digit images and column exponents for the GL
+// GEMM (k_tcgemm.cu layout), field 0 = h_v, field 1 = h_g (mode (0,0)
+// carries H1, H3).  FP64 up to h_v, h_g: h_v is a small remainder of
+// k^2 H2 + i a D H1 + i b D H3 (the gradient part of the Lamb vector
+// cancels), so FP32 derivatives would leave an error ~100x FP32 rounding in
+// it.  h_v, h_g are then rounded to FP32 (a relative error per coefficient)
+// and split into digits below their column's power of two.
+__global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict__ lc,
+                                                       const double* __restrict__ iapha,
+                                                       const double* __restrict__ ibeta, Dims d,
+                                                       const __grid_constant__ FxPlan plan,
+                                                       uint8_t* __restrict__ bimg, int* __restrict__ bexp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int NZ = d.NZ, N = d.N;
   const long modes = d.modes(), ncols = 2 * modes;
-  float* L = reinterpret_cast<float*>(smem_raw);       // [3][NZ][CM][2]
-  float* D = L + 3 * NZ * CM * 2;                      // [4][CM][NZ]: D H1.re, D H1.im, D H3.re, D H3.im
+  double* L = reinterpret_cast<double*>(smem_raw);     // [3][NZ][CM][2]
+  double* D = L + 3 * NZ * CM * 2;                     // [4][CM][NZ]: D H1.re, D H1.im, D H3.re, D H3.im
+  float* Hs = reinterpret_cast<float*>(D + 4 * CM * NZ);  // [2][NZ][CM][2]: h_v, h_g
+  __shared__ int s_e[2][CM * 2];
   const long m0 = (long)blockIdx.x * CM;
   for (int t = threadIdx.x; t < 3 * NZ * CM * 2; t += blockDim.x) {
     int c = t % (CM * 2), n = (t / (CM * 2)) % NZ, f = t / (CM * 2 * NZ);
     long col = 2 * m0 + c;
-    L[t] = col < ncols ? lc[(size_t)f * NZ * ncols + (size_t)n * ncols + col] : 0.f;
+    L[t] = col < ncols ? lc[(size_t)f * NZ * ncols + (size_t)n * ncols + col] : 0.0;
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5;
   for (int task = warp; task < 4 * CM; task += CURL_THREADS / 32) {
     int comp = task / CM, l = task % CM;
     int f = comp < 2 ? 0 : 2, reim = comp & 1;
-    warp_deriv_f(L + (size_t)f * NZ * CM * 2 + l * 2 + reim, CM * 2, D + ((size_t)comp * CM + l) * NZ, 1, N);
+    warp_deriv_d(L + (size_t)f * NZ * CM * 2 + l * 2 + reim, CM * 2, D + ((size_t)comp * CM + l) * NZ, 1, N);
   }
   __syncthreads();
-  // one thread per (column c of this CTA, 8-row group g): 8 values per field
+  for (int t = threadIdx.x; t < NZ * CM * 2; t += blockDim.x) {
+    const int c = t % (CM * 2), n = t / (CM * 2);
+    const int l = c / 2, reim = c % 2;
+    const long m = m0 + l;
+    float v = 0.f, w = 0.f;
+    if (m < modes) {
+      const int kx = (int)(m % d.KX), ky = (int)(m / d.KX);
+      const double a = iapha[kx], b = ibeta[ky], k2 = a * a + b * b;
+      const double* h1 = L + ((size_t)0 * NZ + n) * CM * 2 + l * 2;
+      const double* h2 = L + ((size_t)1 * NZ + n) * CM * 2 + l * 2;
+      const double* h3 = L + ((size_t)2 * NZ + n) * CM * 2 + l * 2;
+      const double d1r = D[(0 * CM + l) * NZ + n], d1i = D[(1 * CM + l) * NZ + n];
+      const double d3r = D[(2 * CM + l) * NZ + n], d3i = D[(3 * CM + l) * NZ + n];
+      if (m == 0) {
+        v = (float)h1[reim];
+        w = (float)h3[reim];
+      } else if (reim == 0) {
+        v = (float)(k2 * h2[0] - a * d1i - b * d3i);   // h_v = k2 H2 + i a D H1 + i b D H3
+        w = (float)(-a * h3[1] + b * h1[1]);           // h_g = i a H3 - i b H1
+      } else {
+        v = (float)(k2 * h2[1] + a * d1r + b * d3r);
+        w = (float)(a * h3[0] - b * h1[0]);
+      }
+    }
+    Hs[(size_t)n * CM * 2 + c] = v;
+    Hs[(size_t)(NZ + n) * CM * 2 + c] = w;
+  }
+  __syncthreads();
+  // column exponents: max |value| < 2^e
+  if (threadIdx.x < 2 * CM * 2) {
+    const int f = threadIdx.x / (CM * 2), c = threadIdx.x % (CM * 2);
+    float mx = 0.f;
+    for (int n = 0; n < NZ; ++n) mx = fmaxf(mx, fabsf(Hs[(size_t)(f * NZ + n) * CM * 2 + c]));
+    int e = 0;
+    if (mx > 0.f) (void)frexpf(mx, &e);
+    s_e[f][c] = e;
+    const long col = 2 * m0 + c;
+    if (col < ncols) bexp[(size_t)f * plan.bexp_stride() + col] = e;
+  }
+  __syncthreads();
+  // one thread per (column c of this CTA, 8-row group g): 8 digits per plane
+  // and field, one 16-byte store each
   const int groups = plan.kpad / 8;
   for (int t = threadIdx.x; t < CM * 2 * groups; t += blockDim.x) {
     const int c = t % (CM * 2), g = t / (CM * 2);
-    const int l = c / 2, reim = c % 2;
-    const long m = m0 + l;
     const long col = 2 * m0 + c;
     if (col >= ncols) continue;
-    const int kx = (int)(m % d.KX), ky = (int)(m / d.KX);
-    const double a = iapha[kx], b = ibeta[ky], k2 = a * a + b * b;
-    const bool mean = (m == 0);
-    uint16_t hv[3][8], hg[3][8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int n = 8 * g + q;
-      float v = 0.f, w = 0.f;
-      if (n < NZ) {
-        const float* h1 = L + ((size_t)0 * NZ + n) * CM * 2 + l * 2;
-        const float* h2 = L + ((size_t)1 * NZ + n) * CM * 2 + l * 2;
-        const float* h3 = L + ((size_t)2 * NZ + n) * CM * 2 + l * 2;
-        const double d1r = D[(0 * CM + l) * NZ + n], d1i = D[(1 * CM + l) * NZ + n];
-        const double d3r = D[(2 * CM + l) * NZ + n], d3i = D[(3 * CM + l) * NZ + n];
-        if (mean) {
-          v = h1[reim];
-          w = h3[reim];
-        } else if (reim == 0) {
-          v = (float)(k2 * h2[0] - a * d1i - b * d3i);   // h_v = k2 H2 + i a D H1 + i b D H3
-          w = (float)(-a * h3[1] + b * h1[1]);           // h_g = i a H3 - i b H1
-        } else {
-          v = (float)(k2 * h2[1] + a * d1r + b * d3r);
-          w = (float)(a * h3[0] - b * h1[0]);
-        }
-      }
-      uint16_t sv[3], sw[3];
-      split3(v, sv);
-      split3(w, sw);
-      for (int pl = 0; pl < 3; ++pl) {
-        hv[pl][q] = sv[pl];
-        hg[pl][q] = sw[pl];
-      }
-    }
-    const int nt = (int)(col / 128), r = (int)(col % 128);
+    const int nt = (int)(col / FX_NT), r = (int)(col % FX_NT);
     const int ch = (8 * g) / TC_KC, kl = 8 * g - ch * TC_KC;
-    const uint32_t pbytes = 128u * plan.kc[ch] * 2u;
-    const size_t off = ((size_t)(kl / 8) * 16 + r / 8) * 128 + (r % 8) * 16;
+    const uint32_t pbytes = (uint32_t)FX_NT * plan.kc[ch] * 2u;
+    const size_t off = ((size_t)(kl / 8) * (FX_NT / 8) + r / 8) * 128 + (r % 8) * 16;
     for (int f = 0; f < 2; ++f) {
-      uint8_t* base = bimg + (size_t)f * bfield_stride + (size_t)nt * plan.tile_bytes + plan.chunk_off[ch];
-      for (int pl = 0; pl < 3; ++pl) {
-        const uint16_t* s = f == 0 ? hv[pl] : hg[pl];
-        uint4 v;
-        v.x = (uint32_t)s[0] | ((uint32_t)s[1] << 16);
-        v.y = (uint32_t)s[2] | ((uint32_t)s[3] << 16);
-        v.z = (uint32_t)s[4] | ((uint32_t)s[5] << 16);
-        v.w = (uint32_t)s[6] | ((uint32_t)s[7] << 16);
-        *reinterpret_cast<uint4*>(base + (size_t)pl * pbytes + off) = v;
+      uint16_t hd[FX_PLANES][8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int n = 8 * g + q;
+        const float x = n < NZ ? Hs[(size_t)(f * NZ + n) * CM * 2 + c] : 0.f;
+        float dg[FX_PLANES];
+        tc::fx_digits_f(x, s_e[f][c], dg);
+#pragma unroll
+        for (int i = 0; i < FX_PLANES; ++i) hd[i][q] = tc::bf16_bits(dg[i]);
+      }
+      uint8_t* base = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes + plan.b_chunk_off[ch];
+#pragma unroll
+      for (int pl = 0; pl < FX_PLANES; ++pl) {
+        uint4 u;
+        u.x = (uint32_t)hd[pl][0] | ((uint32_t)hd[pl][1] << 16);
+        u.y = (uint32_t)hd[pl][2] | ((uint32_t)hd[pl][3] << 16);
+        u.z = (uint32_t)hd[pl][4] | ((uint32_t)hd[pl][5] << 16);
+        u.w = (uint32_t)hd[pl][6] | ((uint32_t)hd[pl][7] << 16);
+        *reinterpret_cast<uint4*>(base + (size_t)pl * pbytes + off) = u;
       }
     }
   }
@@ -199,9 +216,12 @@ int setup_mixed(Handle* h) {
   const Dims& d = h->d;
   const long cols = 2 * d.modes();
   const int N = d.N, NZ = d.NZ, MZ = d.MZ, MP = d.MP;
-  h->tz1 = make_tc_plan(MP, NZ, cols);
-  h->tz2 = make_tc_plan(NZ, MP, cols);
-  h->tgl = make_tc_plan(NZ, NZ, cols);
+  // z transforms with exact accumulation (fixed-point digits, k_tcgemm.cu);
+  // the GL evaluation of h_v, h_g is not differentiated afterwards and keeps
+  // the floating bf16x3 split
+  h->tz1 = make_fx_plan(MP, NZ, cols);
+  h->tz2 = make_fx_plan(NZ, MP, cols);
+  h->tgl = make_fx_plan(NZ, NZ, cols);
   std::vector<double> a1((size_t)MP * NZ), a2((size_t)NZ * MP), a3((size_t)NZ * NZ);
   for (int p = 0; p < MP; ++p)
     for (int n = 0; n < NZ; ++n) a1[(size_t)p * NZ + n] = cospi_ratio((long)n * p, MZ);
@@ -218,18 +238,28 @@ int setup_mixed(Handle* h) {
     if (!cuda_ok(h, cudaMalloc((void**)dst, img.size()), what)) return false;
     return cuda_ok(h, cudaMemcpy(*dst, img.data(), img.size(), cudaMemcpyHostToDevice), what);
   };
-  if (!upload(&h->az1, make_a_image(h->tz1, a1, MP, NZ), "A image z1") ||
-      !upload(&h->az2, make_a_image(h->tz2, a2, NZ, MP), "A image z2") ||
-      !upload(&h->agl, make_a_image(h->tgl, a3, NZ, NZ), "A image gl"))
+  std::vector<int> e1, e2, e3;
+  auto upload_int = [h](int** dst, const std::vector<int>& v, const char* what) {
+    if (!cuda_ok(h, cudaMalloc((void**)dst, sizeof(int) * v.size()), what)) return false;
+    return cuda_ok(h, cudaMemcpy(*dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice), what);
+  };
+  if (!upload(&h->az1, make_a_image_fx(h->tz1, a1, MP, NZ, e1), "A image z1") ||
+      !upload(&h->az2, make_a_image_fx(h->tz2, a2, NZ, MP, e2), "A image z2") ||
+      !upload(&h->agl, make_a_image_fx(h->tgl, a3, NZ, NZ, e3), "A image gl") ||
+      !upload_int(&h->aexp1, e1, "A exponents z1") || !upload_int(&h->aexp2, e2, "A exponents z2") ||
+      !upload_int(&h->aexp3, e3, "A exponents gl"))
     return CHF_E_NOMEM;
-  h->bimg_bytes = std::max({(size_t)6 * h->tz1.ntiles * h->tz1.tile_bytes,
-                            (size_t)3 * h->tz2.ntiles * h->tz2.tile_bytes,
-                            (size_t)2 * h->tgl.ntiles * h->tgl.tile_bytes});
+  if (!cuda_ok(h, cudaMalloc((void**)&h->bexp,
+                            sizeof(int) * 6 * std::max(h->tz1.bexp_stride(), h->tz2.bexp_stride())),
+               "B exponents"))
+    return CHF_E_NOMEM;
+  h->bimg_bytes = std::max({(size_t)6 * h->tz1.b_field_bytes(), (size_t)3 * h->tz2.b_field_bytes(),
+                            (size_t)2 * h->tgl.b_field_bytes()});
   if (!cuda_ok(h, cudaMalloc((void**)&h->bimg, h->bimg_bytes), "B images") ||
       !cuda_ok(h, cudaMemsetAsync(h->bimg, 0, h->bimg_bytes, h->stream), "B images") ||
       !cuda_ok(h, cudaMalloc((void**)&h->wz32, sizeof(cf) * 6 * (size_t)MP * d.modes()), "wz32") ||
       !cuda_ok(h, cudaMalloc((void**)&h->wy32, sizeof(cf) * 6 * (size_t)MP * d.PY * d.KX), "wy32") ||
-      !cuda_ok(h, cudaMalloc((void**)&h->lc32, sizeof(float) * 3 * (size_t)NZ * cols), "lc32"))
+      !cuda_ok(h, cudaMalloc((void**)&h->lc64, sizeof(double) * 3 * (size_t)NZ * cols), "lc64"))
     return CHF_E_NOMEM;
   // FP32 twiddles
   struct {
@@ -257,41 +287,47 @@ int launch_nonlinear_mixed(Handle* h) {
   Ptr8<const double> in6{};
   const int order[6] = {F_U, F_V, F_W, F_OX, F_OY, F_OZ};
   for (int i = 0; i < 6; ++i) in6.p[i] = reinterpret_cast<const double*>(h->f[order[i]]);
-  const size_t fs1 = (size_t)h->tz1.ntiles * h->tz1.tile_bytes;
-  if ((rc = launch_tc_split<double>(h, h->tz1, in6, d.NZ, h->bimg, fs1, 6, K_SPLIT_Z1)) != CHF_OK) return rc;
+  if ((rc = launch_tc_split_fx<double>(h, h->tz1, in6, d.NZ, h->bimg, h->bexp, 6, K_SPLIT_Z1)) != CHF_OK)
+    return rc;
   Ptr8<float> o6{};
   for (int i = 0; i < 6; ++i) o6.p[i] = reinterpret_cast<float*>(h->wz32 + (size_t)i * d.MP * modes);
-  if ((rc = launch_tc_gemm<float>(h, h->tz1, h->az1, h->bimg, fs1, o6, 6, cols, K_GEMM_Z1)) != CHF_OK) return rc;
+  if ((rc = launch_tc_gemm_fx<float>(h, h->tz1, h->az1, h->aexp1, h->bimg, h->bexp, o6, 6, cols,
+                                     K_GEMM_Z1)) != CHF_OK)
+    return rc;
   // y and x transforms with the products, FP32
   if ((rc = launch_xy<float>(h, h->wz32, h->wy32, h->twf_py, h->twf_px)) != CHF_OK) return rc;
   // z: values -> coefficients 0..N
   Ptr8<const float> in3{};
   for (int i = 0; i < 3; ++i) in3.p[i] = reinterpret_cast<const float*>(h->wz32 + (size_t)i * d.MP * modes);
-  const size_t fs2 = (size_t)h->tz2.ntiles * h->tz2.tile_bytes;
-  if ((rc = launch_tc_split<float>(h, h->tz2, in3, d.MP, h->bimg, fs2, 3, K_SPLIT_Z2)) != CHF_OK) return rc;
-  Ptr8<float> o3{};
-  for (int i = 0; i < 3; ++i) o3.p[i] = h->lc32 + (size_t)i * d.NZ * cols;
-  if ((rc = launch_tc_gemm<float>(h, h->tz2, h->az2, h->bimg, fs2, o3, 3, cols, K_GEMM_Z2)) != CHF_OK) return rc;
-  // curl / projection -> tile images for the GL transform
-  const size_t fs3 = (size_t)h->tgl.ntiles * h->tgl.tile_bytes;
+  if ((rc = launch_tc_split_fx<float>(h, h->tz2, in3, d.MP, h->bimg, h->bexp, 3, K_SPLIT_Z2)) != CHF_OK)
+    return rc;
+  Ptr8<double> o3{};
+  for (int i = 0; i < 3; ++i) o3.p[i] = h->lc64 + (size_t)i * d.NZ * cols;
+  if ((rc = launch_tc_gemm_fx<double>(h, h->tz2, h->az2, h->aexp2, h->bimg, h->bexp, o3, 3, cols,
+                                      K_GEMM_Z2)) != CHF_OK)
+    return rc;
+  // curl / projection -> digit images for the GL transform
   {
-    size_t smem = sizeof(float) * ((size_t)3 * d.NZ * CM * 2 + (size_t)4 * CM * d.NZ);
+    size_t smem = sizeof(double) * ((size_t)3 * d.NZ * CM * 2 + (size_t)4 * CM * d.NZ) +
+                  sizeof(float) * (size_t)2 * d.NZ * CM * 2;
     if (smem > 48 * 1024 &&
-        !cuda_ok(h, cudaFuncSetAttribute(k_curl32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                 "k_curl32 smem"))
+        !cuda_ok(h, cudaFuncSetAttribute(k_curl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                 "k_curl smem"))
       return CHF_E_CUDA;
     cudaEvent_t ev;
     prof_begin(h, K_CURL32, &ev);
-    k_curl32<<<(unsigned)((modes + CM - 1) / CM), CURL_THREADS, smem, h->stream>>>(
-        h->lc32, h->iapha, h->ibeta, d, h->tgl, h->bimg, fs3);
+    k_curl<<<(unsigned)((modes + CM - 1) / CM), CURL_THREADS, smem, h->stream>>>(
+        h->lc64, h->iapha, h->ibeta, d, h->tgl, h->bimg, h->bexp);
     prof_end(h, K_CURL32, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_curl32")) return CHF_E_CUDA;
+    if (!cuda_ok(h, cudaGetLastError(), "k_curl")) return CHF_E_CUDA;
   }
   // Gauss-Lobatto values of h_v, h_g -> the unp1 / wnp1 buffers (FP64)
   Ptr8<double> o2{};
   o2.p[0] = reinterpret_cast<double*>(h->f[F_U]);
   o2.p[1] = reinterpret_cast<double*>(h->f[F_W]);
-  if ((rc = launch_tc_gemm<double>(h, h->tgl, h->agl, h->bimg, fs3, o2, 2, cols, K_GEMM_GL)) != CHF_OK) return rc;
+  if ((rc = launch_tc_gemm_fx<double>(h, h->tgl, h->agl, h->aexp3, h->bimg, h->bexp, o2, 2, cols,
+                                      K_GEMM_GL)) != CHF_OK)
+    return rc;
   {
     cudaEvent_t ev;
     prof_begin(h, K_MEANFIX, &ev);

@@ -1,0 +1,73 @@
+// tc_dev.cuh -- device helpers shared by the tcgen05 GEMM kernels: shared
+// addresses, bounded mbarrier waits on %globaltimer, the no-swizzle K-major
+// shared-memory descriptor and the bf16 x bf16 -> f32 instruction
+// descriptor for 128 x 128 tiles, and the fixed-point digit split of
+// k_tcgemm.cu.
+#pragma once
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+namespace chf {
+namespace tc {
+
+constexpr int TC_THREADS = 128;
+constexpr long WAIT_NS = 1000000000L;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+  const uint64_t t0 = gtimer();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (ok) return true;
+    if ((long)(gtimer() - t0) > WAIT_NS) return false;
+  }
+}
+
+// no-swizzle K-major shared-memory matrix descriptor
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// instruction descriptor: D = F32, A = B = BF16, both K-major, M = 128, N = 128
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+
+// FX_PLANES digits of x * 2^-e (|x| < 2^e), each the rint of the scaled
+// remainder, exact in float (FX_PLANES from chf_internal.h)
+__device__ __forceinline__ void fx_digits_f(float x, int e, float* dg) {
+  float y = scalbnf(x, 7 - e);
+#pragma unroll
+  for (int i = 0; i < FX_PLANES; ++i) {
+    const float di = rintf(y);
+    dg[i] = di;
+    y = (y - di) * 128.0f;
+  }
+}
+
+__device__ __forceinline__ uint16_t bf16_bits(float f) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(f));  // exact: |f| <= 128, integer
+}
+
+}  // namespace tc
+}  // namespace chf

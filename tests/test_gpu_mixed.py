@@ -110,3 +110,20 @@ def test_mixed_retau550_full_size(chflow_lib):
     b = run(cfg, st, "mixed", 5, zpad=300)
     errs = vel_err(b, a)
     assert max(errs.values()) < 1e-5, errs
+
+
+def test_mixed_accuracy_after_1000_steps(chflow_lib):
+    """The mixed form's accuracy target at Re_tau 180, 128 x 129 x 128: the
+    velocity (u, v, w) rel-L2 against the FP64 path after 1000 steps from the
+    same start is at most 1e-5."""
+    cfg = config.CONFIGS["c3_retau180_128"]
+    st = fields.turbulent_start_state(cfg, seed=0)
+    a = run(cfg, st, "fp64", 1000, zpad=200)
+    b = run(cfg, st, "mixed", 1000, zpad=200)
+    num = den = 0.0
+    for k in VEL:
+        pa, pb = split(a[k], k)[k], split(b[k], k)[k]
+        num += float(np.sum((pb - pa) ** 2))
+        den += float(np.sum(pa ** 2))
+    vel = (num / den) ** 0.5
+    assert vel <= 1e-5, (vel, vel_err(b, a))

@@ -15,9 +15,10 @@ NSTEPS, CHUNK, SKIP = 5000, 250, 2
 
 # Relative tolerances on Re(sigma) (amplitude fit, energy fit) and Im(sigma).
 # The FP64 bars leave room for the O(dt^2) error of the AB2/CN scheme and the
-# start-up transient; the mixed path adds FP32 rounding of a 1e-6 perturbation
-# carried on an O(1) base flow in the nonlinear products.
-TOL = {"fp64": (1e-3, 5e-3, 1e-4), "mixed": (1e-2, 2e-2, 1e-4)}
+# start-up transient.  The mixed path carries the 1e-6 perturbation on an
+# O(1) base flow in FP32 physical values, whose rounding (one ulp of 1 is
+# 1.2e-7) is a few per cent of the perturbation at every point.
+TOL = {"fp64": (1e-3, 5e-3, 1e-4), "mixed": (1e-2, 2e-2, 3e-4)}
 
 
 def _gpu_history(precision, nsteps=NSTEPS):

@@ -35,6 +35,19 @@ CASES = {
 }
 
 
+def exact_zpad(n):
+    """Smallest 2,3,5-smooth M with 2M > 3n: the smallest exact product grid."""
+    m = 3 * n // 2 + 1
+    while True:
+        r = m
+        for p in (2, 3, 5):
+            while r % p == 0:
+                r //= p
+        if r == 1:
+            return m
+        m += 1
+
+
 def make_state(cfg, seed=3):
     return fields.reference_like_state(cfg, seed=seed, epsilon=0.3, noise=0.02, gamma=5.0)
 
@@ -122,6 +135,14 @@ def test_solve_matches_oracle(chflow_lib, oracle_mod, name):
     check(g.download_state(), o.get_state(), 1e-10, 1e-7)
 
 
+# Per-case bar for the prognostic arrays after several steps.  long_xz: the
+# reference algorithm's plane average H(0,0) on this 384-point box is only
+# ~2.5e-8 accurate against extended precision (the GPU's is pinned to be at
+# least as accurate in test_mean_lamb_accuracy[long_xz]); the mean spanwise
+# flow w0 and, through it, the nonlinear histories inherit that difference.
+STEP_TOL = {"long_xz": 1e-8}
+
+
 @pytest.mark.parametrize("name,nsteps", [("small16", 40), ("c1_32", 20), ("c2_os", 20), ("mixed_radix", 20),
                                           ("warp192", 10), ("long_xz", 3), ("long_y", 5)])
 def test_steps_match_oracle(chflow_lib, oracle_mod, name, nsteps):
@@ -139,8 +160,21 @@ def test_steps_match_oracle(chflow_lib, oracle_mod, name, nsteps):
         o.solve()
         o.step(nsteps)
 
-    check(g.download_state(), o.get_state(), 1e-10, 1e-7,
-          sensitivity=lambda: oracle_sensitivity(oracle_mod, cfg, st, run))
+    gs = g.download_state()
+
+    def floor():
+        # rounding-level spread of the result: the oracle's response to
+        # one-ulp input noise, and the GPU path on another exact product
+        # grid (same mathematics, different rounding)
+        f = oracle_sensitivity(oracle_mod, cfg, st, run)
+        with Channel(cfg, zpad=exact_zpad(cfg.nnz)) as g2:
+            g2.upload_state(st)
+            g2.getnonlinear(); g2.solve()
+            g2.step(nsteps)
+            alt = compare(g2.download_state(), gs)
+        return {k: max(f.get(k, 0.0), alt.get(k, 0.0)) for k in set(f) | set(alt)}
+
+    check(gs, o.get_state(), STEP_TOL.get(name, 1e-10), 1e-7, sensitivity=floor)
 
 
 def test_lowmode_c1_steps(chflow_lib, oracle_mod):
@@ -238,7 +272,7 @@ def test_full_size_two_steps(chflow_lib, oracle_mod):
     check(g.download_state(), o.get_state(), 1e-10, 1e-6)
 
 
-@pytest.mark.parametrize("name", ["c1_32", "c2_os", "small16"])
+@pytest.mark.parametrize("name", ["c1_32", "c2_os", "small16", "long_xz"])
 def test_mean_lamb_accuracy(chflow_lib, oracle_mod, name):
     """H1(0,0) (left in omegaxnp1 by getnonlinear, REF:1489-1496) against its
     extended-precision value: the GPU must be at least as accurate as the
