@@ -23,7 +23,7 @@ EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
            "chf_download_state", "chf_getnonlinear", "chf_solve", "chf_step",
            "chf_synchronize", "chf_diagnostics", "chf_kernels_per_step", "chf_device_field",
            "chf_set_stream", "chf_profile_enable", "chf_profile_reset", "chf_profile_read",
-           "chf_diagnostics_static")
+           "chf_diagnostics_static", "chf_write_restart", "chf_read_restart")
 
 
 class ChannelError(RuntimeError):
@@ -77,6 +77,8 @@ def load_library(path: str = None):
     L.chf_profile_read.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
                                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     L.chf_diagnostics_static.argtypes = [ctypes.c_int] * 3 + [vp] * 6 + [dp, ctypes.POINTER(CDiag), vp]
+    for name in ("chf_write_restart", "chf_read_restart"):
+        getattr(L, name).argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     L.chf_last_error.restype = ctypes.c_char_p
@@ -180,6 +182,16 @@ class Channel:
         return {"energy": d.energy, "wall_shear_top": d.wall_shear_top,
                 "wall_shear_bottom": d.wall_shear_bottom, "max_abs": d.max_abs,
                 "finite": bool(d.finite)}
+
+    def write_restart(self, directory: str, nproc: int = 1, tag: int = 2, istep: int = -1):
+        """The reference's per-rank restart files (output, poiseuilleflow.f90:2460-2504)
+        from the device state; call after getnonlinear, as the reference does."""
+        self._check(self.L.chf_write_restart(self.h, os.fsencode(directory), int(nproc), int(tag), int(istep)))
+
+    def read_restart(self, directory: str, nproc: int = 1, tag: int = 2, istep: int = -1):
+        """Load the reference's per-rank restart files (initial,
+        poiseuilleflow.f90:1873-1917) into the device state; continue with solve()."""
+        self._check(self.L.chf_read_restart(self.h, os.fsencode(directory), int(nproc), int(tag), int(istep)))
 
     def kernels_per_step(self) -> int:
         return int(self.L.chf_kernels_per_step(self.h))

@@ -148,6 +148,22 @@ int chf_profile_reset(chf_handle* h);
  * the last reset (synchronises the stream).  CHF_E_INVALID past the end. */
 int chf_profile_read(chf_handle* h, int idx, const char** name, int* launches, double* total_ms);
 
+/* Restart files in the reference's layout: one Fortran unformatted
+ * sequential file per MPI rank, as output (poiseuilleflow.f90:2460-2504)
+ * writes them and initial (poiseuilleflow.f90:1873-1917) reads them.
+ * Record 1 holds clamb1n, clamb1nm1, clamb3n, clamb3nm1, au0 and w0.
+ * Record 2 holds vnp1, omegaynp1, rhsvn, rhsomegayn, unp1 and wnp1 for the
+ * rank's streamwise slab of nnx / nproc slots; records are framed by 4-byte
+ * byte counts.  Files are <dir>/data<tag:8>_instant.<rank:3>.dat, or
+ * ..._instant.<rank:3>_<istep:8>.dat when istep >= 0 (the reference writes
+ * tag 2).  Write where the reference calls output: after chf_getnonlinear.
+ * After chf_read_restart the run continues with chf_solve, as the
+ * reference's first iteration does.  nproc must satisfy the reference's own
+ * constraints (nnx a multiple of 2 nproc, nny / 2 a multiple of nproc), and a
+ * rank's record must stay below 2 GiB; else CHF_E_INVALID.  Synchronous. */
+int chf_write_restart(chf_handle* h, const char* dir, int nproc, int tag, int istep);
+int chf_read_restart(chf_handle* h, const char* dir, int nproc, int tag, int istep);
+
 /* Allocation-free diagnostics.  No counterpart in the reference: an addition
  * for callers that cannot allocate device memory (their device memory is
  * owned by another runtime's pool, or fully committed to the resident state,
