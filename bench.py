@@ -44,6 +44,8 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--ensemble", type=int, default=96,
+                   help="channels of the batched-ensemble measurement (0: skip)")
     p.add_argument("--accuracy-steps", type=int, default=1000,
                    help="mixed path: steps of the accuracy comparison against the FP64 path (0: skip)")
     return p.parse_args()
@@ -392,6 +394,8 @@ def main():
     }
     if accuracy is not None:
         line["accuracy"] = accuracy
+    if args.ensemble > 0:
+        line["ensemble"] = ensemble_rate(args.ensemble, local, args.precision)
     if fp64_rate is not None:
         line["fp64_steps_per_s"] = fp64_rate
         line["mixed_over_fp64"] = value / world / fp64_rate
@@ -425,6 +429,68 @@ def fp64_peak_tflops(torch, device):
         torch.cuda.synchronize(device)
         best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
     return best
+
+
+def ensemble_configs(n, seed=5):
+    """n channels of the ensemble workload: nnz in {32, 64, 96} (33, 65, 97
+    wall-normal points), nnx = nny in {32, 64}, Re_tau uniform in [100, 300],
+    box 2 pi x 2 x pi, dt 2e-4 (seeded)."""
+    import numpy as np
+    from channel_flow_gb300 import config
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nz = (32, 64, 96)[i % 3]
+        nx = (32, 64)[(i // 3) % 2]
+        out.append(config.small(nnx=nx, nny=nx, nnz=nz, aphi=1.0, beta=0.5, dt=2e-4,
+                                re=float(rng.uniform(100.0, 300.0)), re_p=1.0))
+    return out
+
+
+def ensemble_rate(n, device, precision, steps=20, warmup=4):
+    """Channel-steps/s of n uneven channels advanced by one chf_batch (one
+    graph launch per pair of steps, channels side by side), and of the same
+    channels stepped one after another on one stream (chf_step each)."""
+    import torch
+    from channel_flow_gb300 import Batch, fields
+    cfgs = ensemble_configs(n)
+    t0 = time.perf_counter()
+    b = Batch(cfgs, precision=precision, device=device)
+    t_create = time.perf_counter() - t0
+    for i, (ch, c) in enumerate(zip(b, cfgs)):
+        ch.upload_state(fields.turbulent_start_state(c, seed=100 + i))
+        ch.getnonlinear()
+        ch.solve()
+    b.step(warmup)
+    b.synchronize()
+    t0 = time.perf_counter()
+    b.step(steps)
+    b.synchronize()
+    t_batch = time.perf_counter() - t0
+    # the same channels one after another on one stream
+    s = torch.cuda.Stream(device=device)
+    for ch in b:
+        ch.set_stream(s.cuda_stream)
+    for ch in b:
+        ch.step(2)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for ch in b:
+        ch.step(steps)
+    torch.cuda.synchronize(device)
+    t_seq = time.perf_counter() - t0
+    for ch in b:
+        ch.set_stream(None)
+    finite = all(ch.diagnostics()["finite"] for ch in b)
+    b.close()
+    points = sum(c.points for c in cfgs)
+    return {"channels": n, "precision": precision, "steps": steps,
+            "workload": "nnz in {32,64,96}, nnx = nny in {32,64}, Re_tau U[100,300], 2pi x 2 x pi, dt 2e-4",
+            "channel_steps_per_s": n * steps / t_batch,
+            "grid_point_steps_per_s": points * steps / t_batch,
+            "sequential_channel_steps_per_s": n * steps / t_seq,
+            "batch_over_sequential": t_seq / t_batch, "create_s": t_create, "finite": finite,
+            "timing": "host wall clock around chf_batch_step + synchronize"}
 
 
 def accuracy_vs_fp64(Channel, cfg, st, zpad, device, nsteps):

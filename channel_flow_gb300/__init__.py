@@ -11,11 +11,13 @@ layer over that ABI with the same call sequence as the reference's main loop:
     ch.step(n)                     # n x (getnonlinear + solve)
     state = ch.download_state()
 
+``Batch(cfgs)`` steps an ensemble of independent channels together, and
+``restart`` reads and writes the reference's per-rank restart files.
 There is no CPU fallback: if the library cannot be loaded, every call raises.
 """
 from .config import ChannelConfig, CONFIGS, small  # noqa: F401
-from .channel import Channel, ChannelError, load_library, PRECISION  # noqa: F401
-from . import fields  # noqa: F401
+from .channel import Batch, Channel, ChannelError, load_library, PRECISION  # noqa: F401
+from . import fields, restart  # noqa: F401
 
-__all__ = ["ChannelConfig", "CONFIGS", "small", "Channel", "ChannelError", "load_library",
-           "PRECISION", "fields"]
+__all__ = ["ChannelConfig", "CONFIGS", "small", "Batch", "Channel", "ChannelError", "load_library",
+           "PRECISION", "fields", "restart"]

@@ -23,7 +23,9 @@ EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
            "chf_download_state", "chf_getnonlinear", "chf_solve", "chf_step",
            "chf_synchronize", "chf_diagnostics", "chf_kernels_per_step", "chf_device_field",
            "chf_set_stream", "chf_profile_enable", "chf_profile_reset", "chf_profile_read",
-           "chf_diagnostics_static", "chf_write_restart", "chf_read_restart")
+           "chf_diagnostics_static", "chf_write_restart", "chf_read_restart",
+           "chf_batch_create", "chf_batch_destroy", "chf_batch_last_error", "chf_batch_size",
+           "chf_batch_handle", "chf_batch_step", "chf_batch_synchronize")
 
 
 class ChannelError(RuntimeError):
@@ -79,9 +81,17 @@ def load_library(path: str = None):
     L.chf_diagnostics_static.argtypes = [ctypes.c_int] * 3 + [vp] * 6 + [dp, ctypes.POINTER(CDiag), vp]
     for name in ("chf_write_restart", "chf_read_restart"):
         getattr(L, name).argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.chf_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(CConfig), ctypes.POINTER(vp)]
+    L.chf_batch_last_error.argtypes = [vp]
+    L.chf_batch_last_error.restype = ctypes.c_char_p
+    for name in ("chf_batch_destroy", "chf_batch_size", "chf_batch_synchronize"):
+        getattr(L, name).argtypes = [vp]
+    L.chf_batch_handle.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp)]
+    L.chf_batch_step.argtypes = [vp, ctypes.c_int]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     L.chf_last_error.restype = ctypes.c_char_p
+    L.chf_batch_last_error.restype = ctypes.c_char_p
     if path is None:
         _lib = L
     return L
@@ -221,3 +231,71 @@ class Channel:
             out[name.value.decode()] = (n.value, ms.value)
             i += 1
         return out
+
+
+class _Borrowed(Channel):
+    """A channel owned by a Batch: every Channel call, no destroy."""
+
+    def __init__(self, L, h, cfg):
+        self.L = L
+        self.cfg = cfg
+        self.shape = (cfg.nnz + 1, cfg.nny, cfg.nnx)
+        self.h = h
+
+    def close(self):
+        self.h = ctypes.c_void_p()
+
+
+class Batch:
+    """An ensemble of independent channels on one GPU (a chf_batch)."""
+
+    def __init__(self, cfgs, precision="fp64", zpad=0, device=0):
+        self.L = load_library()
+        cfgs = list(cfgs)
+        precs = precision if isinstance(precision, (list, tuple)) else [precision] * len(cfgs)
+        zpads = zpad if isinstance(zpad, (list, tuple)) else [zpad] * len(cfgs)
+        arr = (CConfig * len(cfgs))(*[make_cconfig(c, p, z, device) for c, p, z in zip(cfgs, precs, zpads)])
+        self.b = ctypes.c_void_p()
+        rc = self.L.chf_batch_create(len(cfgs), arr, ctypes.byref(self.b))
+        if rc != 0:
+            raise ChannelError(rc, self.L.chf_batch_last_error(None).decode())
+        self.channels = []
+        for i, c in enumerate(cfgs):
+            h = ctypes.c_void_p()
+            self._check(self.L.chf_batch_handle(self.b, i, ctypes.byref(h)))
+            self.channels.append(_Borrowed(self.L, h, c))
+
+    def _check(self, rc):
+        if rc != 0:
+            raise ChannelError(rc, self.L.chf_batch_last_error(self.b).decode())
+
+    def __len__(self):
+        return len(self.channels)
+
+    def __getitem__(self, i) -> Channel:
+        return self.channels[i]
+
+    def step(self, n=1):
+        self._check(self.L.chf_batch_step(self.b, int(n)))
+
+    def synchronize(self):
+        self._check(self.L.chf_batch_synchronize(self.b))
+
+    def close(self):
+        if getattr(self, "b", None) and self.b.value:
+            for c in self.channels:
+                c.close()
+            self.L.chf_batch_destroy(self.b)
+            self.b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -137,10 +137,12 @@ static void release(chf_handle* h) {
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
 }
 
-static int step_once(chf_handle* h) {
+namespace chf {
+int step_once(Handle* h) {
   int rc = h->cfg.precision == CHF_MIXED ? launch_nonlinear_mixed(h) : launch_nonlinear_fp64(h);
   return rc == CHF_OK ? launch_solve_fp64(h) : rc;
 }
+}  // namespace chf
 
 // The graph of a pair of steps for the current history arrangement, captured
 // on first use; *out = nullptr when steps must be launched directly: with

@@ -173,6 +173,8 @@ int launch_tc_split_fx(Handle* h, const FxPlan& p, const Ptr8<const InT>& ins, i
                        int* bexp, int nfields, int kid);
 int setup_mixed(Handle* h);
 int launch_nonlinear_mixed(Handle* h);
+// one time step (getnonlinear + solve) on h->stream (chf_api.cu)
+int step_once(Handle* h);
 // launchers (k_solve.cu)
 int setup_solver(Handle* h);
 int launch_solve_fp64(Handle* h);

@@ -164,6 +164,26 @@ int chf_profile_read(chf_handle* h, int idx, const char** name, int* launches, d
 int chf_write_restart(chf_handle* h, const char* dir, int nproc, int tag, int istep);
 int chf_read_restart(chf_handle* h, const char* dir, int nproc, int tag, int istep);
 
+/* Ensembles.  No counterpart in the reference (one channel per MPI job): a
+ * batch holds n independent channels of any sizes, Reynolds numbers and
+ * precisions on one device (all cfgs[i].device equal) and advances them
+ * together.  Pairs of steps replay one CUDA graph that forks into one branch
+ * per channel, so small channels run side by side instead of one launch
+ * after another.  chf_batch_handle lends channel i's handle for
+ * upload/download/diagnostics/restart calls (do not destroy it; it lives
+ * until chf_batch_destroy); each channel's results are bit-identical to
+ * stepping it alone.  chf_batch_step is asynchronous and orders itself after
+ * work already queued on the channels and before work queued later. */
+typedef struct chf_batch chf_batch;
+int chf_batch_create(int n, const chf_config* cfgs, chf_batch** out);
+int chf_batch_destroy(chf_batch* b);
+/* Last error of b, or of the last failed chf_batch_create when b is NULL. */
+const char* chf_batch_last_error(const chf_batch* b);
+int chf_batch_size(const chf_batch* b);
+int chf_batch_handle(chf_batch* b, int i, chf_handle** h);
+int chf_batch_step(chf_batch* b, int nsteps);
+int chf_batch_synchronize(chf_batch* b);
+
 /* Allocation-free diagnostics.  No counterpart in the reference: an addition
  * for callers that cannot allocate device memory (their device memory is
  * owned by another runtime's pool, or fully committed to the resident state,

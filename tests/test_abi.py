@@ -81,3 +81,22 @@ def test_static_diagnostics_rejects_oversized_grid(chflow_lib):
     rc = chflow_lib.chf_diagnostics_static(16, 8, 1025, one, one, one, one, one, one, None,
                                            ctypes.byref(d), None)
     assert rc == -1
+
+
+def test_batch_rejects_mixed_devices_and_bad_channels(chflow_lib):
+    base = make_cconfig(config.CONFIGS["c1_poiseuille_32"])
+    other = make_cconfig(config.CONFIGS["c1_poiseuille_32"], device=1)
+    arr = (CConfig * 2)(base, other)
+    b = ctypes.c_void_p()
+    assert chflow_lib.chf_batch_create(2, arr, ctypes.byref(b)) == -1
+    assert "one device" in chflow_lib.chf_batch_last_error(None).decode()
+    bad = make_cconfig(config.CONFIGS["c1_poiseuille_32"])
+    bad.nnz = 33
+    arr = (CConfig * 2)(base, bad)
+    rc = chflow_lib.chf_batch_create(2, arr, ctypes.byref(b))
+    assert rc != 0 and not b.value
+    assert chflow_lib.chf_batch_create(0, arr, ctypes.byref(b)) == -1
+    assert chflow_lib.chf_batch_step(None, 1) == -1
+    assert chflow_lib.chf_batch_destroy(None) == -1
+    assert chflow_lib.chf_write_restart(None, b".", 1, 2, -1) == -1
+    assert chflow_lib.chf_read_restart(None, b".", 1, 2, -1) == -1
