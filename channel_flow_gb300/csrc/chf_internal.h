@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../../include/chflow.h"
+#include "df32.cuh"
 #include "fft_dev.cuh"
 
 namespace chf {
@@ -81,6 +82,7 @@ struct Handle {
   int nk2 = 0;
   double* k2vals = nullptr;   // nk2
   double* xinv = nullptr;     // nk2 * sl.stride
+  float2* xinv2 = nullptr;    // (hi, lo) float pairs (mixed path's increment solve)
   double* xmean = nullptr;    // inverse of the (0,0) operator, NZ x NZ column-major
   int* group_start = nullptr; // nk2 + 1 (modes grouped by k^2)
   int* group_modes = nullptr; // solved modes, sorted by k^2 index
@@ -90,6 +92,7 @@ struct Handle {
   FftPlan py, px, pz2, pzm;   // PY, PX, 2N, 2MZ
   cd *tw_py = nullptr, *tw_px = nullptr, *tw_z2 = nullptr, *tw_zm = nullptr;
   cf *twf_py = nullptr, *twf_px = nullptr;
+  cplx<df32>* twd_z2 = nullptr;  // double-float twiddles of the 2N-point DFT
 
   // work buffers
   cd* wz = nullptr;   // 6 x [MP][KY][KX]  (values on the product grid)
@@ -177,6 +180,7 @@ int launch_nonlinear_mixed(Handle* h);
 int step_once(Handle* h);
 // launchers (k_solve.cu)
 int setup_solver(Handle* h);
+int setup_solver_mixed(Handle* h);
 int launch_solve_fp64(Handle* h);
 int launch_diagnostics(Handle* h, chf_diag* out);
 
