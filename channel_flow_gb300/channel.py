@@ -25,7 +25,8 @@ EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
            "chf_set_stream", "chf_profile_enable", "chf_profile_reset", "chf_profile_read",
            "chf_diagnostics_static", "chf_write_restart", "chf_read_restart",
            "chf_batch_create", "chf_batch_destroy", "chf_batch_last_error", "chf_batch_size",
-           "chf_batch_handle", "chf_batch_step", "chf_batch_synchronize")
+           "chf_batch_handle", "chf_batch_step", "chf_batch_synchronize",
+           "chf_set_flow_rate", "chf_get_flow_rate", "chf_statistics")
 
 
 class ChannelError(RuntimeError):
@@ -39,6 +40,11 @@ class CConfig(ctypes.Structure):
                 ("aphi", ctypes.c_double), ("beta", ctypes.c_double), ("dt", ctypes.c_double),
                 ("re", ctypes.c_double), ("re_p", ctypes.c_double), ("precision", ctypes.c_int),
                 ("zpad", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class CStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("u_tau_top", "u_tau_bottom", "re_tau_top", "re_tau_bottom",
+                                               "re_centre", "re_bulk", "bulk_velocity", "energy")]
 
 
 class CDiag(ctypes.Structure):
@@ -88,6 +94,9 @@ def load_library(path: str = None):
         getattr(L, name).argtypes = [vp]
     L.chf_batch_handle.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp)]
     L.chf_batch_step.argtypes = [vp, ctypes.c_int]
+    L.chf_set_flow_rate.argtypes = [vp, ctypes.c_double]
+    L.chf_get_flow_rate.argtypes = [vp, dp, dp, dp]
+    L.chf_statistics.argtypes = [vp, dp, ctypes.POINTER(CStats)]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     L.chf_last_error.restype = ctypes.c_char_p
@@ -202,6 +211,27 @@ class Channel:
         """Load the reference's per-rank restart files (initial,
         poiseuilleflow.f90:1873-1917) into the device state; continue with solve()."""
         self._check(self.L.chf_read_restart(self.h, os.fsencode(directory), int(nproc), int(tag), int(istep)))
+
+    def statistics(self) -> dict:
+        """Plane statistics at the Gauss-Lobatto points and the scalar
+        diagnostics of the reference's statistics routine."""
+        prof = np.zeros((10, self.cfg.nnz + 1))
+        st = CStats()
+        self._check(self.L.chf_statistics(self.h, _dptr(prof), ctypes.byref(st)))
+        out = {n: getattr(st, n) for n, _ in CStats._fields_}
+        for i, n in enumerate(("z", "u", "v", "w", "uu", "vv", "ww", "uv", "uw", "vw")):
+            out[n] = prof[i]
+        return out
+
+    def set_flow_rate(self, bulk_velocity: float):
+        """Hold the bulk velocity at bulk_velocity (> 0) by adjusting the mean
+        pressure gradient every step; 0 switches the control off."""
+        self._check(self.L.chf_set_flow_rate(self.h, float(bulk_velocity)))
+
+    def flow_rate(self) -> dict:
+        t, u, p = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.L.chf_get_flow_rate(self.h, ctypes.byref(t), ctypes.byref(u), ctypes.byref(p)))
+        return {"target": t.value, "bulk_velocity": u.value, "dpdx_correction": p.value}
 
     def kernels_per_step(self) -> int:
         return int(self.L.chf_kernels_per_step(self.h))

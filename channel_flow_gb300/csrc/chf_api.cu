@@ -125,7 +125,7 @@ static void release(chf_handle* h) {
   for (auto& p : h->mean) cudaFree(p);
   void* ptrs[] = {h->iapha, h->ibeta, h->t0, h->t2, h->t4, h->k2vals, h->xinv, h->xmean,
                   h->group_start, h->group_modes, h->tw_py, h->tw_px, h->tw_z2, h->tw_zm,
-                  h->twf_py, h->twf_px, h->twd_z2, h->xinv2, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
+                  h->twf_py, h->twf_px, h->twd_z2, h->xinv2, h->phi, h->flow, h->stats_buf, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
                   h->agl, h->bimg, h->wz32, h->wy32, h->lc64, h->aexp1, h->aexp2, h->aexp3, h->bexp};
   for (void* p : ptrs) cudaFree(p);
   for (auto& p : h->pending) {
@@ -425,6 +425,33 @@ int chf_diagnostics(chf_handle* h, chf_diag* out) {
 }
 
 int chf_kernels_per_step(const chf_handle* h) { return h ? h->kernels_per_step : 0; }
+
+int chf_set_flow_rate(chf_handle* h, double bulk_velocity) {
+  if (!h) return CHF_E_INVALID;
+  if (!(bulk_velocity >= 0.0) || !std::isfinite(bulk_velocity)) {
+    h->err = "bulk velocity must be finite and >= 0 (0 switches the control off)";
+    return CHF_E_INVALID;
+  }
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice") ||
+      !cuda_ok(h, cudaMemcpyAsync(h->flow, &bulk_velocity, sizeof(double), cudaMemcpyHostToDevice, h->stream),
+               "flow rate") ||
+      !cuda_ok(h, cudaStreamSynchronize(h->stream), "flow rate"))
+    return CHF_E_CUDA;
+  return CHF_OK;
+}
+
+int chf_get_flow_rate(chf_handle* h, double* target, double* bulk_velocity, double* dpdx_correction) {
+  if (!h) return CHF_E_INVALID;
+  double w[4];
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice") ||
+      !cuda_ok(h, cudaMemcpyAsync(w, h->flow, sizeof(w), cudaMemcpyDeviceToHost, h->stream), "flow rate") ||
+      !cuda_ok(h, cudaStreamSynchronize(h->stream), "flow rate"))
+    return CHF_E_CUDA;
+  if (target) *target = w[0];
+  if (bulk_velocity) *bulk_velocity = w[3];
+  if (dpdx_correction) *dpdx_correction = w[1];
+  return CHF_OK;
+}
 
 int chf_set_stream(chf_handle* h, void* stream) {
   if (!h) return CHF_E_INVALID;

@@ -87,6 +87,11 @@ struct Handle {
   int* group_start = nullptr; // nk2 + 1 (modes grouped by k^2)
   int* group_modes = nullptr; // solved modes, sorted by k^2 index
   int nsolve = 0;
+  // constant flow rate (chf_set_flow_rate): influence function, its bulk
+  // velocity, device word {target, correction, bulk before, bulk after}
+  double* phi = nullptr;
+  double ubphi = 0.0;
+  double* flow = nullptr;
 
   // FFT plans and twiddles
   FftPlan py, px, pz2, pzm;   // PY, PX, 2N, 2MZ
@@ -98,6 +103,7 @@ struct Handle {
   cd* wz = nullptr;   // 6 x [MP][KY][KX]  (values on the product grid)
   cd* wy = nullptr;   // 6 x [MP][PY][KX]  (after the spanwise transform)
   void* scratch = nullptr;  // reduction scratch (diagnostics)
+  void* stats_buf = nullptr;  // chf_statistics: GL values of u, v, w + plane sums (first call)
   size_t scratch_bytes = 0;
 
   // mixed-precision path (k_mixed.cu): FP32 transforms, tcgen05 GEMMs

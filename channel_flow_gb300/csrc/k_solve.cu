@@ -191,6 +191,12 @@ struct SolveArgs {
   // the 2N-point DFT
   const float2* xinv2;
   const cplx<df32>* tw2d;
+  // constant flow rate: influence function phi of a unit mean pressure
+  // gradient over one step, its bulk velocity, and the device word
+  // flow = {target bulk velocity (0: off), last correction, bulk before, bulk after}
+  const double* phi;
+  double ubphi;
+  double* flow;
 };
 
 // rhs of the increment solve: (hi, lo) floats of the real and imaginary parts
@@ -536,6 +542,26 @@ __global__ void __launch_bounds__(S_THREADS, MIX ? 2 : 3) k_solve(const __grid_c
     __syncthreads();
     // ---- F: store, then getvelocityandvorticity (REF:2347-2407)
     if (mean) {
+      // constant flow rate (no counterpart in the reference, which holds the
+      // pressure gradient re_p fixed): add the multiple of phi that restores
+      // the target bulk velocity U_b = sum_{n even} Re(au0_n) / (1 - n^2);
+      // the multiple is this step's extra mean pressure gradient
+      const double target = a.flow[0];
+      if (target > 0.0 && warp == 0) {
+        const int lane = tid & 31;
+        double ub = 0.0;
+        for (int n = lane; n < NZ; n += 32)
+          if (!(n & 1)) ub += s.co[n].re / (1.0 - (double)n * (double)n);
+        for (int off = 16; off > 0; off >>= 1) ub += __shfl_xor_sync(0xffffffffu, ub, off);
+        const double alpha = (target - ub) / a.ubphi;
+        for (int n = lane; n < NZ; n += 32) s.co[n].re += alpha * a.phi[n];
+        if (lane == 0) {
+          a.flow[1] = alpha;
+          a.flow[2] = ub;
+          a.flow[3] = ub + alpha * a.ubphi;
+        }
+      }
+      __syncthreads();
       for (int t = tid; t < nm * NZ; t += blockDim.x) {
         int m = t / NZ, n = t % NZ;
         cd x = s.co[t];
@@ -727,6 +753,54 @@ int setup_solver(Handle* h) {
       !up((void**)&h->group_modes, gmodes.data(),
           sizeof(int) * std::max<size_t>(1, gmodes.size()), "group_modes"))
     return CHF_E_CUDA;
+  // constant-flow-rate influence function: the mean-mode operator of
+  // get_coef_u0 (REF:3493-3511) applied to phi equals a unit mean pressure
+  // gradient over one step (dt on the collocation rows, as re_p enters the
+  // right-hand side of REF:401-412), with phi = 0 at both walls
+  {
+    const int Z = NZ;
+    const double dt = h->cfg.dt, re = h->cfg.re;
+    std::vector<double> A((size_t)Z * Z), phi(Z, 0.0);
+    for (int j = 0; j < Z; ++j) {
+      A[j] = 1.0;
+      A[(size_t)Z + j] = (j % 2 == 0) ? 1.0 : -1.0;
+    }
+    for (int i = 2; i < Z; ++i) {
+      for (int j = 0; j < Z; ++j)
+        A[(size_t)i * Z + j] = t0[(size_t)(i - 1) + (size_t)Z * j] - dt * 0.5 / re * t2[(size_t)(i - 1) + (size_t)Z * j];
+      phi[i] = dt;
+    }
+    // Gaussian elimination with partial pivoting
+    for (int k = 0; k < Z; ++k) {
+      int p = k;
+      for (int i = k + 1; i < Z; ++i)
+        if (std::fabs(A[(size_t)i * Z + k]) > std::fabs(A[(size_t)p * Z + k])) p = i;
+      if (A[(size_t)p * Z + k] == 0.0) {
+        h->err = "mean-mode operator is singular";
+        return CHF_E_NUMERIC;
+      }
+      if (p != k) {
+        for (int j = 0; j < Z; ++j) std::swap(A[(size_t)k * Z + j], A[(size_t)p * Z + j]);
+        std::swap(phi[k], phi[p]);
+      }
+      for (int i = k + 1; i < Z; ++i) {
+        const double f = A[(size_t)i * Z + k] / A[(size_t)k * Z + k];
+        for (int j = k; j < Z; ++j) A[(size_t)i * Z + j] -= f * A[(size_t)k * Z + j];
+        phi[i] -= f * phi[k];
+      }
+    }
+    for (int k = Z - 1; k >= 0; --k) {
+      double acc = phi[k];
+      for (int j = k + 1; j < Z; ++j) acc -= A[(size_t)k * Z + j] * phi[j];
+      phi[k] = acc / A[(size_t)k * Z + k];
+    }
+    h->ubphi = 0.0;
+    for (int n = 0; n < Z; n += 2) h->ubphi += phi[n] / (1.0 - (double)n * (double)n);
+    const double zero4[4] = {0.0, 0.0, 0.0, 0.0};
+    if (!up((void**)&h->phi, phi.data(), sizeof(double) * Z, "phi") ||
+        !up((void**)&h->flow, zero4, sizeof(zero4), "flow"))
+      return CHF_E_CUDA;
+  }
   size_t xbytes = sizeof(double) * sl.stride * (size_t)(h->nk2 + 1);
   if (!cuda_ok(h, cudaMalloc((void**)&h->xinv, xbytes), "xinv")) return CHF_E_NOMEM;
   int* dstatus = nullptr;
@@ -815,6 +889,9 @@ int launch_solve_fp64(Handle* h) {
   a.tw2 = h->tw_z2;
   a.xinv2 = h->xinv2;
   a.tw2d = h->twd_z2;
+  a.phi = h->phi;
+  a.ubphi = h->ubphi;
+  a.flow = h->flow;
   a.nk2 = h->nk2;
   const int mb2 = fft_fits(2 * CH, 2 * d.N, S_THREADS, 2) ? 2 : 4;
   if (d.N + 1 > 32 * WD_EMAX || !fft_fits(2 * CH, 2 * d.N, S_THREADS, mb2)) {

@@ -171,6 +171,15 @@ def reference_like_state(cfg: ChannelConfig, seed: int = 0, epsilon: float = 1.0
     return st
 
 
+def bulk_velocity(st: dict) -> float:
+    """U_b = (1/2) int_{-1}^{1} u dz of the mean profile au0 (Chebyshev
+    coefficients): sum over even n of au0_n / (1 - n^2)."""
+    a = st["au0"][:, 0]
+    n = np.arange(a.size)
+    even = n % 2 == 0
+    return float(np.sum(a[even] / (1.0 - n[even] ** 2.0)))
+
+
 def laminar_state(cfg: ChannelConfig, gamma: float = None) -> dict:
     """Plane Poiseuille flow U = gamma (1 - z^2) alone in the (0,0) mode, with
     omega_z = -dU/dz = 2 gamma z.  With gamma = re*re_p/2 and steady mean

@@ -148,6 +148,37 @@ int chf_profile_reset(chf_handle* h);
  * the last reset (synchronises the stream).  CHF_E_INVALID past the end. */
 int chf_profile_read(chf_handle* h, int idx, const char** name, int* launches, double* total_ms);
 
+/* Flow statistics of the current state, as statistics
+ * (poiseuilleflow.f90:2666-3198) forms them from the physical
+ * nnx x nny x (nz+1) grid, computed here from spectral sums (Parseval) with
+ * no in-plane transform.  profiles (NULL or 10 x (nz+1) doubles, row-major):
+ * z_k = cos(pi k / nz), <u>, <v>, <w>, <u'u'>, <v'v'>, <w'w'>, <u'v'>, <u'w'>,
+ * <v'w'> at the Gauss-Lobatto points (u streamwise, v wall-normal, w
+ * spanwise).  The first call allocates a scratch of 3 (nz+1) nnx nny / 2
+ * complex doubles kept until chf_destroy.  Synchronous. */
+typedef struct chf_stats {
+  double u_tau_top, u_tau_bottom;   /* sqrt(|d<u>/dz| / re) at z = +1 and z = -1 */
+  double re_tau_top, re_tau_bottom; /* u_tau * re (the "R_t" print) */
+  double re_centre;                 /* <u>(z = 0) * re ("R_c") */
+  double re_bulk;                   /* 2 U_b re with the reference's half-channel rectangle rule ("R_b") */
+  double bulk_velocity;             /* (1/2) int <u> dz, exact from the Chebyshev coefficients of au0 */
+  double energy;                    /* 0.5 sum of u^2 + v^2 + w^2 over the physical grid (energy.plt) */
+} chf_stats;
+int chf_statistics(chf_handle* h, double* profiles, chf_stats* out);
+
+/* Constant flow rate.  No counterpart in the reference, which drives the
+ * flow with the fixed mean pressure gradient re_p (paraandcons.f90:25);
+ * required by the 32^3 Poiseuille workload.  With a target bulk velocity
+ * U_b > 0 (U_b = (1/2) int u dz over the (0,0) mode), every solve adds to
+ * the new mean profile au0 the multiple of the response to a unit mean
+ * pressure gradient (same operator and walls as poiseuilleflow.f90:401-474)
+ * that restores U_b; that multiple is the step's extra pressure gradient.
+ * 0 switches the control off (the default). */
+int chf_set_flow_rate(chf_handle* h, double bulk_velocity);
+/* The target, the bulk velocity after the last solve and the last extra mean
+ * pressure gradient (all 0 while the control is off; synchronous). */
+int chf_get_flow_rate(chf_handle* h, double* target, double* bulk_velocity, double* dpdx_correction);
+
 /* Restart files in the reference's layout: one Fortran unformatted
  * sequential file per MPI rank, as output (poiseuilleflow.f90:2460-2504)
  * writes them and initial (poiseuilleflow.f90:1873-1917) reads them.
