@@ -498,7 +498,7 @@ def accuracy_vs_fp64(Channel, cfg, st, zpad, device, nsteps):
     getnonlinear + solve): rel-L2 of each field of the mixed state against
     the FP64 state, and of the velocity vector (u, v, w) as a whole."""
     import numpy as np
-    out = {}
+    out, extra = {}, {}
     for prec in ("fp64", "mixed"):
         ch = Channel(cfg, precision=prec, zpad=zpad, device=device)
         ch.upload_state(st)
@@ -507,6 +507,7 @@ def accuracy_vs_fp64(Channel, cfg, st, zpad, device, nsteps):
         ch.step(nsteps)
         ch.synchronize()
         out[prec] = ch.download_state()
+        extra[prec] = (ch.pressure(), ch.statistics())
         ch.close()
     a, b = out["fp64"], out["mixed"]
     nyq = cfg.nny // 2
@@ -519,10 +520,20 @@ def accuracy_vs_fp64(Channel, cfg, st, zpad, device, nsteps):
         if k != "omegaynp1":
             num, den = num + d2, den + r2
     vel = (num / den) ** 0.5
+    pa = np.delete(extra["fp64"][0], nyq, axis=1)
+    pb = np.delete(extra["mixed"][0], nyq, axis=1)
+    errs["pressure"] = float(np.linalg.norm(pb - pa) / np.linalg.norm(pa))
+    sa, sb = extra["fp64"][1], extra["mixed"][1]
+    rel = lambda k: abs(sb[k] - sa[k]) / abs(sa[k])
+    errs["wall_shear_top"] = rel("u_tau_top") * 2.0     # tau_w = u_tau^2
+    errs["wall_shear_bottom"] = rel("u_tau_bottom") * 2.0
+    errs["energy"] = rel("energy")
     return {"steps": nsteps, "rel_l2_vs_fp64": errs, "velocity_rel_l2": vel,
             "velocity_component_max_rel_l2": max(errs[k] for k in ("unp1", "vnp1", "wnp1")),
             "target": 1e-5, "met": vel <= 1e-5,
-            "note": "spectral coefficients without the spanwise Nyquist slot; velocity = (u, v, w) as one vector"}
+            "note": "spectral coefficients without the spanwise Nyquist slot; velocity = (u, v, w) as one "
+                    "vector; pressure = total head (chf_pressure); wall shear and energy from chf_statistics "
+                    "(relative differences)"}
 
 
 def read_traffic(kname):

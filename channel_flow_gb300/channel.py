@@ -26,7 +26,7 @@ EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
            "chf_diagnostics_static", "chf_write_restart", "chf_read_restart",
            "chf_batch_create", "chf_batch_destroy", "chf_batch_last_error", "chf_batch_size",
            "chf_batch_handle", "chf_batch_step", "chf_batch_synchronize",
-           "chf_set_flow_rate", "chf_get_flow_rate", "chf_statistics")
+           "chf_set_flow_rate", "chf_get_flow_rate", "chf_statistics", "chf_pressure")
 
 
 class ChannelError(RuntimeError):
@@ -97,6 +97,7 @@ def load_library(path: str = None):
     L.chf_set_flow_rate.argtypes = [vp, ctypes.c_double]
     L.chf_get_flow_rate.argtypes = [vp, dp, dp, dp]
     L.chf_statistics.argtypes = [vp, dp, ctypes.POINTER(CStats)]
+    L.chf_pressure.argtypes = [vp, dp]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     L.chf_last_error.restype = ctypes.c_char_p
@@ -221,6 +222,13 @@ class Channel:
         out = {n: getattr(st, n) for n, _ in CStats._fields_}
         for i, n in enumerate(("z", "u", "v", "w", "uu", "vv", "ww", "uv", "uw", "vw")):
             out[n] = prof[i]
+        return out
+
+    def pressure(self) -> np.ndarray:
+        """Total-head pressure P = p + |u|^2/2 of the current state (after a
+        solve), Chebyshev coefficients in the field layout."""
+        out = np.zeros(self.shape)
+        self._check(self.L.chf_pressure(self.h, _dptr(out)))
         return out
 
     def set_flow_rate(self, bulk_velocity: float):

@@ -104,6 +104,7 @@ struct Handle {
   cd* wy = nullptr;   // 6 x [MP][PY][KX]  (after the spanwise transform)
   void* scratch = nullptr;  // reduction scratch (diagnostics)
   void* stats_buf = nullptr;  // chf_statistics: GL values of u, v, w + plane sums (first call)
+  void* pres_buf = nullptr;   // chf_pressure: Lamb coefficients, right-hand sides, P (first call)
   size_t scratch_bytes = 0;
 
   // mixed-precision path (k_mixed.cu): FP32 transforms, tcgen05 GEMMs
@@ -164,6 +165,7 @@ bool cuda_ok(Handle* h, cudaError_t e, const char* what);
 
 // launchers (k_nonlinear.cu)
 int launch_nonlinear_fp64(Handle* h);
+int launch_lamb_fp64(Handle* h, cd* hc);
 template <typename T>
 int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const cplx<T>* tw_px);
 // launchers (k_tcgemm.cu, k_mixed.cu)

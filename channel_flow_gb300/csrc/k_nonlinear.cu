@@ -362,6 +362,45 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zcurl(
 
 
 // ---------------------------------------------------------------------------
+// z forward only: the Lamb vector H1, H2, H3 on the product grid ->
+// Chebyshev coefficients 0..N (the first part of k_zcurl), for the pressure.
+// ZL modes per CTA, grid (ceil(modes / ZL), 3); out: 3 x [NZ][modes].
+// ---------------------------------------------------------------------------
+template <int MB2, int ZL>
+__global__ void __launch_bounds__(ZC_THREADS) k_zfwd(const cd* __restrict__ wz, cd* __restrict__ out, Dims d,
+                                                     const __grid_constant__ FftPlan pzm,
+                                                     const cd* __restrict__ twm) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int L = 2 * d.MZ, ls = L;
+  const int NZ = d.NZ;
+  cd* s = reinterpret_cast<cd*>(smem_raw);
+  const long modes = d.modes();
+  const long m0 = (long)blockIdx.x * ZL;
+  const int f = blockIdx.y;
+  const double inv_mz = 1.0 / (double)d.MZ;
+  const cd* __restrict__ src = wz + (size_t)f * d.MP * modes;
+  for (int t = threadIdx.x; t < ZL * d.MP; t += blockDim.x) {
+    int l = t % ZL, p = t / ZL;
+    long m = m0 + l;
+    cd v{0.0, 0.0};
+    if (m < modes) v = src[(size_t)p * modes + m];
+    s[l * ls + p] = v;
+    if (p > 0 && p < d.MZ) s[l * ls + L - p] = v;
+  }
+  __syncthreads();
+  smem_fft<double, -1, MB2>(s, ZL, ls, pzm, twm);
+  cd* __restrict__ dst = out + (size_t)f * NZ * modes;
+  for (int t = threadIdx.x; t < ZL * NZ; t += blockDim.x) {
+    int l = t % ZL, n = t / ZL;
+    long m = m0 + l;
+    if (m >= modes) continue;
+    cd v = s[l * ls + n];
+    double sc = (n == 0) ? 0.5 * inv_mz : inv_mz;
+    dst[(size_t)n * modes + m] = cd{v.re * sc, v.im * sc};
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Length-192 specialisations (3/2-padded 128-point directions), one warp per
 // line with the register FFT of fft_warp.cuh.  Rows written by k_yinv_w and
 // read by k_xprod_w / k_yfwd_w are in the permuted order 32 k1 + lane of that
@@ -703,6 +742,28 @@ int launch_nonlinear_fp64(Handle* h) {
   std::swap(h->f[F_U], h->f[F_RV]);
   std::swap(h->f[F_W], h->f[F_RG]);
   return CHF_OK;
+}
+
+// The Lamb vector of the current state (velocities and vorticities, as
+// after a solve) as Chebyshev coefficients hc = 3 x [NZ][modes], FP64; the
+// work buffers wz / wy must exist.  For the pressure (chf_pressure).
+int launch_lamb_fp64(Handle* h, cd* hc) {
+  const Dims& d = h->d;
+  const int zl = pick_zl_c2v(d);
+  if (!zl) {
+    h->err = "z transforms: FFT length too large for the launch shapes";
+    return CHF_E_INVALID;
+  }
+  int rc = zl == 8 ? run_zc2v<8>(h) : zl == 4 ? run_zc2v<4>(h) : run_zc2v<2>(h);
+  if (rc != CHF_OK) return rc;
+  rc = launch_xy<double>(h, h->wz, h->wy, h->tw_py, h->tw_px);
+  if (rc != CHF_OK) return rc;
+  const size_t smem = zc2v_smem(d, zl);
+  auto kern = zl == 8 ? k_zfwd<4, 8> : zl == 4 ? k_zfwd<4, 4> : k_zfwd<4, 2>;
+  if (!set_smem(h, kern, smem)) return CHF_E_CUDA;
+  dim3 grid((unsigned)((d.modes() + zl - 1) / zl), 3);
+  kern<<<grid, ZC_THREADS, smem, h->stream>>>(h->wz, hc, d, h->pzm, h->tw_zm);
+  return cuda_ok(h, cudaGetLastError(), "k_zfwd") ? CHF_OK : CHF_E_CUDA;
 }
 
 }  // namespace chf

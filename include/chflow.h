@@ -166,6 +166,19 @@ typedef struct chf_stats {
 } chf_stats;
 int chf_statistics(chf_handle* h, double* profiles, chf_stats* out);
 
+/* Pressure of the current state (after a solve: velocities and vorticities
+ * in the module arrays), as Chebyshev coefficients in the field layout
+ * (p_out: (0:nx,0:ny,0:nz) real*8, host).  The reference's pressure routine
+ * (instantp, poiseuilleflow.f90:3701-3890) is never called; this is a
+ * spectral replacement consistent with the time step: P is the total head
+ * p + |u|^2 / 2 of the rotational form u_t = -H - grad P + lap u / re, from
+ * (D^2 - k^2) P = -(i alpha H1 + D H2 + i beta H3) with the Neumann walls
+ * D P = -H2 + (D^2 - k^2) v / re, collocated at the Gauss-Lobatto points;
+ * the (0,0) mode has zero mean over z and excludes the driving gradient
+ * re_p.  FP64 for either precision; the first call allocates its work
+ * buffers (kept until chf_destroy).  Synchronous. */
+int chf_pressure(chf_handle* h, double* p_out);
+
 /* Constant flow rate.  No counterpart in the reference, which drives the
  * flow with the fixed mean pressure gradient re_p (paraandcons.f90:25);
  * required by the 32^3 Poiseuille workload.  With a target bulk velocity
