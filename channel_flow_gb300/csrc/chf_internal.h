@@ -60,6 +60,21 @@ struct SolveLayout {
   size_t stride;   // doubles per k^2 entry: ne_v^2 + no_v^2 + ne_w^2 + no_w^2
 };
 
+// Offsets of the four blocks (v even, v odd, omega even, omega odd) inside
+// one k^2 entry of the inverses; each block column-major, X[c * n + r].
+struct BlockOffsets {
+  size_t ve, vo, we, wo;
+};
+
+__host__ __device__ inline BlockOffsets block_offsets(const SolveLayout& s) {
+  BlockOffsets b;
+  b.ve = 0;
+  b.vo = b.ve + (size_t)s.ne_v * s.ne_v;
+  b.we = b.vo + (size_t)s.no_v * s.no_v;
+  b.wo = b.we + (size_t)s.ne_w * s.ne_w;
+  return b;
+}
+
 struct Handle {
   chf_config cfg;
   Dims d;
@@ -105,6 +120,7 @@ struct Handle {
   void* scratch = nullptr;  // reduction scratch (diagnostics)
   void* stats_buf = nullptr;  // chf_statistics: GL values of u, v, w + plane sums (first call)
   void* pres_buf = nullptr;   // chf_pressure: Lamb coefficients, right-hand sides, P (first call)
+  void* inc_buf = nullptr;    // mixed solve: explicit increments and folded right-hand sides
   size_t scratch_bytes = 0;
 
   // mixed-precision path (k_mixed.cu): FP32 transforms, tcgen05 GEMMs
@@ -153,7 +169,8 @@ struct Handle {
 // Kernel ids for profiling.
 enum KernelId {
   K_ZC2V = 0, K_YINV, K_XPROD, K_YFWD, K_ZCURL, K_SOLVE, K_DIAG,
-  K_SPLIT_Z1, K_GEMM_Z1, K_SPLIT_Z2, K_GEMM_Z2, K_CURL32, K_GEMM_GL, K_MEANFIX, K_COUNT
+  K_SPLIT_Z1, K_GEMM_Z1, K_SPLIT_Z2, K_GEMM_Z2, K_CURL32, K_GEMM_GL, K_MEANFIX,
+  K_INC_EXPL, K_INC_FOLD, K_INC_MATVEC, K_INC_RECOVER, K_SOLVE_MEAN, K_COUNT
 };
 extern const char* const kKernelNames[K_COUNT];
 
@@ -190,6 +207,8 @@ int step_once(Handle* h);
 int setup_solver(Handle* h);
 int setup_solver_mixed(Handle* h);
 int launch_solve_fp64(Handle* h);
+int launch_solve_mean(Handle* h);   // the (0,0) mode alone
+int launch_solve_mixed(Handle* h);  // k_solve_mixed.cu
 int launch_diagnostics(Handle* h, chf_diag* out);
 
 // FFT plan helper (host)

@@ -11,7 +11,7 @@
 //   k_tc_split_z2   the three Lamb components [MP][2 modes] -> digit images
 //   k_tc_gemm_z2    Chebyshev coefficients in FP64: L = W V, W = DCT-I weights
 //                   on the product grid, rows 0..N (truncation, REF:1686-1704)
-//   k_curl          dz of H1, H3 by FP64 warp scans, h_v = k^2 H2 + i a D H1 + i b D H3,
+//   k_curl          dz of H1, H3 by FP64 recurrences (one thread per mode), h_v = k^2 H2 + i a D H1 + i b D H3,
 //                   h_g = i a H3 - i b H1 (REF:1502-1540), written as tile images
 //   k_tc_gemm_gl    Gauss-Lobatto values T0 h (REF:1573-1609) into the FP64
 //                   history buffers
@@ -33,150 +33,122 @@ namespace chf {
 
 namespace {
 
-constexpr int CM = 8;           // modes per CTA in k_curl
-constexpr int CURL_THREADS = 256;
+constexpr int CURL_THREADS = 128;  // modes per CTA in k_curl
 
-// dz (REF:570-599) of a[0..N] (stride as) into b (stride bs) by one warp, in
-// FP64: suffix sums per parity class, lane-local then a warp scan (the scheme
-// of k_solve.cu)
-__device__ __forceinline__ void warp_deriv_d(const double* a, int as, double* b, int bs, int N) {
-  const int lane = threadIdx.x & 31;
-  const int E = (N + 32) / 32;
-  const int i0 = lane * E;
-  double te = 0.0, to = 0.0;
-  for (int q = 0; q < E; ++q) {
-    int j = i0 + q;
-    if (j <= N) {
-      double g = 2.0 * (double)j * a[j * as];
-      if (j & 1) to += g; else te += g;
-    }
-  }
-  double se = te, so = to;
-  for (int off = 1; off < 32; off <<= 1) {
-    double ue = __shfl_down_sync(0xffffffffu, se, off);
-    double uo = __shfl_down_sync(0xffffffffu, so, off);
-    if (lane + off < 32) { se += ue; so += uo; }
-  }
-  double re_ = se - te, ro = so - to;
-  for (int q = E - 1; q >= 0; --q) {
-    int i = i0 + q;
-    if (i <= N) {
-      double bi = (i & 1) ? re_ : ro;
-      if (i == 0) bi *= 0.5;
-      b[i * bs] = bi;
-      double g = 2.0 * (double)i * a[i * as];
-      if (i & 1) ro += g; else re_ += g;
-    }
-  }
-  __syncwarp();
-}
-
-// grid (ceil(modes / CM)), CURL_THREADS threads.
+// One thread per mode, grid (ceil(modes / CURL_THREADS)).
 // lc: 3 fields [NZ][ncols] FP64 (H1, H2, H3 coefficients from the exact z
 // transform); out: fixed-point digit images and column exponents for the GL
 // GEMM (k_tcgemm.cu layout), field 0 = h_v, field 1 = h_g (mode (0,0)
 // carries H1, H3).  FP64 up to h_v, h_g: h_v is a small remainder of
 // k^2 H2 + i a D H1 + i b D H3 (the gradient part of the Lamb vector
 // cancels), so FP32 derivatives would leave an error ~100x FP32 rounding in
-// it.  h_v, h_g are then rounded to FP32 (a relative error per coefficient)
-// and split into digits below their column's power of two.
+// it.  D H1, D H3 follow dz's backward recurrence (REF:570-599) in
+// registers.  Two descending passes: the first finds each column's largest
+// |value| (its power of two), the second rounds h_v, h_g to FP32 (a relative
+// error per coefficient) and writes their digits, 8 rows per 16-byte store.
+__device__ __forceinline__ void curl_at(const double* __restrict__ lc, long ncols, long m, int k, int NZ,
+                                        double a, double b, double k2, bool mean, double* dh1, double* dh3,
+                                        double* h1k1, double* h3k1, int N, float* out) {
+  const size_t base = (size_t)k * ncols + 2 * m;
+  const double2 H1 = *reinterpret_cast<const double2*>(lc + base);
+  const double2 H2 = *reinterpret_cast<const double2*>(lc + (size_t)NZ * ncols + base);
+  const double2 H3 = *reinterpret_cast<const double2*>(lc + (size_t)2 * NZ * ncols + base);
+  // dh*[0..1]: b_{k+1}, dh*[2..3]: b_{k+2} per component; h*k1: values at k+1
+  double d1[2], d3[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const double n1 = k == N ? 0.0 : dh1[2 + c] + 2.0 * (double)(k + 1) * h1k1[c];
+    const double n3 = k == N ? 0.0 : dh3[2 + c] + 2.0 * (double)(k + 1) * h3k1[c];
+    dh1[2 + c] = dh1[c];
+    dh1[c] = n1;
+    dh3[2 + c] = dh3[c];
+    dh3[c] = n3;
+    d1[c] = k == 0 ? 0.5 * n1 : n1;
+    d3[c] = k == 0 ? 0.5 * n3 : n3;
+  }
+  h1k1[0] = H1.x;
+  h1k1[1] = H1.y;
+  h3k1[0] = H3.x;
+  h3k1[1] = H3.y;
+  if (mean) {
+    out[0] = (float)H1.x;
+    out[1] = (float)H1.y;
+    out[2] = (float)H3.x;
+    out[3] = (float)H3.y;
+  } else {
+    out[0] = (float)(k2 * H2.x - a * d1[1] - b * d3[1]);  // h_v = k2 H2 + i a D H1 + i b D H3
+    out[1] = (float)(k2 * H2.y + a * d1[0] + b * d3[0]);
+    out[2] = (float)(-a * H3.y + b * H1.y);                // h_g = i a H3 - i b H1
+    out[3] = (float)(a * H3.x - b * H1.x);
+  }
+}
+
 __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict__ lc,
                                                        const double* __restrict__ iapha,
                                                        const double* __restrict__ ibeta, Dims d,
                                                        const __grid_constant__ FxPlan plan,
                                                        uint8_t* __restrict__ bimg, int* __restrict__ bexp) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int NZ = d.NZ, N = d.N;
   const long modes = d.modes(), ncols = 2 * modes;
-  double* L = reinterpret_cast<double*>(smem_raw);     // [3][NZ][CM][2]
-  double* D = L + 3 * NZ * CM * 2;                     // [4][CM][NZ]: D H1.re, D H1.im, D H3.re, D H3.im
-  float* Hs = reinterpret_cast<float*>(D + 4 * CM * NZ);  // [2][NZ][CM][2]: h_v, h_g
-  __shared__ int s_e[2][CM * 2];
-  const long m0 = (long)blockIdx.x * CM;
-  for (int t = threadIdx.x; t < 3 * NZ * CM * 2; t += blockDim.x) {
-    int c = t % (CM * 2), n = (t / (CM * 2)) % NZ, f = t / (CM * 2 * NZ);
-    long col = 2 * m0 + c;
-    L[t] = col < ncols ? lc[(size_t)f * NZ * ncols + (size_t)n * ncols + col] : 0.0;
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5;
-  for (int task = warp; task < 4 * CM; task += CURL_THREADS / 32) {
-    int comp = task / CM, l = task % CM;
-    int f = comp < 2 ? 0 : 2, reim = comp & 1;
-    warp_deriv_d(L + (size_t)f * NZ * CM * 2 + l * 2 + reim, CM * 2, D + ((size_t)comp * CM + l) * NZ, 1, N);
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < NZ * CM * 2; t += blockDim.x) {
-    const int c = t % (CM * 2), n = t / (CM * 2);
-    const int l = c / 2, reim = c % 2;
-    const long m = m0 + l;
-    float v = 0.f, w = 0.f;
-    if (m < modes) {
-      const int kx = (int)(m % d.KX), ky = (int)(m / d.KX);
-      const double a = iapha[kx], b = ibeta[ky], k2 = a * a + b * b;
-      const double* h1 = L + ((size_t)0 * NZ + n) * CM * 2 + l * 2;
-      const double* h2 = L + ((size_t)1 * NZ + n) * CM * 2 + l * 2;
-      const double* h3 = L + ((size_t)2 * NZ + n) * CM * 2 + l * 2;
-      const double d1r = D[(0 * CM + l) * NZ + n], d1i = D[(1 * CM + l) * NZ + n];
-      const double d3r = D[(2 * CM + l) * NZ + n], d3i = D[(3 * CM + l) * NZ + n];
-      if (m == 0) {
-        v = (float)h1[reim];
-        w = (float)h3[reim];
-      } else if (reim == 0) {
-        v = (float)(k2 * h2[0] - a * d1i - b * d3i);   // h_v = k2 H2 + i a D H1 + i b D H3
-        w = (float)(-a * h3[1] + b * h1[1]);           // h_g = i a H3 - i b H1
-      } else {
-        v = (float)(k2 * h2[1] + a * d1r + b * d3r);
-        w = (float)(a * h3[0] - b * h1[0]);
-      }
+  const long m = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= modes) return;
+  const int N = d.N, NZ = d.NZ;
+  const double a = iapha[m % d.KX], b = ibeta[m / d.KX], k2 = a * a + b * b;
+  const bool mean = (m == 0);
+  // pass 1: column maxima of h_v re, h_v im, h_g re, h_g im
+  float mx[4] = {0.f, 0.f, 0.f, 0.f};
+  {
+    double dh1[4] = {0, 0, 0, 0}, dh3[4] = {0, 0, 0, 0}, h1k1[2] = {0, 0}, h3k1[2] = {0, 0};
+    for (int k = N; k >= 0; --k) {
+      float o[4];
+      curl_at(lc, ncols, m, k, NZ, a, b, k2, mean, dh1, dh3, h1k1, h3k1, N, o);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) mx[q] = fmaxf(mx[q], fabsf(o[q]));
     }
-    Hs[(size_t)n * CM * 2 + c] = v;
-    Hs[(size_t)(NZ + n) * CM * 2 + c] = w;
   }
-  __syncthreads();
-  // column exponents: max |value| < 2^e
-  if (threadIdx.x < 2 * CM * 2) {
-    const int f = threadIdx.x / (CM * 2), c = threadIdx.x % (CM * 2);
-    float mx = 0.f;
-    for (int n = 0; n < NZ; ++n) mx = fmaxf(mx, fabsf(Hs[(size_t)(f * NZ + n) * CM * 2 + c]));
-    int e = 0;
-    if (mx > 0.f) (void)frexpf(mx, &e);
-    s_e[f][c] = e;
-    const long col = 2 * m0 + c;
-    if (col < ncols) bexp[(size_t)f * plan.bexp_stride() + col] = e;
+  int e[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    e[q] = 0;
+    if (mx[q] > 0.f) (void)frexpf(mx[q], &e[q]);
+    bexp[(size_t)(q / 2) * plan.bexp_stride() + 2 * m + (q & 1)] = e[q];
   }
-  __syncthreads();
-  // one thread per (column c of this CTA, 8-row group g): 8 digits per plane
-  // and field, one 16-byte store each
-  const int groups = plan.kpad / 8;
-  for (int t = threadIdx.x; t < CM * 2 * groups; t += blockDim.x) {
-    const int c = t % (CM * 2), g = t / (CM * 2);
-    const long col = 2 * m0 + c;
-    if (col >= ncols) continue;
-    const int nt = (int)(col / FX_NT), r = (int)(col % FX_NT);
+  // pass 2: digits, groups of 8 rows from the top (rows >= NZ are zero)
+  double dh1[4] = {0, 0, 0, 0}, dh3[4] = {0, 0, 0, 0}, h1k1[2] = {0, 0}, h3k1[2] = {0, 0};
+  for (int g = plan.kpad / 8 - 1; g >= 0; --g) {
+    float val[4][8];
+#pragma unroll
+    for (int q = 7; q >= 0; --q) {
+      const int k = 8 * g + q;
+      float o[4] = {0.f, 0.f, 0.f, 0.f};
+      if (k <= N) curl_at(lc, ncols, m, k, NZ, a, b, k2, mean, dh1, dh3, h1k1, h3k1, N, o);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) val[c][q] = o[c];
+    }
     const int ch = (8 * g) / TC_KC, kl = 8 * g - ch * TC_KC;
     const uint32_t pbytes = (uint32_t)FX_NT * plan.kc[ch] * 2u;
-    const size_t off = ((size_t)(kl / 8) * (FX_NT / 8) + r / 8) * 128 + (r % 8) * 16;
-    for (int f = 0; f < 2; ++f) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const long col = 2 * m + (c & 1);
+      const int nt = (int)(col / FX_NT), r = (int)(col % FX_NT);
+      const size_t off = ((size_t)(kl / 8) * (FX_NT / 8) + r / 8) * 128 + (r % 8) * 16;
+      uint8_t* base = bimg + (size_t)(c / 2) * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes +
+                      plan.b_chunk_off[ch];
       uint16_t hd[FX_PLANES][8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        const int n = 8 * g + q;
-        const float x = n < NZ ? Hs[(size_t)(f * NZ + n) * CM * 2 + c] : 0.f;
         float dg[FX_PLANES];
-        tc::fx_digits_f(x, s_e[f][c], dg);
+        tc::fx_digits_f(val[c][q], e[c], dg);
 #pragma unroll
         for (int i = 0; i < FX_PLANES; ++i) hd[i][q] = tc::bf16_bits(dg[i]);
       }
-      uint8_t* base = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes + plan.b_chunk_off[ch];
 #pragma unroll
       for (int pl = 0; pl < FX_PLANES; ++pl) {
-        uint4 u;
-        u.x = (uint32_t)hd[pl][0] | ((uint32_t)hd[pl][1] << 16);
-        u.y = (uint32_t)hd[pl][2] | ((uint32_t)hd[pl][3] << 16);
-        u.z = (uint32_t)hd[pl][4] | ((uint32_t)hd[pl][5] << 16);
-        u.w = (uint32_t)hd[pl][6] | ((uint32_t)hd[pl][7] << 16);
-        *reinterpret_cast<uint4*>(base + (size_t)pl * pbytes + off) = u;
+        uint4 u4;
+        u4.x = (uint32_t)hd[pl][0] | ((uint32_t)hd[pl][1] << 16);
+        u4.y = (uint32_t)hd[pl][2] | ((uint32_t)hd[pl][3] << 16);
+        u4.z = (uint32_t)hd[pl][4] | ((uint32_t)hd[pl][5] << 16);
+        u4.w = (uint32_t)hd[pl][6] | ((uint32_t)hd[pl][7] << 16);
+        *reinterpret_cast<uint4*>(base + (size_t)pl * pbytes + off) = u4;
       }
     }
   }
@@ -308,15 +280,9 @@ int launch_nonlinear_mixed(Handle* h) {
     return rc;
   // curl / projection -> digit images for the GL transform
   {
-    size_t smem = sizeof(double) * ((size_t)3 * d.NZ * CM * 2 + (size_t)4 * CM * d.NZ) +
-                  sizeof(float) * (size_t)2 * d.NZ * CM * 2;
-    if (smem > 48 * 1024 &&
-        !cuda_ok(h, cudaFuncSetAttribute(k_curl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                 "k_curl smem"))
-      return CHF_E_CUDA;
     cudaEvent_t ev;
     prof_begin(h, K_CURL32, &ev);
-    k_curl<<<(unsigned)((modes + CM - 1) / CM), CURL_THREADS, smem, h->stream>>>(
+    k_curl<<<(unsigned)((modes + CURL_THREADS - 1) / CURL_THREADS), CURL_THREADS, 0, h->stream>>>(
         h->lc64, h->iapha, h->ibeta, d, h->tgl, h->bimg, h->bexp);
     prof_end(h, K_CURL32, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_curl")) return CHF_E_CUDA;

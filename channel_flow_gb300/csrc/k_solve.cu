@@ -42,20 +42,6 @@ namespace {
 constexpr int S_THREADS = 256;
 constexpr int INV_THREADS = 256;
 
-// Offsets of the four blocks inside one k^2 entry of xinv.
-struct BlockOffsets {
-  size_t ve, vo, we, wo;
-};
-
-__host__ __device__ inline BlockOffsets block_offsets(const SolveLayout& s) {
-  BlockOffsets b;
-  b.ve = 0;
-  b.vo = b.ve + (size_t)s.ne_v * s.ne_v;
-  b.we = b.vo + (size_t)s.no_v * s.no_v;
-  b.wo = b.we + (size_t)s.ne_w * s.ne_w;
-  return b;
-}
-
 // ---------------------------------------------------------------------------
 // Set-up: assemble one even/odd block of the v or omega_y collocation
 // operator (get_coef_v REF:3348-3381, get_coef_omegay REF:3432-3455) for one
@@ -187,10 +173,7 @@ struct SolveArgs {
   FftPlan pz2;
   const cd* tw2;
   int nk2;
-  // mixed path: xinv as (hi, lo) float pairs and double-float twiddles of
-  // the 2N-point DFT
-  const float2* xinv2;
-  const cplx<df32>* tw2d;
+  int g0;  // group of CTA 0 (nk2: the (0,0) mode alone)
   // constant flow rate: influence function phi of a unit mean pressure
   // gradient over one step, its bulk velocity, and the device word
   // flow = {target bulk velocity (0: off), last correction, bulk before, bulk after}
@@ -199,10 +182,6 @@ struct SolveArgs {
   double* flow;
 };
 
-// rhs of the increment solve: (hi, lo) floats of the real and imaginary parts
-struct RhsHL {
-  float hr, hi, lr, li;
-};
 
 constexpr int CH = 2;          // modes per chunk
 constexpr int S_WARPS = S_THREADS / 32;
@@ -265,18 +244,8 @@ __device__ __forceinline__ double* dslot(const ChunkSmem& s, int m, int q, int N
 
 // MB2 bounds the radix-2 butterflies per thread of the 2N-point DFTs (2 up
 // to nnz = 128, 4 up to nnz = 256)
-// MIX (mixed path, every group but the (0,0) mode): the new coefficients are
-// x = c + delta with A delta = r, r = (B - A) c + dt (3/2 N^n - 1/2 N^{n-1})
-// on the collocation rows, B - A = (dt/re) (D^2 - k^2)^2 for v and
-// (dt/re) (D^2 - k^2) for omega_y (the CN operators of get_coef_v /
-// get_coef_omegay and get_coef_rhs / get_rhs_omegay, REF:3348-3489), and zero
-// boundary rows (c already satisfies the wall conditions).  The derivative
-// scans and sums stay FP64; the 2N-point DFT of (B - A) c runs in
-// double-float arithmetic (df32.cuh) and the inverse matvec multiplies
-// (hi, lo) float splits of the inverse and of r with compensated (TwoSum)
-// FP32 accumulation: both about 2^-44 accurate, on the FP32 pipe.
-template <int MB2, bool MIX>
-__global__ void __launch_bounds__(S_THREADS, MIX ? 2 : 3) k_solve(const __grid_constant__ SolveArgs a) {
+template <int MB2>
+__global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ SolveArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Dims& d = a.d;
   const int N = d.N, NZ = d.NZ, L2 = 2 * N;
@@ -295,9 +264,8 @@ __global__ void __launch_bounds__(S_THREADS, MIX ? 2 : 3) k_solve(const __grid_c
   }
   for (int j = threadIdx.x; j < NZ; j += blockDim.x) s.tj[j] = 2.0 * (double)j;
   __syncthreads();
-  const int g = blockIdx.x;
+  const int g = blockIdx.x + a.g0;
   const bool mean = (g == a.nk2);
-  const bool mix = MIX && !mean;
   const double dt = a.dt, re = a.re;
   const double k2 = mean ? 0.0 : a.k2vals[g];
   const double* X = a.xinv + (size_t)g * a.sl.stride;
@@ -362,16 +330,13 @@ __global__ void __launch_bounds__(S_THREADS, MIX ? 2 : 3) k_solve(const __grid_c
     }
     __syncthreads();
     // ---- C: explicit right-hand sides as Chebyshev series -> DFT lines
-    // (FP64 lines of B c; mixed: double-float lines of (B - A) c in the same bytes)
     {
-      const double v4 = mix ? dt / re : dt * 0.5 / re;
-      const double v2 = mix ? -2.0 * k2 * dt / re : 1.0 - k2 * dt / re;
-      const double v0 = mix ? k2 * k2 * dt / re : -k2 * (1.0 - k2 * dt * 0.5 / re);
-      const double w2 = mix ? dt / re : dt * 0.5 / re;
-      const double w0 = mix ? -k2 * dt / re : 1.0 - k2 * dt * 0.5 / re;
-      cplx<df32>* fbd = reinterpret_cast<cplx<df32>*>(s.fb);
+      const double v4 = dt * 0.5 / re, v2 = 1.0 - k2 * dt / re, v0 = -k2 * (1.0 - k2 * dt * 0.5 / re);
+      const double w2 = dt * 0.5 / re, w0 = 1.0 - k2 * dt * 0.5 / re;
       for (int t = tid; t < CH * NZ; t += blockDim.x) {
         int m = t / NZ, n = t % NZ;
+        cd* lv = s.fb + (2 * m) * L2;
+        cd* lw = s.fb + (2 * m + 1) * L2;
         cd cv = s.cv[t], co = s.co[t];
         cd wv{0.0, 0.0}, ww{0.0, 0.0};
         if (m < nm) {
@@ -385,91 +350,44 @@ __global__ void __launch_bounds__(S_THREADS, MIX ? 2 : 3) k_solve(const __grid_c
         double dbl = (n == 0 || n == N) ? 2.0 : 1.0;
         // the omega line's first 2*NZ doubles held D1 scratch; all reads of
         // it finished before the barrier above
-        if (mix) {
-          cplx<df32>* lv = fbd + (2 * m) * L2;
-          cplx<df32>* lw = fbd + (2 * m + 1) * L2;
-          lv[n] = cplx<df32>{df32(dbl * wv.re), df32(dbl * wv.im)};
-          lw[n] = cplx<df32>{df32(dbl * ww.re), df32(dbl * ww.im)};
-          if (n > 0 && n < N) {
-            lv[L2 - n] = cplx<df32>{df32(wv.re), df32(wv.im)};
-            lw[L2 - n] = cplx<df32>{df32(ww.re), df32(ww.im)};
-          }
-        } else {
-          cd* lv = s.fb + (2 * m) * L2;
-          cd* lw = s.fb + (2 * m + 1) * L2;
-          lv[n] = cd{dbl * wv.re, dbl * wv.im};
-          lw[n] = cd{dbl * ww.re, dbl * ww.im};
-          if (n > 0 && n < N) {
-            lv[L2 - n] = wv;
-            lw[L2 - n] = ww;
-          }
+        lv[n] = cd{dbl * wv.re, dbl * wv.im};
+        lw[n] = cd{dbl * ww.re, dbl * ww.im};
+        if (n > 0 && n < N) {
+          lv[L2 - n] = wv;
+          lw[L2 - n] = ww;
         }
       }
     }
     __syncthreads();
-    if (mix)
-      smem_fft<df32, -1, MB2>(reinterpret_cast<cplx<df32>*>(s.fb), 2 * CH, L2, a.pz2, a.tw2d);
-    else
-      smem_fft<double, -1, MB2>(s.fb, 2 * CH, L2, a.pz2, a.tw2);
+    smem_fft<double, -1, MB2>(s.fb, 2 * CH, L2, a.pz2, a.tw2);
     // ---- D: fold the collocation rows into even / odd right-hand sides.
     // rhs storage reuses dd: [CH][4 blocks][NZ] complex (fits in 10*NZ doubles)
     const int nev = sl.ne_v, nov = sl.no_v, new_ = sl.ne_w, now_ = sl.no_w;
     cd* rhs = reinterpret_cast<cd*>(s.dd);  // rhs[(m*4 + b) * NZ + r]
-    RhsHL* rhsf = reinterpret_cast<RhsHL*>(s.dd);
     for (int t = tid; t < CH * NZ; t += blockDim.x) {
       int m = t / NZ, r = t % NZ;
-      cd lvp, lvq, lwp, lwq;
-      {
-        const int p = r, q = N - r;
-        if (mix) {
-          const cplx<df32>* lv = reinterpret_cast<const cplx<df32>*>(s.fb) + (2 * m) * L2;
-          const cplx<df32>* lw = reinterpret_cast<const cplx<df32>*>(s.fb) + (2 * m + 1) * L2;
-          lvp = cd{lv[p].re.to_double(), lv[p].im.to_double()};
-          lvq = cd{lv[q].re.to_double(), lv[q].im.to_double()};
-          lwp = cd{lw[p].re.to_double(), lw[p].im.to_double()};
-          lwq = cd{lw[q].re.to_double(), lw[q].im.to_double()};
-        } else {
-          const cd* lv = s.fb + (2 * m) * L2;
-          const cd* lw = s.fb + (2 * m + 1) * L2;
-          lvp = lv[p];
-          lvq = lv[q];
-          lwp = lw[p];
-          lwq = lw[q];
-        }
-      }
+      const cd* lv = s.fb + (2 * m) * L2;
+      const cd* lw = s.fb + (2 * m + 1) * L2;
       cd ev{0.0, 0.0}, ovv{0.0, 0.0}, ew{0.0, 0.0}, ow{0.0, 0.0};
       if (m < nm && r <= N / 2) {
         int p = r, q = N - r;
         if (!mean && r >= 2) {
-          cd Rp{0.5 * lvp.re + s.rv[m * NZ + p].re, 0.5 * lvp.im + s.rv[m * NZ + p].im};
-          cd Rq{0.5 * lvq.re + s.rv[m * NZ + q].re, 0.5 * lvq.im + s.rv[m * NZ + q].im};
+          cd Rp{0.5 * lv[p].re + s.rv[m * NZ + p].re, 0.5 * lv[p].im + s.rv[m * NZ + p].im};
+          cd Rq{0.5 * lv[q].re + s.rv[m * NZ + q].re, 0.5 * lv[q].im + s.rv[m * NZ + q].im};
           ev = cd{0.5 * (Rp.re + Rq.re), 0.5 * (Rp.im + Rq.im)};
           ovv = cd{0.5 * (Rp.re - Rq.re), 0.5 * (Rp.im - Rq.im)};
         }
         if (r >= 1) {
-          cd Rp{0.5 * lwp.re + s.rg[m * NZ + p].re, 0.5 * lwp.im + s.rg[m * NZ + p].im};
-          cd Rq{0.5 * lwq.re + s.rg[m * NZ + q].re, 0.5 * lwq.im + s.rg[m * NZ + q].im};
+          cd Rp{0.5 * lw[p].re + s.rg[m * NZ + p].re, 0.5 * lw[p].im + s.rg[m * NZ + p].im};
+          cd Rq{0.5 * lw[q].re + s.rg[m * NZ + q].re, 0.5 * lw[q].im + s.rg[m * NZ + q].im};
           ew = cd{0.5 * (Rp.re + Rq.re), 0.5 * (Rp.im + Rq.im)};
           ow = cd{0.5 * (Rp.re - Rq.re), 0.5 * (Rp.im - Rq.im)};
         }
       }
-      // all lines were read into registers above; dd (the rhs) and fb (the
-      // lines) do not overlap, so rhs can be written in place
-      if (mix) {
-        auto hl = [](cd x) {
-          const float hr = (float)x.re, hi = (float)x.im;
-          return RhsHL{hr, hi, (float)(x.re - (double)hr), (float)(x.im - (double)hi)};
-        };
-        if (r < nev) rhsf[(m * 4 + 0) * NZ + r] = hl(ev);
-        if (r < nov) rhsf[(m * 4 + 1) * NZ + r] = hl(ovv);
-        if (r < new_) rhsf[(m * 4 + 2) * NZ + r] = hl(ew);
-        if (r < now_) rhsf[(m * 4 + 3) * NZ + r] = hl(ow);
-      } else {
-        if (r < nev) rhs[(m * 4 + 0) * NZ + r] = ev;
-        if (r < nov) rhs[(m * 4 + 1) * NZ + r] = ovv;
-        if (r < new_) rhs[(m * 4 + 2) * NZ + r] = ew;
-        if (r < now_) rhs[(m * 4 + 3) * NZ + r] = ow;
-      }
+      if (r < nev) rhs[(m * 4 + 0) * NZ + r] = ev;
+      if (r < nov) rhs[(m * 4 + 1) * NZ + r] = ovv;
+      if (r < new_) rhs[(m * 4 + 2) * NZ + r] = ew;
+      if (r < now_) rhs[(m * 4 + 3) * NZ + r] = ow;
     }
     __syncthreads();
     // ---- E: block matvecs, each inverse element used for every mode of the chunk
@@ -482,61 +400,25 @@ __global__ void __launch_bounds__(S_THREADS, MIX ? 2 : 3) k_solve(const __grid_c
         else if (t < nev + nov + new_) { b = 2; row = t - nev - nov; n = new_; r0 = 1; }
         else { b = 3; row = t - nev - nov - new_; n = now_; r0 = 1; }
         if (mean && b < 2) continue;
-        const size_t boff = b == 0 ? bo.ve : b == 1 ? bo.vo : b == 2 ? bo.we : bo.wo;
+        const double* Xb = X + (b == 0 ? bo.ve : b == 1 ? bo.vo : b == 2 ? bo.we : bo.wo);
+        double acc[CH][2];
+#pragma unroll
+        for (int m = 0; m < CH; ++m) acc[m][0] = acc[m][1] = 0.0;
+#pragma unroll 4
+        for (int c = r0; c < n; ++c) {
+          double xv = __ldg(Xb + (size_t)c * n + row);
+#pragma unroll
+          for (int m = 0; m < CH; ++m) {
+            cd rr = rhs[(m * 4 + b) * NZ + c];
+            acc[m][0] = fma(xv, rr.re, acc[m][0]);
+            acc[m][1] = fma(xv, rr.im, acc[m][1]);
+          }
+        }
         int j = (b == 0 || b == 2) ? 2 * row : 2 * row + 1;
         cd* dst = b < 2 ? s.cv : s.co;
-        if (mix) {
-          // sum_c (xh + xl)(rh + rl): the exact product xh rh = p + pe goes
-          // through TwoSum into S (+ error into C); xh rl + xl rh and pe into C
-          const float2* Xb = a.xinv2 + (size_t)g * a.sl.stride + boff;
-          float S[CH][2], C[CH][2];
 #pragma unroll
-          for (int m = 0; m < CH; ++m) S[m][0] = S[m][1] = C[m][0] = C[m][1] = 0.f;
-#pragma unroll 2
-          for (int c = r0; c < n; ++c) {
-            const float2 x = __ldg(Xb + (size_t)c * n + row);
-#pragma unroll
-            for (int m = 0; m < CH; ++m) {
-              const RhsHL rr = rhsf[(m * 4 + b) * NZ + c];
-              const float rh[2] = {rr.hr, rr.hi}, rl[2] = {rr.lr, rr.li};
-#pragma unroll
-              for (int q = 0; q < 2; ++q) {
-                const float p = __fmul_rn(x.x, rh[q]);
-                const float pe = __fmaf_rn(x.x, rh[q], -p);
-                const df32 t = df_two_sum(S[m][q], p);
-                S[m][q] = t.hi;
-                C[m][q] = __fadd_rn(C[m][q], __fadd_rn(__fadd_rn(t.lo, pe),
-                                                       __fmaf_rn(x.x, rl[q], __fmul_rn(x.y, rh[q]))));
-              }
-            }
-          }
-          // x = c + delta (cv / co still hold c)
-#pragma unroll
-          for (int m = 0; m < CH; ++m)
-            if (m < nm) {
-              cd c0 = dst[m * NZ + j];
-              dst[m * NZ + j] = cd{c0.re + ((double)S[m][0] + (double)C[m][0]),
-                                   c0.im + ((double)S[m][1] + (double)C[m][1])};
-            }
-        } else {
-          const double* Xb = X + boff;
-          double acc[CH][2];
-#pragma unroll
-          for (int m = 0; m < CH; ++m) acc[m][0] = acc[m][1] = 0.0;
-#pragma unroll 4
-          for (int c = r0; c < n; ++c) {
-            double xv = __ldg(Xb + (size_t)c * n + row);
-#pragma unroll
-            for (int m = 0; m < CH; ++m) {
-              cd rr = rhs[(m * 4 + b) * NZ + c];
-              acc[m][0] = fma(xv, rr.re, acc[m][0]);
-              acc[m][1] = fma(xv, rr.im, acc[m][1]);
-            }
-          }
-#pragma unroll
-          for (int m = 0; m < CH; ++m)
-            if (m < nm) dst[m * NZ + j] = cd{acc[m][0], acc[m][1]};
-        }
+        for (int m = 0; m < CH; ++m)
+          if (m < nm) dst[m * NZ + j] = cd{acc[m][0], acc[m][1]};
       }
     }
     __syncthreads();
@@ -858,7 +740,8 @@ int setup_solver_mixed(Handle* h) {
   return CHF_OK;
 }
 
-int launch_solve_fp64(Handle* h) {
+// groups g0 .. nk2 (the last CTA is the (0,0) mode)
+static int launch_solve_from(Handle* h, int g0) {
   const Dims& d = h->d;
   SolveArgs a;
   a.v = h->f[F_V];
@@ -887,8 +770,7 @@ int launch_solve_fp64(Handle* h) {
   a.re = h->cfg.re;
   a.pz2 = h->pz2;
   a.tw2 = h->tw_z2;
-  a.xinv2 = h->xinv2;
-  a.tw2d = h->twd_z2;
+  a.g0 = g0;
   a.phi = h->phi;
   a.ubphi = h->ubphi;
   a.flow = h->flow;
@@ -900,20 +782,22 @@ int launch_solve_fp64(Handle* h) {
   }
   size_t smem = sizeof(cd) * (4 * (size_t)CH * d.NZ + 2 * (size_t)CH * 2 * d.N) +
                 sizeof(double) * (10 * (size_t)CH + 1) * d.NZ;
-  const bool mix = h->cfg.precision == CHF_MIXED;
-  auto kern = mix ? (mb2 == 2 ? k_solve<2, true> : k_solve<4, true>)
-                  : (mb2 == 2 ? k_solve<2, false> : k_solve<4, false>);
+  auto kern = mb2 == 2 ? k_solve<2> : k_solve<4>;
   if (smem > 48 * 1024 &&
       !cuda_ok(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                "k_solve smem"))
     return CHF_E_CUDA;
   cudaEvent_t ev;
-  prof_begin(h, K_SOLVE, &ev);
-  kern<<<h->nk2 + 1, S_THREADS, smem, h->stream>>>(a);
-  prof_end(h, K_SOLVE, ev);
+  prof_begin(h, g0 == 0 ? K_SOLVE : K_SOLVE_MEAN, &ev);
+  kern<<<h->nk2 + 1 - g0, S_THREADS, smem, h->stream>>>(a);
+  prof_end(h, g0 == 0 ? K_SOLVE : K_SOLVE_MEAN, ev);
   if (!cuda_ok(h, cudaGetLastError(), "k_solve")) return CHF_E_CUDA;
   return CHF_OK;
 }
+
+int launch_solve_fp64(Handle* h) { return launch_solve_from(h, 0); }
+
+int launch_solve_mean(Handle* h) { return launch_solve_from(h, h->nk2); }
 
 int launch_diagnostics(Handle* h, chf_diag* out) {
   const Dims& d = h->d;
