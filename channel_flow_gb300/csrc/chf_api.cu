@@ -50,7 +50,7 @@ static std::vector<cd> twiddles(int L) {
 const char* const kKernelNames[K_COUNT] = {
     "k_zc2v", "k_yinv", "k_xprod", "k_yfwd", "k_zcurl", "k_solve", "k_diag",
     "k_tc_split_z1", "k_tc_gemm_z1", "k_tc_split_z2", "k_tc_gemm_z2", "k_curl", "k_tc_gemm_gl",
-    "k_meanfix", "k_inc_expl", "k_inc_fold", "k_inc_matvec", "k_inc_recover", "k_solve_mean"};
+    "k_meanfix", "k_inc_solve", "k_inc_recover", "k_solve_mean"};
 
 static cudaEvent_t take_event(Handle* h) {
   if (!h->event_pool.empty()) {
@@ -125,7 +125,7 @@ static void release(chf_handle* h) {
   for (auto& p : h->mean) cudaFree(p);
   void* ptrs[] = {h->iapha, h->ibeta, h->t0, h->t2, h->t4, h->k2vals, h->xinv, h->xmean,
                   h->group_start, h->group_modes, h->tw_py, h->tw_px, h->tw_z2, h->tw_zm,
-                  h->twf_py, h->twf_px, h->twd_z2, h->xinv2, h->phi, h->flow, h->stats_buf, h->pres_buf, h->inc_buf, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
+                  h->twf_py, h->twf_px, h->incm, h->incx, h->phi, h->flow, h->stats_buf, h->pres_buf, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
                   h->agl, h->bimg, h->wz32, h->wy32, h->lc64, h->aexp1, h->aexp2, h->aexp3, h->bexp};
   for (void* p : ptrs) cudaFree(p);
   for (auto& p : h->pending) {
@@ -285,7 +285,7 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
     if (rc == CHF_OK) rc = setup_solver_mixed(h);
     if (rc != CHF_OK) return fail(rc);
   }
-  h->kernels_per_step = cfg->precision == CHF_MIXED ? 15 : 6;
+  h->kernels_per_step = cfg->precision == CHF_MIXED ? 13 : 6;
   if (!cuda_ok(h, cudaStreamSynchronize(h->stream), "create sync")) return fail(CHF_E_CUDA);
   *out = h;
   return CHF_OK;

@@ -7,7 +7,6 @@
 #include <vector>
 
 #include "../../include/chflow.h"
-#include "df32.cuh"
 #include "fft_dev.cuh"
 
 namespace chf {
@@ -97,7 +96,8 @@ struct Handle {
   int nk2 = 0;
   double* k2vals = nullptr;   // nk2
   double* xinv = nullptr;     // nk2 * sl.stride
-  float2* xinv2 = nullptr;    // (hi, lo) float pairs (mixed path's increment solve)
+  float2* incm = nullptr;     // mixed solve: A^-1 (B - A) per k^2 as (hi, lo) float pairs
+  float* incx = nullptr;      // mixed solve: A^-1 per k^2 as floats
   double* xmean = nullptr;    // inverse of the (0,0) operator, NZ x NZ column-major
   int* group_start = nullptr; // nk2 + 1 (modes grouped by k^2)
   int* group_modes = nullptr; // solved modes, sorted by k^2 index
@@ -112,7 +112,6 @@ struct Handle {
   FftPlan py, px, pz2, pzm;   // PY, PX, 2N, 2MZ
   cd *tw_py = nullptr, *tw_px = nullptr, *tw_z2 = nullptr, *tw_zm = nullptr;
   cf *twf_py = nullptr, *twf_px = nullptr;
-  cplx<df32>* twd_z2 = nullptr;  // double-float twiddles of the 2N-point DFT
 
   // work buffers
   cd* wz = nullptr;   // 6 x [MP][KY][KX]  (values on the product grid)
@@ -120,7 +119,6 @@ struct Handle {
   void* scratch = nullptr;  // reduction scratch (diagnostics)
   void* stats_buf = nullptr;  // chf_statistics: GL values of u, v, w + plane sums (first call)
   void* pres_buf = nullptr;   // chf_pressure: Lamb coefficients, right-hand sides, P (first call)
-  void* inc_buf = nullptr;    // mixed solve: explicit increments and folded right-hand sides
   size_t scratch_bytes = 0;
 
   // mixed-precision path (k_mixed.cu): FP32 transforms, tcgen05 GEMMs
@@ -170,7 +168,7 @@ struct Handle {
 enum KernelId {
   K_ZC2V = 0, K_YINV, K_XPROD, K_YFWD, K_ZCURL, K_SOLVE, K_DIAG,
   K_SPLIT_Z1, K_GEMM_Z1, K_SPLIT_Z2, K_GEMM_Z2, K_CURL32, K_GEMM_GL, K_MEANFIX,
-  K_INC_EXPL, K_INC_FOLD, K_INC_MATVEC, K_INC_RECOVER, K_SOLVE_MEAN, K_COUNT
+  K_INC_SOLVE, K_INC_RECOVER, K_SOLVE_MEAN, K_COUNT
 };
 extern const char* const kKernelNames[K_COUNT];
 

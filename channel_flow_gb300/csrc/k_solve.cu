@@ -33,7 +33,6 @@
 #include <vector>
 
 #include "chf_internal.h"
-#include "df32.cuh"
 
 namespace chf {
 
@@ -709,34 +708,6 @@ int setup_solver(Handle* h) {
     return CHF_E_NUMERIC;
   }
   (void)NZ;
-  return CHF_OK;
-}
-
-namespace {
-__global__ void k_to_hilo(const double* __restrict__ a, float2* __restrict__ b, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const float hi = (float)a[i];
-    b[i] = make_float2(hi, (float)(a[i] - (double)hi));
-  }
-}
-}  // namespace
-
-// (hi, lo) float pairs of the implicit-operator inverses and double-float
-// twiddles of the 2N-point DFT for the mixed path's increment solve.
-int setup_solver_mixed(Handle* h) {
-  const size_t n = h->sl.stride * (size_t)(h->nk2 + 1);
-  if (!cuda_ok(h, cudaMalloc((void**)&h->xinv2, sizeof(float2) * n), "xinv2")) return CHF_E_NOMEM;
-  k_to_hilo<<<1216, 256, 0, h->stream>>>(h->xinv, h->xinv2, n);
-  if (!cuda_ok(h, cudaGetLastError(), "k_to_hilo")) return CHF_E_CUDA;
-  const int L = 2 * h->d.N;
-  std::vector<cplx<df32>> tw(L);
-  for (int k = 0; k < L; ++k) {
-    const double t = -2.0 * 3.14159265358979323846 * (double)k / (double)L;
-    tw[k] = cplx<df32>{df32(std::cos(t)), df32(std::sin(t))};
-  }
-  if (!cuda_ok(h, cudaMalloc((void**)&h->twd_z2, sizeof(cplx<df32>) * L), "twd_z2") ||
-      !cuda_ok(h, cudaMemcpy(h->twd_z2, tw.data(), sizeof(cplx<df32>) * L, cudaMemcpyHostToDevice), "twd_z2"))
-    return CHF_E_CUDA;
   return CHF_OK;
 }
 

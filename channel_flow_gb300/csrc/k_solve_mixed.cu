@@ -1,26 +1,27 @@
-// k_solve_mixed.cu -- the implicit solve of the mixed path as four kernels.
+// k_solve_mixed.cu -- the implicit solve of the mixed path.
 //
 // The per-mode solve (poiseuilleflow.f90:242-394) for every (kx, ky) but the
 // (0,0) mode, written as an FP64 state plus an increment:
-//   x = c + delta,   A delta = r,   r = (B - A) c + dt (3/2 N^n - 1/2 N^{n-1})
+//   x = c + delta,   delta = A^-1 (B - A) c + A^-1 r,
+//   r = dt (3/2 N^n - 1/2 N^{n-1})
 // on the collocation rows and 0 on the wall rows, with B - A =
 // (dt/re) (D^2 - k^2)^2 for v and (dt/re) (D^2 - k^2) for omega_y (the CN
 // operators of get_coef_v / get_coef_omegay and of get_coef_rhs /
-// get_rhs_omegay, REF:3348-3489), A^-1 the even/odd inverses of k_solve.cu.
-// delta is O(dt) smaller than x, so the DFT of (B - A) c runs in double-float
-// arithmetic (df32.cuh) and the matvec A^-1 r multiplies (hi, lo) float
-// splits with compensated FP32 accumulation, both about 2^-44 accurate, on
-// the FP32 pipe; derivative scans and x = c + delta stay FP64.  Split so that
-// every stage runs at full occupancy without CTA-wide phases:
-//   k_inc_expl     w_v = (dt/re)(D^2-k^2)^2 c_v, w_g = (dt/re)(D^2-k^2) c_g, FP64, one
-//                  thread per column running the derivative recurrences in registers
-//   k_inc_fold     double-float 2N-point DFT of w -> Gauss-Lobatto values, + AB2 term,
-//                  folded into even / odd right-hand sides, split into (hi, lo)
-//   k_inc_matvec   one CTA per k^2 group: delta = A^-1 r, x = c + delta
+// get_rhs_omegay, REF:3348-3489) and A^-1 the even/odd inverses of
+// k_solve.cu.  Forming (B - A) c at the collocation points cancels heavily
+// (fourth derivatives of the coefficients against an O(c) result), so the
+// set-up multiplies it into the inverse once per k^2 in FP64:
+// M = A^-1 (B - A) maps coefficients to coefficients and has no such
+// cancellation (its rows sum to within ~10x of the result).  A step is then
+//   k_inc_solve    one CTA per k^2 group: delta = M c (compensated FP32 on
+//                  (hi, lo) splits of M and c, about 2^-44 relative) + A^-1 r
+//                  (FP32), x = c + delta in FP64
 //   k_inc_recover  u, w, omega_x, omega_z from v and omega_y (getvelocityandvorticity,
 //                  REF:2347-2407), FP64, one thread per (mode, re/im)
 // The (0,0) mode (REF:401-474) stays with k_solve (FP64, one CTA).
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "chf_internal.h"
 #include "df32.cuh"
@@ -30,22 +31,11 @@ namespace chf {
 namespace {
 
 constexpr int I_THREADS = 256;
-constexpr int FL = 4;            // modes per CTA in the DFT kernel (2 lines each)
 constexpr int MV_THREADS = 288;  // threads over the 2 NZ rows of one group's four blocks
-constexpr int MCH = 4;           // modes per pass in the matvec kernel
+constexpr int MCH = 4;           // modes per pass in k_inc_solve
 
-struct RhsHL {
-  float hr, hi, lr, li;
-};
-
-// ---------------------------------------------------------------------------
-// k_inc_expl: grid (ceil(modes / TM)).  The Chebyshev derivatives follow
-// dz's backward recurrence (REF:570-599)
-//   b_k = b_{k+2} + 2 (k+1) a_{k+1},  b_0 halved,
-// and since order j+1 at index k needs order j only at index k+1, one
-// descending pass per column carries D1..D4 of v (D1, D2 of omega_y) in
-// registers and emits w at every k.
-// ---------------------------------------------------------------------------
+// Chebyshev derivative recurrence (dz, REF:570-599), descending in k:
+//   b_k = b_{k+2} + 2 (k+1) a_{k+1}   (b_0 is halved by the caller)
 struct Rec {  // one recurrence: values at k+1 and k+2
   double b1 = 0.0, b2 = 0.0;
   __device__ __forceinline__ double step(double src_k1, int k, bool top) {
@@ -56,153 +46,126 @@ struct Rec {  // one recurrence: values at k+1 and k+2
   }
 };
 
-// TM modes per CTA: the tile [2 fields][NZ][TM][re, im] is loaded by all
-// threads (coalesced), 4 TM threads (one per field and column) run the
-// recurrences from shared memory and overwrite the tile with w, which all
-// threads then store.
-constexpr int TM = 16;
+constexpr int TM = 16;  // modes per CTA in k_inc_recover
 
-__global__ void __launch_bounds__(I_THREADS) k_inc_expl(const cd* __restrict__ v, const cd* __restrict__ g,
-                                                        cd* __restrict__ wv, cd* __restrict__ wg,
-                                                        const double* __restrict__ iapha,
-                                                        const double* __restrict__ ibeta, Dims d, double dt_re) {
+// ---------------------------------------------------------------------------
+// Set-up of the increment operators, grid (nk2, 4 blocks): with X = A^-1 the
+// block's inverse (k_solve.cu, FP64) and W the folded rows of B - A,
+//   W[q][c] = (dt/re) (T4 - 2 k^2 T2 + k^4 T0)(z_q, T_j)   (v)
+//   W[q][c] = (dt/re) (T2 - k^2 T0)(z_q, T_j)               (omega_y)
+// for q >= r0 (0 on the wall rows), j = 2c or 2c + 1, the kernel forms
+// M = X W in FP64 (W staged BW columns at a time, X read through L1) and
+// stores it as (hi, lo) float pairs, and X as floats; both column-major,
+// M[c * n + r], at the inverses' block offsets.
+// ---------------------------------------------------------------------------
+constexpr int BW = 32;  // columns of W staged per pass in k_build_incr
+
+__global__ void __launch_bounds__(256) k_build_incr(const double* __restrict__ t0,
+                                                    const double* __restrict__ t2,
+                                                    const double* __restrict__ t4,
+                                                    const double* __restrict__ k2vals,
+                                                    const double* __restrict__ xinv, SolveLayout sl, int N,
+                                                    double dt_re, float2* __restrict__ incm,
+                                                    float* __restrict__ incx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int N = d.N, NZ = d.NZ, C2 = 2 * TM;
-  const long modes = d.modes();
-  double* T = reinterpret_cast<double*>(smem_raw);  // [2][NZ][C2]
-  const long m0 = (long)blockIdx.x * TM;
-  for (int t = threadIdx.x; t < 2 * NZ * C2; t += blockDim.x) {
-    const int c = t % C2, n = (t / C2) % NZ, f = t / (C2 * NZ);
-    const long col = 2 * m0 + c;
-    const double* src = reinterpret_cast<const double*>(f == 0 ? v : g);
-    T[t] = col < 2 * modes ? src[(size_t)n * 2 * modes + col] : 0.0;
-  }
-  __syncthreads();
-  if (threadIdx.x < 2 * C2) {
-    const int f = threadIdx.x / C2, c = threadIdx.x % C2;
-    const long m = m0 + c / 2;
-    double k2 = 0.0;
-    if (m < modes) {
-      const double a = iapha[m % d.KX], b = ibeta[m / d.KX];
-      k2 = a * a + b * b;
-    }
-    double* col = T + (size_t)f * NZ * C2 + c;  // stride C2
-    Rec r1, r2, r3, r4;
-    double ck1 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;  // c, D1, D2, D3 at k+1
-    for (int k = N; k >= 0; --k) {
-      const bool top = (k == N);
-      const double ck = col[k * C2];
-      const double d1 = r1.step(ck1, k, top);
-      const double d2 = r2.step(p1, k, top);
-      double out;
-      if (f == 0) {
-        const double d3 = r3.step(p2, k, top);
-        const double d4 = r4.step(p3, k, top);
-        p3 = d3;
-        const double h = k == 0 ? 0.5 : 1.0;  // only the k = 0 outputs halve
-        out = dt_re * (h * d4 - 2.0 * k2 * h * d2 + k2 * k2 * ck);
-      } else {
-        out = dt_re * ((k == 0 ? 0.5 : 1.0) * d2 - k2 * ck);
+  const int g = blockIdx.x, blk = blockIdx.y, NZ = N + 1;
+  const bool isv = blk < 2, even = (blk % 2) == 0;
+  const int n = isv ? (even ? sl.ne_v : sl.no_v) : (even ? sl.ne_w : sl.no_w);
+  const int r0 = isv ? 2 : 1;
+  const BlockOffsets bo = block_offsets(sl);
+  const size_t off = (size_t)g * sl.stride + (blk == 0 ? bo.ve : blk == 1 ? bo.vo : blk == 2 ? bo.we : bo.wo);
+  const double* X = xinv + off;                     // column-major X[q * n + r]
+  double* W = reinterpret_cast<double*>(smem_raw);  // W[q * BW + cc], column c0 + cc
+  const double k2 = k2vals[g];
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) incx[off + t] = (float)X[t];
+  for (int c0 = 0; c0 < n; c0 += BW) {
+    const int nc = min(BW, n - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * BW; t += blockDim.x) {
+      const int q = t / BW, cc = t % BW, j = even ? 2 * (c0 + cc) : 2 * (c0 + cc) + 1;
+      double w = 0.0;
+      if (q >= r0 && cc < nc) {
+        const size_t p = (size_t)q + (size_t)NZ * j;
+        w = isv ? dt_re * (t4[p] - 2.0 * k2 * t2[p] + k2 * k2 * t0[p]) : dt_re * (t2[p] - k2 * t0[p]);
       }
-      p1 = d1;
-      p2 = d2;
-      ck1 = ck;
-      col[k * C2] = out;  // c_k is kept in ck1 for the next step
+      W[t] = w;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * nc; t += blockDim.x) {
+      const int cc = t / n, r = t % n;
+      double acc = 0.0;
+      for (int q = r0; q < n; ++q) acc = fma(X[(size_t)q * n + r], W[q * BW + cc], acc);
+      const float hi = (float)acc;
+      incm[off + (size_t)(c0 + cc) * n + r] = make_float2(hi, (float)(acc - (double)hi));
     }
   }
-  __syncthreads();
-  for (int t = threadIdx.x; t < 2 * NZ * C2; t += blockDim.x) {
-    const int c = t % C2, n = (t / C2) % NZ, f = t / (C2 * NZ);
-    const long col = 2 * m0 + c;
-    if (col < 2 * modes) reinterpret_cast<double*>(f == 0 ? wv : wg)[(size_t)n * 2 * modes + col] = T[t];
-  }
 }
 
 // ---------------------------------------------------------------------------
-// k_inc_fold: grid (ceil(modes / FL)).  2 FL double-float lines of 2N points
-// (even extension of w with doubled end coefficients), forward DFT, then
-// R = 1/2 DFT + AB2 term at the Gauss-Lobatto points, folded:
-//   even rows 1/2 (R_p + R_{N-p}), odd rows 1/2 (R_p - R_{N-p}), p = 0..N/2,
-// wall rows (v: p < 2, omega_y: p < 1) zero.  Out: rb[mode][2 NZ] (hi, lo)
-// in the order v-even (ne), v-odd (no), omega-even (ne), omega-odd (no).
+// k_inc_solve: one CTA per k^2 group (mean excluded), MCH modes of the group
+// per pass.  Per mode the CTA stages in shared memory
+//   * the coefficients c of v and omega_y as (hi, lo) floats, ordered as the
+//     four blocks' columns (v even j, v odd j, omega even j, omega odd j);
+//   * the AB2 term r = dt (3/2 N^n - 1/2 N^{n-1}) at the Gauss-Lobatto
+//     points, folded (even rows 1/2 (r_p + r_{N-p}), odd rows
+//     1/2 (r_p - r_{N-p}), p = row) with the wall rows zero, as floats;
+// then one thread per block row forms
+//   delta = M c + X r
+// M c with compensated FP32 arithmetic (the exact product of the high parts
+// added by TwoSum, the cross terms and rounding errors into a second
+// accumulator; about 2^-44 relative), X r in plain FP32 (r is O(dt) and
+// X r has no cancellation), and writes x = c + delta in FP64.
 // ---------------------------------------------------------------------------
-template <int MB2>
-__global__ void __launch_bounds__(I_THREADS) k_inc_fold(const cd* __restrict__ wv, const cd* __restrict__ wg,
-                                                        const cd* __restrict__ rv, const cd* __restrict__ uh,
-                                                        const cd* __restrict__ rg, const cd* __restrict__ wh,
-                                                        Dims d, double c3, double c1,
-                                                        const __grid_constant__ FftPlan pz2,
-                                                        const cplx<df32>* __restrict__ tw, RhsHL* __restrict__ rb) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  using C = cplx<df32>;
-  C* lines = reinterpret_cast<C*>(smem_raw);  // [2 FL][2N]: line 2l = v, 2l+1 = omega_y
-  const int N = d.N, NZ = d.NZ, L2 = 2 * N, ne = N / 2 + 1;
-  const long modes = d.modes();
-  const long m0 = (long)blockIdx.x * FL;
-  for (int t = threadIdx.x; t < 2 * FL * NZ; t += blockDim.x) {
-    const int ln = t / NZ, n = t % NZ, l = ln / 2, f = ln % 2;
-    const long m = m0 + l;
-    cd x{0.0, 0.0};
-    if (m < modes) x = (f == 0 ? wv : wg)[(size_t)n * modes + m];
-    const double dbl = (n == 0 || n == N) ? 2.0 : 1.0;
-    lines[ln * L2 + n] = C{df32(dbl * x.re), df32(dbl * x.im)};
-    if (n > 0 && n < N) lines[ln * L2 + L2 - n] = C{df32(x.re), df32(x.im)};
-  }
-  __syncthreads();
-  smem_fft<df32, -1, MB2>(lines, 2 * FL, L2, pz2, tw);
-  for (int t = threadIdx.x; t < 2 * FL * ne; t += blockDim.x) {
-    const int ln = t / ne, r = t % ne, l = ln / 2, f = ln % 2;
-    const long m = m0 + l;
-    if (m >= modes) continue;
-    const int p = r, q = N - r;
-    const C* line = lines + ln * L2;
-    const cd* H = f == 0 ? rv : rg;   // N^n (GL values)
-    const cd* Ho = f == 0 ? uh : wh;  // N^{n-1}
-    const cd hp = H[(size_t)p * modes + m], hq = H[(size_t)q * modes + m];
-    const cd op = Ho[(size_t)p * modes + m], oq = Ho[(size_t)q * modes + m];
-    const double Rp_re = 0.5 * line[p].re.to_double() + (c3 * hp.re - c1 * op.re);
-    const double Rp_im = 0.5 * line[p].im.to_double() + (c3 * hp.im - c1 * op.im);
-    const double Rq_re = 0.5 * line[q].re.to_double() + (c3 * hq.re - c1 * oq.re);
-    const double Rq_im = 0.5 * line[q].im.to_double() + (c3 * hq.im - c1 * oq.im);
-    const bool wall = (f == 0) ? (r < 2) : (r < 1);
-    const double er = wall ? 0.0 : 0.5 * (Rp_re + Rq_re), ei = wall ? 0.0 : 0.5 * (Rp_im + Rq_im);
-    const double orr = wall ? 0.0 : 0.5 * (Rp_re - Rq_re), oi = wall ? 0.0 : 0.5 * (Rp_im - Rq_im);
-    auto hl = [](double xr, double xi) {
-      const float hr = (float)xr, hi = (float)xi;
-      return RhsHL{hr, hi, (float)(xr - (double)hr), (float)(xi - (double)hi)};
-    };
-    RhsHL* out = rb + (size_t)m * 2 * NZ + (f == 0 ? 0 : NZ);
-    out[r] = hl(er, ei);                       // even block, row r (r < ne)
-    if (r < N / 2) out[ne + r] = hl(orr, oi);  // odd block, row r (r < no)
-  }
-}
+struct CoefHL {
+  float hr, hi, lr, li;  // high and low parts of the real and imaginary parts
+};
 
-// ---------------------------------------------------------------------------
-// k_inc_matvec: one CTA per k^2 group (mean excluded), threads over the rows
-// of the four blocks; MCH modes of the group per pass.  Compensated FP32: the
-// exact product xh rh = p + pe is added by TwoSum into S (error into C),
-// xh rl + xl rh + pe into C.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(MV_THREADS) k_inc_matvec(const RhsHL* __restrict__ rb,
-                                                           const float2* __restrict__ xinv2, SolveLayout sl,
-                                                           const int* __restrict__ group_start,
-                                                           const int* __restrict__ group_modes,
-                                                           cd* __restrict__ v, cd* __restrict__ g, Dims d) {
+constexpr int CB = 8;  // matrix columns loaded per batch
+
+__global__ void __launch_bounds__(MV_THREADS) k_inc_solve(cd* __restrict__ v, cd* __restrict__ g,
+                                                          const cd* __restrict__ rv, const cd* __restrict__ uh,
+                                                          const cd* __restrict__ rg, const cd* __restrict__ wh,
+                                                          const float2* __restrict__ incm,
+                                                          const float* __restrict__ incx, SolveLayout sl,
+                                                          const int* __restrict__ group_start,
+                                                          const int* __restrict__ group_modes, Dims d,
+                                                          double c3, double c1) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  RhsHL* R = reinterpret_cast<RhsHL*>(smem_raw);  // [MCH][2 NZ]
-  const int NZ = d.NZ;
+  const int N = d.N, NZ = d.NZ, ne = N / 2 + 1;
   const long modes = d.modes();
+  CoefHL* Cs = reinterpret_cast<CoefHL*>(smem_raw);        // [MCH][2 NZ]
+  float2* Rs = reinterpret_cast<float2*>(Cs + MCH * 2 * NZ);  // [MCH][2 NZ]
   const int grp = blockIdx.x;
   const int gs = group_start[grp], ge = group_start[grp + 1];
   const int nev = sl.ne_v, nov = sl.no_v, new_ = sl.ne_w, now_ = sl.no_w;
   const int rows = nev + nov + new_ + now_;
   const BlockOffsets bo = block_offsets(sl);
-  const float2* Xg = xinv2 + (size_t)grp * sl.stride;
+  const float2* Mg = incm + (size_t)grp * sl.stride;
+  const float* Xg = incx + (size_t)grp * sl.stride;
   for (int base = gs; base < ge; base += MCH) {
     const int nm = min(MCH, ge - base);
     for (int e = threadIdx.x; e < nm * 2 * NZ; e += blockDim.x) {
-      const int q = e / (2 * NZ), i = e % (2 * NZ);
-      R[e] = rb[(size_t)group_modes[base + q] * 2 * NZ + i];
+      const int q = e / (2 * NZ), i = e % (2 * NZ), f = i / NZ, k = i % NZ;
+      const long m = group_modes[base + q];
+      const cd x = (f == 0 ? v : g)[(size_t)k * modes + m];
+      const float hr = (float)x.re, hi = (float)x.im;
+      const int slot = f * NZ + ((k & 1) ? ne + k / 2 : k / 2);
+      Cs[q * 2 * NZ + slot] = CoefHL{hr, hi, (float)(x.re - (double)hr), (float)(x.im - (double)hi)};
+    }
+    for (int e = threadIdx.x; e < nm * 2 * ne; e += blockDim.x) {
+      const int q = e / (2 * ne), i = e % (2 * ne), f = i / ne, r = i % ne;
+      const long m = group_modes[base + q];
+      const cd* H = f == 0 ? rv : rg;   // N^n (GL values)
+      const cd* Ho = f == 0 ? uh : wh;  // N^{n-1}
+      const size_t ip = (size_t)r * modes + m, iq = (size_t)(N - r) * modes + m;
+      const cd hp = H[ip], hq = H[iq], op = Ho[ip], oq = Ho[iq];
+      const double pr = c3 * hp.re - c1 * op.re, pi = c3 * hp.im - c1 * op.im;
+      const double qr = c3 * hq.re - c1 * oq.re, qi = c3 * hq.im - c1 * oq.im;
+      const bool wall = (f == 0) ? (r < 2) : (r < 1);
+      float2* out = Rs + q * 2 * NZ + f * NZ;
+      out[r] = wall ? make_float2(0.f, 0.f) : make_float2((float)(0.5 * (pr + qr)), (float)(0.5 * (pi + qi)));
+      if (r < N / 2)
+        out[ne + r] = wall ? make_float2(0.f, 0.f) : make_float2((float)(0.5 * (pr - qr)), (float)(0.5 * (pi - qi)));
     }
     __syncthreads();
     for (int t = threadIdx.x; t < rows; t += blockDim.x) {
@@ -212,28 +175,54 @@ __global__ void __launch_bounds__(MV_THREADS) k_inc_matvec(const RhsHL* __restri
       else if (t < nev + nov) { b = 1; row = t - nev; n = nov; r0 = 2; boff = bo.vo; }
       else if (t < nev + nov + new_) { b = 2; row = t - nev - nov; n = new_; r0 = 1; boff = bo.we; }
       else { b = 3; row = t - nev - nov - new_; n = now_; r0 = 1; boff = bo.wo; }
-      // offset of block b inside a mode's 2 NZ right-hand-side entries
+      // offset of block b inside a mode's 2 NZ staged entries
       const int roff = b == 0 ? 0 : b == 1 ? nev : b == 2 ? NZ : NZ + new_;
-      const float2* X = Xg + boff;
-      float S[MCH][2], C[MCH][2];
+      const float2* Mb = Mg + boff + row;
+      const float* Xb = Xg + boff + row;
+      float S[MCH][2], C[MCH][2], A[MCH][2];
 #pragma unroll
-      for (int q = 0; q < MCH; ++q) S[q][0] = S[q][1] = C[q][0] = C[q][1] = 0.f;
-#pragma unroll 2
-      for (int c = r0; c < n; ++c) {
-        const float2 x = __ldg(X + (size_t)c * n + row);
+      for (int q = 0; q < MCH; ++q)
+        S[q][0] = S[q][1] = C[q][0] = C[q][1] = A[q][0] = A[q][1] = 0.f;
+      for (int c0 = 0; c0 < n; c0 += CB) {
+        float2 mm[CB];
 #pragma unroll
-        for (int q = 0; q < MCH; ++q) {
-          if (q < nm) {
-            const RhsHL rr = R[q * 2 * NZ + roff + c];
-            const float rh[2] = {rr.hr, rr.hi}, rl[2] = {rr.lr, rr.li};
+        for (int u = 0; u < CB; ++u) mm[u] = c0 + u < n ? __ldg(Mb + (size_t)(c0 + u) * n) : make_float2(0.f, 0.f);
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-              const float p = __fmul_rn(x.x, rh[k]);
-              const float pe = __fmaf_rn(x.x, rh[k], -p);
-              const df32 s = df_two_sum(S[q][k], p);
-              S[q][k] = s.hi;
-              C[q][k] = __fadd_rn(C[q][k],
-                                  __fadd_rn(__fadd_rn(s.lo, pe), __fmaf_rn(x.x, rl[k], __fmul_rn(x.y, rh[k]))));
+        for (int u = 0; u < CB; ++u) {
+          if (c0 + u < n) {
+#pragma unroll
+            for (int q = 0; q < MCH; ++q) {
+              if (q < nm) {
+                const CoefHL cc = Cs[q * 2 * NZ + roff + c0 + u];
+                const float ch[2] = {cc.hr, cc.hi}, cl[2] = {cc.lr, cc.li};
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                  const float p = __fmul_rn(mm[u].x, ch[k]);
+                  const float pe = __fmaf_rn(mm[u].x, ch[k], -p);
+                  const df32 sm = df_two_sum(S[q][k], p);
+                  S[q][k] = sm.hi;
+                  C[q][k] = __fadd_rn(C[q][k], __fadd_rn(__fadd_rn(sm.lo, pe),
+                                                         __fmaf_rn(mm[u].x, cl[k], __fmul_rn(mm[u].y, ch[k]))));
+                }
+              }
+            }
+          }
+        }
+      }
+      for (int c0 = r0; c0 < n; c0 += CB) {
+        float xx[CB];
+#pragma unroll
+        for (int u = 0; u < CB; ++u) xx[u] = c0 + u < n ? __ldg(Xb + (size_t)(c0 + u) * n) : 0.f;
+#pragma unroll
+        for (int u = 0; u < CB; ++u) {
+          if (c0 + u < n) {
+#pragma unroll
+            for (int q = 0; q < MCH; ++q) {
+              if (q < nm) {
+                const float2 rr = Rs[q * 2 * NZ + roff + c0 + u];
+                A[q][0] = __fmaf_rn(xx[u], rr.x, A[q][0]);
+                A[q][1] = __fmaf_rn(xx[u], rr.y, A[q][1]);
+              }
             }
           }
         }
@@ -245,7 +234,9 @@ __global__ void __launch_bounds__(MV_THREADS) k_inc_matvec(const RhsHL* __restri
         if (q < nm) {
           const size_t idx = (size_t)j * modes + group_modes[base + q];
           const cd c0 = dst[idx];
-          dst[idx] = cd{c0.re + ((double)S[q][0] + (double)C[q][0]), c0.im + ((double)S[q][1] + (double)C[q][1])};
+          const double dr = (double)S[q][0] + ((double)C[q][0] + (double)A[q][0]);
+          const double di = (double)S[q][1] + ((double)C[q][1] + (double)A[q][1]);
+          dst[idx] = cd{c0.re + dr, c0.im + di};
         }
       }
     }
@@ -256,7 +247,7 @@ __global__ void __launch_bounds__(MV_THREADS) k_inc_matvec(const RhsHL* __restri
 // ---------------------------------------------------------------------------
 // k_inc_recover: grid (ceil(modes / TM)); tiles of v and omega_y in shared
 // memory, one thread per (mode, re/im) running one descending pass (the
-// recurrence of k_inc_expl), the other component from its partner lane:
+// derivative recurrence), the other component from its partner lane:
 //   Dv_k -> u_k = (i a Dv - i b g) / k^2, w_k = (i b Dv + i a g) / k^2
 //   Du_k, Dw_k (from u, w at k+1) -> omega_z = -Du + i a v, omega_x = Dw - i b v
 // for every solved mode (not (0,0), not the spanwise Nyquist slot).
@@ -326,54 +317,41 @@ __global__ void __launch_bounds__(I_THREADS) k_inc_recover(const cd* __restrict_
 
 }  // namespace
 
+int setup_solver_mixed(Handle* h) {
+  const SolveLayout& sl = h->sl;
+  const size_t n = sl.stride * (size_t)h->nk2;
+  if (n == 0) return CHF_OK;
+  if (!cuda_ok(h, cudaMalloc((void**)&h->incm, sizeof(float2) * n), "increment operators") ||
+      !cuda_ok(h, cudaMalloc((void**)&h->incx, sizeof(float) * n), "increment operators"))
+    return CHF_E_NOMEM;
+  const int nmax = std::max(sl.ne_v, sl.ne_w);
+  const size_t smem = sizeof(double) * (size_t)nmax * BW;
+  if (smem > 48 * 1024 &&
+      !cuda_ok(h, cudaFuncSetAttribute(k_build_incr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+               "k_build_incr smem"))
+    return CHF_E_CUDA;
+  k_build_incr<<<dim3(h->nk2, 4), 256, smem, h->stream>>>(h->t0, h->t2, h->t4, h->k2vals, h->xinv, sl, h->d.N,
+                                                          h->cfg.dt / h->cfg.re, h->incm, h->incx);
+  if (!cuda_ok(h, cudaGetLastError(), "k_build_incr") ||
+      !cuda_ok(h, cudaStreamSynchronize(h->stream), "k_build_incr sync"))
+    return CHF_E_CUDA;
+  return CHF_OK;
+}
+
 int launch_solve_mixed(Handle* h) {
   const Dims& d = h->d;
-  const int N = d.N, NZ = d.NZ;
+  const int NZ = d.NZ;
   const long modes = d.modes();
-  const double dt = h->cfg.dt, re = h->cfg.re;
-  if (!h->inc_buf) {  // w_v, w_g (FP64 coefficients) and the folded right-hand sides
-    const size_t bytes = sizeof(cd) * 2 * (size_t)NZ * modes + sizeof(RhsHL) * 2 * (size_t)NZ * modes;
-    if (!cuda_ok(h, cudaMalloc(&h->inc_buf, bytes), "increment buffers")) return CHF_E_NOMEM;
-  }
-  cd* wv = static_cast<cd*>(h->inc_buf);
-  cd* wg = wv + (size_t)NZ * modes;
-  RhsHL* rb = reinterpret_cast<RhsHL*>(wg + (size_t)NZ * modes);
+  const double dt = h->cfg.dt;
   cudaStream_t st = h->stream;
   cudaEvent_t ev;
-  {
-    prof_begin(h, K_INC_EXPL, &ev);
-    const size_t smem = sizeof(double) * 2 * (size_t)NZ * 2 * TM;
-    if (smem > 48 * 1024 &&
-        !cuda_ok(h, cudaFuncSetAttribute(k_inc_expl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                 "k_inc_expl smem"))
-      return CHF_E_CUDA;
-    k_inc_expl<<<(unsigned)((modes + TM - 1) / TM), I_THREADS, smem, st>>>(
-        h->f[F_V], h->f[F_OY], wv, wg, h->iapha, h->ibeta, d, dt / re);
-    prof_end(h, K_INC_EXPL, ev);
-  }
-  {
-    const int mb2 = fft_fits(2 * FL, 2 * N, I_THREADS, 2) ? 2 : fft_fits(2 * FL, 2 * N, I_THREADS, 4) ? 4 : 8;
-    if (!fft_fits(2 * FL, 2 * N, I_THREADS, mb2)) {
-      h->err = "mixed solve: nnz too large for the DFT launch shape";
-      return CHF_E_INVALID;
-    }
-    const size_t smem = sizeof(cplx<df32>) * 2 * FL * 2 * N;
-    auto kern = mb2 == 2 ? k_inc_fold<2> : mb2 == 4 ? k_inc_fold<4> : k_inc_fold<8>;
-    if (smem > 48 * 1024 &&
-        !cuda_ok(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                 "k_inc_fold smem"))
-      return CHF_E_CUDA;
-    prof_begin(h, K_INC_FOLD, &ev);
-    kern<<<(unsigned)((modes + FL - 1) / FL), I_THREADS, smem, st>>>(
-        wv, wg, h->f[F_RV], h->f[F_U], h->f[F_RG], h->f[F_W], d, 1.5 * dt, 0.5 * dt, h->pz2, h->twd_z2, rb);
-    prof_end(h, K_INC_FOLD, ev);
-  }
-  {
-    const size_t smem = sizeof(RhsHL) * MCH * 2 * NZ;
-    prof_begin(h, K_INC_MATVEC, &ev);
-    k_inc_matvec<<<h->nk2, MV_THREADS, smem, st>>>(rb, h->xinv2, h->sl, h->group_start, h->group_modes,
-                                                   h->f[F_V], h->f[F_OY], d);
-    prof_end(h, K_INC_MATVEC, ev);
+  if (h->nk2 > 0) {
+    const size_t smem = (sizeof(CoefHL) + sizeof(float2)) * MCH * 2 * (size_t)NZ;
+    prof_begin(h, K_INC_SOLVE, &ev);
+    k_inc_solve<<<h->nk2, MV_THREADS, smem, st>>>(h->f[F_V], h->f[F_OY], h->f[F_RV], h->f[F_U], h->f[F_RG],
+                                                   h->f[F_W], h->incm, h->incx, h->sl, h->group_start,
+                                                   h->group_modes, d, 1.5 * dt, 0.5 * dt);
+    prof_end(h, K_INC_SOLVE, ev);
   }
   {
     prof_begin(h, K_INC_RECOVER, &ev);
