@@ -120,21 +120,35 @@ struct CoefHL {
   float hr, hi, lr, li;  // high and low parts of the real and imaginary parts
 };
 
-constexpr int CB = 8;  // matrix columns loaded per batch
+constexpr int CB = 4;  // matrix columns per load batch (two batches in flight)
 
-__global__ void __launch_bounds__(MV_THREADS) k_inc_solve(cd* __restrict__ v, cd* __restrict__ g,
-                                                          const cd* __restrict__ rv, const cd* __restrict__ uh,
-                                                          const cd* __restrict__ rg, const cd* __restrict__ wh,
-                                                          const float2* __restrict__ incm,
-                                                          const float* __restrict__ incx, SolveLayout sl,
-                                                          const int* __restrict__ group_start,
-                                                          const int* __restrict__ group_modes, Dims d,
-                                                          double c3, double c1) {
+// S + C += (mh + ml)(ch + cl), compensated: p + e = mh ch exactly, the cross
+// terms join e, TwoSum keeps the rounding error of S + p.
+__device__ __forceinline__ void comp_mac(float mh, float ml, float ch, float cl, float& S, float& C) {
+  const float p = __fmul_rn(mh, ch);
+  float e = __fmaf_rn(mh, ch, -p);
+  e = __fmaf_rn(mh, cl, e);
+  e = __fmaf_rn(ml, ch, e);
+  const df32 sm = df_two_sum(S, p);
+  S = sm.hi;
+  C = __fadd_rn(C, __fadd_rn(sm.lo, e));
+}
+
+__global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v, cd* __restrict__ g,
+                                                             const cd* __restrict__ rv, const cd* __restrict__ uh,
+                                                             const cd* __restrict__ rg, const cd* __restrict__ wh,
+                                                             const float2* __restrict__ incm,
+                                                             const float* __restrict__ incx, SolveLayout sl,
+                                                             const int* __restrict__ group_start,
+                                                             const int* __restrict__ group_modes, Dims d,
+                                                             double c3, double c1) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = d.N, NZ = d.NZ, ne = N / 2 + 1;
   const long modes = d.modes();
-  CoefHL* Cs = reinterpret_cast<CoefHL*>(smem_raw);        // [MCH][2 NZ]
-  float2* Rs = reinterpret_cast<float2*>(Cs + MCH * 2 * NZ);  // [MCH][2 NZ]
+  cd* Cd = reinterpret_cast<cd*>(smem_raw);                   // [MCH][2 NZ] FP64 coefficients
+  CoefHL* Cs = reinterpret_cast<CoefHL*>(Cd + MCH * 2 * NZ);  // [MCH][2 NZ] their (hi, lo) splits
+  float2* Rs = reinterpret_cast<float2*>(Cs + MCH * 2 * NZ);  // [MCH][2 NZ] folded AB2 term
+  __shared__ int s_mode[MCH];
   const int grp = blockIdx.x;
   const int gs = group_start[grp], ge = group_start[grp + 1];
   const int nev = sl.ne_v, nov = sl.no_v, new_ = sl.ne_w, now_ = sl.no_w;
@@ -144,17 +158,19 @@ __global__ void __launch_bounds__(MV_THREADS) k_inc_solve(cd* __restrict__ v, cd
   const float* Xg = incx + (size_t)grp * sl.stride;
   for (int base = gs; base < ge; base += MCH) {
     const int nm = min(MCH, ge - base);
+    if (threadIdx.x < nm) s_mode[threadIdx.x] = group_modes[base + threadIdx.x];
+    __syncthreads();
     for (int e = threadIdx.x; e < nm * 2 * NZ; e += blockDim.x) {
       const int q = e / (2 * NZ), i = e % (2 * NZ), f = i / NZ, k = i % NZ;
-      const long m = group_modes[base + q];
-      const cd x = (f == 0 ? v : g)[(size_t)k * modes + m];
+      const cd x = (f == 0 ? v : g)[(size_t)k * modes + s_mode[q]];
       const float hr = (float)x.re, hi = (float)x.im;
-      const int slot = f * NZ + ((k & 1) ? ne + k / 2 : k / 2);
-      Cs[q * 2 * NZ + slot] = CoefHL{hr, hi, (float)(x.re - (double)hr), (float)(x.im - (double)hi)};
+      const int slot = q * 2 * NZ + f * NZ + ((k & 1) ? ne + k / 2 : k / 2);
+      Cd[slot] = x;
+      Cs[slot] = CoefHL{hr, hi, (float)(x.re - (double)hr), (float)(x.im - (double)hi)};
     }
     for (int e = threadIdx.x; e < nm * 2 * ne; e += blockDim.x) {
       const int q = e / (2 * ne), i = e % (2 * ne), f = i / ne, r = i % ne;
-      const long m = group_modes[base + q];
+      const long m = s_mode[q];
       const cd* H = f == 0 ? rv : rg;   // N^n (GL values)
       const cd* Ho = f == 0 ? uh : wh;  // N^{n-1}
       const size_t ip = (size_t)r * modes + m, iq = (size_t)(N - r) * modes + m;
@@ -169,12 +185,12 @@ __global__ void __launch_bounds__(MV_THREADS) k_inc_solve(cd* __restrict__ v, cd
     }
     __syncthreads();
     for (int t = threadIdx.x; t < rows; t += blockDim.x) {
-      int b, row, n, r0;
+      int b, row, n;
       size_t boff;
-      if (t < nev) { b = 0; row = t; n = nev; r0 = 2; boff = bo.ve; }
-      else if (t < nev + nov) { b = 1; row = t - nev; n = nov; r0 = 2; boff = bo.vo; }
-      else if (t < nev + nov + new_) { b = 2; row = t - nev - nov; n = new_; r0 = 1; boff = bo.we; }
-      else { b = 3; row = t - nev - nov - new_; n = now_; r0 = 1; boff = bo.wo; }
+      if (t < nev) { b = 0; row = t; n = nev; boff = bo.ve; }
+      else if (t < nev + nov) { b = 1; row = t - nev; n = nov; boff = bo.vo; }
+      else if (t < nev + nov + new_) { b = 2; row = t - nev - nov; n = new_; boff = bo.we; }
+      else { b = 3; row = t - nev - nov - new_; n = now_; boff = bo.wo; }
       // offset of block b inside a mode's 2 NZ staged entries
       const int roff = b == 0 ? 0 : b == 1 ? nev : b == 2 ? NZ : NZ + new_;
       const float2* Mb = Mg + boff + row;
@@ -183,48 +199,44 @@ __global__ void __launch_bounds__(MV_THREADS) k_inc_solve(cd* __restrict__ v, cd
 #pragma unroll
       for (int q = 0; q < MCH; ++q)
         S[q][0] = S[q][1] = C[q][0] = C[q][1] = A[q][0] = A[q][1] = 0.f;
-      for (int c0 = 0; c0 < n; c0 += CB) {
-        float2 mm[CB];
+      // columns c < r0 of X meet the zero wall entries of the staged rhs
+      float2 ma[CB];
+      float xa[CB];
 #pragma unroll
-        for (int u = 0; u < CB; ++u) mm[u] = c0 + u < n ? __ldg(Mb + (size_t)(c0 + u) * n) : make_float2(0.f, 0.f);
+      for (int u = 0; u < CB; ++u) {
+        ma[u] = u < n ? __ldg(Mb + (size_t)u * n) : make_float2(0.f, 0.f);
+        xa[u] = u < n ? __ldg(Xb + (size_t)u * n) : 0.f;
+      }
+      for (int c0 = 0; c0 < n; c0 += CB) {
+        float2 mb[CB];
+        float xb[CB];
+#pragma unroll
+        for (int u = 0; u < CB; ++u) {
+          const int c = c0 + CB + u;
+          mb[u] = c < n ? __ldg(Mb + (size_t)c * n) : make_float2(0.f, 0.f);
+          xb[u] = c < n ? __ldg(Xb + (size_t)c * n) : 0.f;
+        }
 #pragma unroll
         for (int u = 0; u < CB; ++u) {
           if (c0 + u < n) {
 #pragma unroll
             for (int q = 0; q < MCH; ++q) {
               if (q < nm) {
-                const CoefHL cc = Cs[q * 2 * NZ + roff + c0 + u];
-                const float ch[2] = {cc.hr, cc.hi}, cl[2] = {cc.lr, cc.li};
-#pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                  const float p = __fmul_rn(mm[u].x, ch[k]);
-                  const float pe = __fmaf_rn(mm[u].x, ch[k], -p);
-                  const df32 sm = df_two_sum(S[q][k], p);
-                  S[q][k] = sm.hi;
-                  C[q][k] = __fadd_rn(C[q][k], __fadd_rn(__fadd_rn(sm.lo, pe),
-                                                         __fmaf_rn(mm[u].x, cl[k], __fmul_rn(mm[u].y, ch[k]))));
-                }
+                const int si = q * 2 * NZ + roff + c0 + u;
+                const CoefHL cc = Cs[si];
+                const float2 rr = Rs[si];
+                comp_mac(ma[u].x, ma[u].y, cc.hr, cc.lr, S[q][0], C[q][0]);
+                comp_mac(ma[u].x, ma[u].y, cc.hi, cc.li, S[q][1], C[q][1]);
+                A[q][0] = __fmaf_rn(xa[u], rr.x, A[q][0]);
+                A[q][1] = __fmaf_rn(xa[u], rr.y, A[q][1]);
               }
             }
           }
         }
-      }
-      for (int c0 = r0; c0 < n; c0 += CB) {
-        float xx[CB];
-#pragma unroll
-        for (int u = 0; u < CB; ++u) xx[u] = c0 + u < n ? __ldg(Xb + (size_t)(c0 + u) * n) : 0.f;
 #pragma unroll
         for (int u = 0; u < CB; ++u) {
-          if (c0 + u < n) {
-#pragma unroll
-            for (int q = 0; q < MCH; ++q) {
-              if (q < nm) {
-                const float2 rr = Rs[q * 2 * NZ + roff + c0 + u];
-                A[q][0] = __fmaf_rn(xx[u], rr.x, A[q][0]);
-                A[q][1] = __fmaf_rn(xx[u], rr.y, A[q][1]);
-              }
-            }
-          }
+          ma[u] = mb[u];
+          xa[u] = xb[u];
         }
       }
       const int j = (b == 0 || b == 2) ? 2 * row : 2 * row + 1;
@@ -232,11 +244,10 @@ __global__ void __launch_bounds__(MV_THREADS) k_inc_solve(cd* __restrict__ v, cd
 #pragma unroll
       for (int q = 0; q < MCH; ++q) {
         if (q < nm) {
-          const size_t idx = (size_t)j * modes + group_modes[base + q];
-          const cd c0 = dst[idx];
+          const cd c0 = Cd[q * 2 * NZ + roff + row];
           const double dr = (double)S[q][0] + ((double)C[q][0] + (double)A[q][0]);
           const double di = (double)S[q][1] + ((double)C[q][1] + (double)A[q][1]);
-          dst[idx] = cd{c0.re + dr, c0.im + di};
+          dst[(size_t)j * modes + s_mode[q]] = cd{c0.re + dr, c0.im + di};
         }
       }
     }
@@ -346,7 +357,11 @@ int launch_solve_mixed(Handle* h) {
   cudaStream_t st = h->stream;
   cudaEvent_t ev;
   if (h->nk2 > 0) {
-    const size_t smem = (sizeof(CoefHL) + sizeof(float2)) * MCH * 2 * (size_t)NZ;
+    const size_t smem = (sizeof(cd) + sizeof(CoefHL) + sizeof(float2)) * MCH * 2 * (size_t)NZ;
+    if (smem > 48 * 1024 &&
+        !cuda_ok(h, cudaFuncSetAttribute(k_inc_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                 "k_inc_solve smem"))
+      return CHF_E_CUDA;
     prof_begin(h, K_INC_SOLVE, &ev);
     k_inc_solve<<<h->nk2, MV_THREADS, smem, st>>>(h->f[F_V], h->f[F_OY], h->f[F_RV], h->f[F_U], h->f[F_RG],
                                                    h->f[F_W], h->incm, h->incx, h->sl, h->group_start,
