@@ -11,7 +11,8 @@
 //   k_tc_split_z2   the three Lamb components [MP][2 modes] -> digit images
 //   k_tc_gemm_z2    Chebyshev coefficients in FP64: L = W V, W = DCT-I weights
 //                   on the product grid, rows 0..N (truncation, REF:1686-1704)
-//   k_curl          dz of H1, H3 by FP64 recurrences (one thread per mode), h_v = k^2 H2 + i a D H1 + i b D H3,
+//   k_curl          h_v = k^2 H2 + D (i a H1 + i b H3) with one FP64 recurrence
+//                   per (mode, re/im) column,
 //                   h_g = i a H3 - i b H1 (REF:1502-1540), written as tile images
 //   k_tc_gemm_gl    Gauss-Lobatto values T0 h (REF:1573-1609) into the FP64
 //                   history buffers
@@ -27,120 +28,102 @@
 #include <vector>
 
 #include "chf_internal.h"
+#include "f64bits.cuh"
 #include "tc_dev.cuh"
 
 namespace chf {
 
 namespace {
 
-constexpr int CURL_THREADS = 128;  // modes per CTA in k_curl
+constexpr int CURL_THREADS = 32;  // (mode, re/im) columns per CTA in k_curl
 
-// One thread per mode, grid (ceil(modes / CURL_THREADS)).
+// One thread per (mode, re/im) column, grid (ceil(2 modes / CURL_THREADS)).
 // lc: 3 fields [NZ][ncols] FP64 (H1, H2, H3 coefficients from the exact z
-// transform); out: fixed-point digit images and column exponents for the GL
-// GEMM (k_tcgemm.cu layout), field 0 = h_v, field 1 = h_g (mode (0,0)
-// carries H1, H3).  FP64 up to h_v, h_g: h_v is a small remainder of
-// k^2 H2 + i a D H1 + i b D H3 (the gradient part of the Lamb vector
-// cancels), so FP32 derivatives would leave an error ~100x FP32 rounding in
-// it.  D H1, D H3 follow dz's backward recurrence (REF:570-599) in
-// registers.  Two descending passes: the first finds each column's largest
-// |value| (its power of two), the second rounds h_v, h_g to FP32 (a relative
-// error per coefficient) and writes their digits, 8 rows per 16-byte store.
-__device__ __forceinline__ void curl_at(const double* __restrict__ lc, long ncols, long m, int k, int NZ,
-                                        double a, double b, double k2, bool mean, double* dh1, double* dh3,
-                                        double* h1k1, double* h3k1, int N, float* out) {
-  const size_t base = (size_t)k * ncols + 2 * m;
-  const double2 H1 = *reinterpret_cast<const double2*>(lc + base);
-  const double2 H2 = *reinterpret_cast<const double2*>(lc + (size_t)NZ * ncols + base);
-  const double2 H3 = *reinterpret_cast<const double2*>(lc + (size_t)2 * NZ * ncols + base);
-  // dh*[0..1]: b_{k+1}, dh*[2..3]: b_{k+2} per component; h*k1: values at k+1
-  double d1[2], d3[2];
-#pragma unroll
-  for (int c = 0; c < 2; ++c) {
-    const double n1 = k == N ? 0.0 : dh1[2 + c] + 2.0 * (double)(k + 1) * h1k1[c];
-    const double n3 = k == N ? 0.0 : dh3[2 + c] + 2.0 * (double)(k + 1) * h3k1[c];
-    dh1[2 + c] = dh1[c];
-    dh1[c] = n1;
-    dh3[2 + c] = dh3[c];
-    dh3[c] = n3;
-    d1[c] = k == 0 ? 0.5 * n1 : n1;
-    d3[c] = k == 0 ? 0.5 * n3 : n3;
-  }
-  h1k1[0] = H1.x;
-  h1k1[1] = H1.y;
-  h3k1[0] = H3.x;
-  h3k1[1] = H3.y;
+// transform); hs: FP32 scratch [2][NZ][ncols]; out: fixed-point digit images
+// and column exponents for the GL GEMM (k_tcgemm.cu layout), field 0 = h_v,
+// field 1 = h_g (mode (0,0) carries H1, H3).  FP64 up to h_v, h_g: h_v is a
+// small remainder of k^2 H2 + D G with G = i a H1 + i b H3 (the gradient part
+// of the Lamb vector cancels), so FP32 derivatives would leave an error ~100x
+// FP32 rounding in it.  Only G is differentiated (dz's backward recurrence,
+// REF:570-599, in registers); multiplying by i folds into the signs of the
+// per-thread coefficients, the partner component is read directly.  Pass 1
+// (descending k, 6 FP64 operations per element) rounds h_v, h_g to FP32 by
+// integer operations into hs and finds the column maxima (their powers of
+// two); pass 2 writes the digits, 8 rows per 16-byte store.
+struct CurlRegs {
+  double dg1 = 0, dg2 = 0, gk1 = 0;  // D G at k+1, k+2; G at k+1
+  float mv = 0.f, mg = 0.f;          // column maxima of |h_v|, |h_g|
+};
+
+template <bool ZERO>
+__device__ __forceinline__ void curl_at(int k, bool top, long col, long ncols, int NZ, bool mean, double k2,
+                                        double sa, double sb, const double* __restrict__ lc,
+                                        float* __restrict__ hs, CurlRegs& R) {
+  const size_t base = (size_t)k * ncols;
+  const long pcol = col ^ 1;
+  const double h1p = lc[base + pcol], h3p = lc[(size_t)2 * NZ * ncols + base + pcol];
+  const double gk = fma(sa, h1p, sb * h3p);  // (i a H1 + i b H3) for this component
+  double dg = 0.0;
+  if (!top) dg = fma(bits::from_int(2u * (uint32_t)(k + 1)), R.gk1, R.dg2);
+  R.dg2 = R.dg1;
+  R.dg1 = dg;
+  R.gk1 = gk;
+  if (ZERO) dg *= 0.5;
+  float ov, og;
   if (mean) {
-    out[0] = (float)H1.x;
-    out[1] = (float)H1.y;
-    out[2] = (float)H3.x;
-    out[3] = (float)H3.y;
+    ov = bits::narrow(lc[base + col]);
+    og = bits::narrow(lc[(size_t)2 * NZ * ncols + base + col]);
   } else {
-    out[0] = (float)(k2 * H2.x - a * d1[1] - b * d3[1]);  // h_v = k2 H2 + i a D H1 + i b D H3
-    out[1] = (float)(k2 * H2.y + a * d1[0] + b * d3[0]);
-    out[2] = (float)(-a * H3.y + b * H1.y);                // h_g = i a H3 - i b H1
-    out[3] = (float)(a * H3.x - b * H1.x);
+    ov = bits::narrow(fma(k2, lc[(size_t)NZ * ncols + base + col], dg));  // h_v = k^2 H2 + D G
+    og = bits::narrow(fma(sa, h3p, -(sb * h1p)));                          // h_g = i a H3 - i b H1
   }
+  hs[base + col] = ov;
+  hs[(size_t)NZ * ncols + base + col] = og;
+  R.mv = fmaxf(R.mv, fabsf(ov));
+  R.mg = fmaxf(R.mg, fabsf(og));
 }
 
 __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict__ lc,
                                                        const double* __restrict__ iapha,
                                                        const double* __restrict__ ibeta, Dims d,
-                                                       const __grid_constant__ FxPlan plan,
+                                                       const __grid_constant__ FxPlan plan, float* __restrict__ hs,
                                                        uint8_t* __restrict__ bimg, int* __restrict__ bexp) {
   const long modes = d.modes(), ncols = 2 * modes;
-  const long m = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= modes) return;
+  const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncols) return;
+  const long m = col >> 1;
   const int N = d.N, NZ = d.NZ;
   const double a = iapha[m % d.KX], b = ibeta[m / d.KX], k2 = a * a + b * b;
+  const double s = (col & 1) ? 1.0 : -1.0;  // (i z)_re = -z_im, (i z)_im = z_re
+  const double sa = s * a, sb = s * b;
   const bool mean = (m == 0);
-  // pass 1: column maxima of h_v re, h_v im, h_g re, h_g im
-  float mx[4] = {0.f, 0.f, 0.f, 0.f};
-  {
-    double dh1[4] = {0, 0, 0, 0}, dh3[4] = {0, 0, 0, 0}, h1k1[2] = {0, 0}, h3k1[2] = {0, 0};
-    for (int k = N; k >= 0; --k) {
-      float o[4];
-      curl_at(lc, ncols, m, k, NZ, a, b, k2, mean, dh1, dh3, h1k1, h3k1, N, o);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) mx[q] = fmaxf(mx[q], fabsf(o[q]));
-    }
-  }
-  int e[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    e[q] = 0;
-    if (mx[q] > 0.f) (void)frexpf(mx[q], &e[q]);
-    bexp[(size_t)(q / 2) * plan.bexp_stride() + 2 * m + (q & 1)] = e[q];
-  }
-  // pass 2: digits, groups of 8 rows from the top (rows >= NZ are zero)
-  double dh1[4] = {0, 0, 0, 0}, dh3[4] = {0, 0, 0, 0}, h1k1[2] = {0, 0}, h3k1[2] = {0, 0};
-  for (int g = plan.kpad / 8 - 1; g >= 0; --g) {
-    float val[4][8];
-#pragma unroll
-    for (int q = 7; q >= 0; --q) {
-      const int k = 8 * g + q;
-      float o[4] = {0.f, 0.f, 0.f, 0.f};
-      if (k <= N) curl_at(lc, ncols, m, k, NZ, a, b, k2, mean, dh1, dh3, h1k1, h3k1, N, o);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) val[c][q] = o[c];
-    }
+  CurlRegs R;
+  for (int k = N; k >= 1; --k) curl_at<false>(k, k == N, col, ncols, NZ, mean, k2, sa, sb, lc, hs, R);
+  curl_at<true>(0, false, col, ncols, NZ, mean, k2, sa, sb, lc, hs, R);
+  int e[2] = {0, 0};
+  if (R.mv > 0.f) (void)frexpf(R.mv, &e[0]);
+  if (R.mg > 0.f) (void)frexpf(R.mg, &e[1]);
+  bexp[col] = e[0];
+  bexp[plan.bexp_stride() + col] = e[1];
+  // pass 2: digits, groups of 8 rows (rows >= NZ are zero)
+  const int nt = (int)(col / FX_NT), r = (int)(col % FX_NT);
+  for (int g = 0; g < plan.kpad / 8; ++g) {
     const int ch = (8 * g) / TC_KC, kl = 8 * g - ch * TC_KC;
     const uint32_t pbytes = (uint32_t)FX_NT * plan.kc[ch] * 2u;
+    const size_t off = ((size_t)(kl / 8) * (FX_NT / 8) + r / 8) * 128 + (r % 8) * 16;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const long col = 2 * m + (c & 1);
-      const int nt = (int)(col / FX_NT), r = (int)(col % FX_NT);
-      const size_t off = ((size_t)(kl / 8) * (FX_NT / 8) + r / 8) * 128 + (r % 8) * 16;
-      uint8_t* base = bimg + (size_t)(c / 2) * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes +
-                      plan.b_chunk_off[ch];
+    for (int f = 0; f < 2; ++f) {
       uint16_t hd[FX_PLANES][8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
+        const int k = 8 * g + q;
+        const float x = k <= N ? hs[(size_t)f * NZ * ncols + (size_t)k * ncols + col] : 0.f;
         float dg[FX_PLANES];
-        tc::fx_digits_f(val[c][q], e[c], dg);
+        tc::fx_digits_f(x, e[f], dg);
 #pragma unroll
         for (int i = 0; i < FX_PLANES; ++i) hd[i][q] = tc::bf16_bits(dg[i]);
       }
+      uint8_t* base = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes + plan.b_chunk_off[ch];
 #pragma unroll
       for (int pl = 0; pl < FX_PLANES; ++pl) {
         uint4 u4;
@@ -282,8 +265,10 @@ int launch_nonlinear_mixed(Handle* h) {
   {
     cudaEvent_t ev;
     prof_begin(h, K_CURL32, &ev);
-    k_curl<<<(unsigned)((modes + CURL_THREADS - 1) / CURL_THREADS), CURL_THREADS, 0, h->stream>>>(
-        h->lc64, h->iapha, h->ibeta, d, h->tgl, h->bimg, h->bexp);
+    // FP32 scratch for h_v, h_g: the product-grid buffer, free once the z2
+    // digits are formed (2 NZ <= 6 MP rows of modes complex values)
+    k_curl<<<(unsigned)((cols + CURL_THREADS - 1) / CURL_THREADS), CURL_THREADS, 0, h->stream>>>(
+        h->lc64, h->iapha, h->ibeta, d, h->tgl, reinterpret_cast<float*>(h->wz32), h->bimg, h->bexp);
     prof_end(h, K_CURL32, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_curl")) return CHF_E_CUDA;
   }

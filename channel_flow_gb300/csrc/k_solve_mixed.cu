@@ -17,7 +17,9 @@
 //                  (hi, lo) splits of M and c, about 2^-44 relative) + A^-1 r
 //                  (FP32), x = c + delta in FP64
 //   k_inc_recover  u, w, omega_x, omega_z from v and omega_y (getvelocityandvorticity,
-//                  REF:2347-2407), FP64, one thread per (mode, re/im)
+//                  REF:2347-2407), FP64 recurrences, one thread per (mode, re/im)
+// FP64 arithmetic and double <-> float conversions share GB300's narrow FP64
+// pipe, so the conversions here are integer operations (f64bits.cuh).
 // The (0,0) mode (REF:401-474) stays with k_solve (FP64, one CTA).
 #include <cuda_runtime.h>
 
@@ -25,28 +27,17 @@
 
 #include "chf_internal.h"
 #include "df32.cuh"
+#include "f64bits.cuh"
 
 namespace chf {
 
 namespace {
 
-constexpr int I_THREADS = 256;
 constexpr int MV_THREADS = 288;  // threads over the 2 NZ rows of one group's four blocks
 constexpr int MCH = 4;           // modes per pass in k_inc_solve
 
 // Chebyshev derivative recurrence (dz, REF:570-599), descending in k:
-//   b_k = b_{k+2} + 2 (k+1) a_{k+1}   (b_0 is halved by the caller)
-struct Rec {  // one recurrence: values at k+1 and k+2
-  double b1 = 0.0, b2 = 0.0;
-  __device__ __forceinline__ double step(double src_k1, int k, bool top) {
-    const double b = top ? 0.0 : b2 + 2.0 * (double)(k + 1) * src_k1;
-    b2 = b1;
-    b1 = b;
-    return b;
-  }
-};
-
-constexpr int TM = 16;  // modes per CTA in k_inc_recover
+//   b_k = b_{k+2} + 2 (k+1) a_{k+1}   (b_0 halved on output)
 
 // ---------------------------------------------------------------------------
 // Set-up of the increment operators, grid (nk2, 4 blocks): with X = A^-1 the
@@ -134,6 +125,86 @@ __device__ __forceinline__ void comp_mac(float mh, float ml, float ch, float cl,
   C = __fadd_rn(C, __fadd_rn(sm.lo, e));
 }
 
+// Rows of one pass of k_inc_solve for NM staged modes: thread t owns row t of
+// the four blocks (v even, v odd, omega even, omega odd).
+template <int NM>
+__device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g, const float2* __restrict__ Mg,
+                                         const float* __restrict__ Xg, const SolveLayout& sl,
+                                         const BlockOffsets& bo, int NZ, long modes, const cd* Cd,
+                                         const CoefHL* Cs, const float2* Rs, const int* s_mode) {
+  const int nev = sl.ne_v, nov = sl.no_v, new_ = sl.ne_w, now_ = sl.no_w;
+  const int rows = nev + nov + new_ + now_;
+  for (int t = threadIdx.x; t < rows; t += blockDim.x) {
+    int b, row, n;
+    size_t boff;
+    if (t < nev) { b = 0; row = t; n = nev; boff = bo.ve; }
+    else if (t < nev + nov) { b = 1; row = t - nev; n = nov; boff = bo.vo; }
+    else if (t < nev + nov + new_) { b = 2; row = t - nev - nov; n = new_; boff = bo.we; }
+    else { b = 3; row = t - nev - nov - new_; n = now_; boff = bo.wo; }
+    // offset of block b inside a mode's 2 NZ staged entries
+    const int roff = b == 0 ? 0 : b == 1 ? nev : b == 2 ? NZ : NZ + new_;
+    const float2* Mb = Mg + boff + row;
+    const float* Xb = Xg + boff + row;
+    float S[NM][2], C[NM][2], A[NM][2];
+#pragma unroll
+    for (int q = 0; q < NM; ++q) S[q][0] = S[q][1] = C[q][0] = C[q][1] = A[q][0] = A[q][1] = 0.f;
+    // columns c < r0 of X meet the zero wall entries of the staged rhs
+    float2 ma[CB];
+    float xa[CB];
+#pragma unroll
+    for (int u = 0; u < CB; ++u) {
+      ma[u] = u < n ? __ldg(Mb + (size_t)u * n) : make_float2(0.f, 0.f);
+      xa[u] = u < n ? __ldg(Xb + (size_t)u * n) : 0.f;
+    }
+    for (int c0 = 0; c0 < n; c0 += CB) {
+      float2 mb[CB];
+      float xb[CB];
+#pragma unroll
+      for (int u = 0; u < CB; ++u) {
+        const int c = c0 + CB + u;
+        mb[u] = c < n ? __ldg(Mb + (size_t)c * n) : make_float2(0.f, 0.f);
+        xb[u] = c < n ? __ldg(Xb + (size_t)c * n) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < CB; ++u) {
+        if (c0 + u < n) {
+#pragma unroll
+          for (int q = 0; q < NM; ++q) {
+            const int si = q * 2 * NZ + roff + c0 + u;
+            const CoefHL cc = Cs[si];
+            const float2 rr = Rs[si];
+            comp_mac(ma[u].x, ma[u].y, cc.hr, cc.lr, S[q][0], C[q][0]);
+            comp_mac(ma[u].x, ma[u].y, cc.hi, cc.li, S[q][1], C[q][1]);
+            A[q][0] = __fmaf_rn(xa[u], rr.x, A[q][0]);
+            A[q][1] = __fmaf_rn(xa[u], rr.y, A[q][1]);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < CB; ++u) {
+        ma[u] = mb[u];
+        xa[u] = xb[u];
+      }
+    }
+    const int j = (b == 0 || b == 2) ? 2 * row : 2 * row + 1;
+    cd* dst = b < 2 ? v : g;
+#pragma unroll
+    for (int q = 0; q < NM; ++q) {
+      const cd c0 = Cd[q * 2 * NZ + roff + row];
+      double x[2];
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        // delta = S + A + C as a double-float, then x = c + delta with two
+        // FP64 additions (the float -> double moves are integer operations)
+        const df32 t = df_two_sum(S[q][k], A[q][k]);
+        const df32 dd = df_fast_two_sum(t.hi, __fadd_rn(t.lo, C[q][k]));
+        x[k] = ((k == 0 ? c0.re : c0.im) + bits::widen(dd.hi)) + bits::widen(dd.lo);
+      }
+      dst[(size_t)j * modes + s_mode[q]] = cd{x[0], x[1]};
+    }
+  }
+}
+
 __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v, cd* __restrict__ g,
                                                              const cd* __restrict__ rv, const cd* __restrict__ uh,
                                                              const cd* __restrict__ rg, const cd* __restrict__ wh,
@@ -141,7 +212,7 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
                                                              const float* __restrict__ incx, SolveLayout sl,
                                                              const int* __restrict__ group_start,
                                                              const int* __restrict__ group_modes, Dims d,
-                                                             double c3, double c1) {
+                                                             float c3, float c1) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = d.N, NZ = d.NZ, ne = N / 2 + 1;
   const long modes = d.modes();
@@ -151,8 +222,6 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
   __shared__ int s_mode[MCH];
   const int grp = blockIdx.x;
   const int gs = group_start[grp], ge = group_start[grp + 1];
-  const int nev = sl.ne_v, nov = sl.no_v, new_ = sl.ne_w, now_ = sl.no_w;
-  const int rows = nev + nov + new_ + now_;
   const BlockOffsets bo = block_offsets(sl);
   const float2* Mg = incm + (size_t)grp * sl.stride;
   const float* Xg = incx + (size_t)grp * sl.stride;
@@ -163,11 +232,14 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
     for (int e = threadIdx.x; e < nm * 2 * NZ; e += blockDim.x) {
       const int q = e / (2 * NZ), i = e % (2 * NZ), f = i / NZ, k = i % NZ;
       const cd x = (f == 0 ? v : g)[(size_t)k * modes + s_mode[q]];
-      const float hr = (float)x.re, hi = (float)x.im;
       const int slot = q * 2 * NZ + f * NZ + ((k & 1) ? ne + k / 2 : k / 2);
       Cd[slot] = x;
-      Cs[slot] = CoefHL{hr, hi, (float)(x.re - (double)hr), (float)(x.im - (double)hi)};
+      CoefHL h;
+      bits::split(x.re, h.hr, h.lr);
+      bits::split(x.im, h.hi, h.li);
+      Cs[slot] = h;
     }
+    // the AB2 term in FP32 (X r is an FP32 product of an O(dt) term)
     for (int e = threadIdx.x; e < nm * 2 * ne; e += blockDim.x) {
       const int q = e / (2 * ne), i = e % (2 * ne), f = i / ne, r = i % ne;
       const long m = s_mode[q];
@@ -175,155 +247,118 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
       const cd* Ho = f == 0 ? uh : wh;  // N^{n-1}
       const size_t ip = (size_t)r * modes + m, iq = (size_t)(N - r) * modes + m;
       const cd hp = H[ip], hq = H[iq], op = Ho[ip], oq = Ho[iq];
-      const double pr = c3 * hp.re - c1 * op.re, pi = c3 * hp.im - c1 * op.im;
-      const double qr = c3 * hq.re - c1 * oq.re, qi = c3 * hq.im - c1 * oq.im;
+      const float pr = c3 * bits::narrow(hp.re) - c1 * bits::narrow(op.re);
+      const float pi = c3 * bits::narrow(hp.im) - c1 * bits::narrow(op.im);
+      const float qr = c3 * bits::narrow(hq.re) - c1 * bits::narrow(oq.re);
+      const float qi = c3 * bits::narrow(hq.im) - c1 * bits::narrow(oq.im);
       const bool wall = (f == 0) ? (r < 2) : (r < 1);
       float2* out = Rs + q * 2 * NZ + f * NZ;
-      out[r] = wall ? make_float2(0.f, 0.f) : make_float2((float)(0.5 * (pr + qr)), (float)(0.5 * (pi + qi)));
-      if (r < N / 2)
-        out[ne + r] = wall ? make_float2(0.f, 0.f) : make_float2((float)(0.5 * (pr - qr)), (float)(0.5 * (pi - qi)));
+      out[r] = wall ? make_float2(0.f, 0.f) : make_float2(0.5f * (pr + qr), 0.5f * (pi + qi));
+      if (r < N / 2) out[ne + r] = wall ? make_float2(0.f, 0.f) : make_float2(0.5f * (pr - qr), 0.5f * (pi - qi));
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < rows; t += blockDim.x) {
-      int b, row, n;
-      size_t boff;
-      if (t < nev) { b = 0; row = t; n = nev; boff = bo.ve; }
-      else if (t < nev + nov) { b = 1; row = t - nev; n = nov; boff = bo.vo; }
-      else if (t < nev + nov + new_) { b = 2; row = t - nev - nov; n = new_; boff = bo.we; }
-      else { b = 3; row = t - nev - nov - new_; n = now_; boff = bo.wo; }
-      // offset of block b inside a mode's 2 NZ staged entries
-      const int roff = b == 0 ? 0 : b == 1 ? nev : b == 2 ? NZ : NZ + new_;
-      const float2* Mb = Mg + boff + row;
-      const float* Xb = Xg + boff + row;
-      float S[MCH][2], C[MCH][2], A[MCH][2];
-#pragma unroll
-      for (int q = 0; q < MCH; ++q)
-        S[q][0] = S[q][1] = C[q][0] = C[q][1] = A[q][0] = A[q][1] = 0.f;
-      // columns c < r0 of X meet the zero wall entries of the staged rhs
-      float2 ma[CB];
-      float xa[CB];
-#pragma unroll
-      for (int u = 0; u < CB; ++u) {
-        ma[u] = u < n ? __ldg(Mb + (size_t)u * n) : make_float2(0.f, 0.f);
-        xa[u] = u < n ? __ldg(Xb + (size_t)u * n) : 0.f;
-      }
-      for (int c0 = 0; c0 < n; c0 += CB) {
-        float2 mb[CB];
-        float xb[CB];
-#pragma unroll
-        for (int u = 0; u < CB; ++u) {
-          const int c = c0 + CB + u;
-          mb[u] = c < n ? __ldg(Mb + (size_t)c * n) : make_float2(0.f, 0.f);
-          xb[u] = c < n ? __ldg(Xb + (size_t)c * n) : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < CB; ++u) {
-          if (c0 + u < n) {
-#pragma unroll
-            for (int q = 0; q < MCH; ++q) {
-              if (q < nm) {
-                const int si = q * 2 * NZ + roff + c0 + u;
-                const CoefHL cc = Cs[si];
-                const float2 rr = Rs[si];
-                comp_mac(ma[u].x, ma[u].y, cc.hr, cc.lr, S[q][0], C[q][0]);
-                comp_mac(ma[u].x, ma[u].y, cc.hi, cc.li, S[q][1], C[q][1]);
-                A[q][0] = __fmaf_rn(xa[u], rr.x, A[q][0]);
-                A[q][1] = __fmaf_rn(xa[u], rr.y, A[q][1]);
-              }
-            }
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < CB; ++u) {
-          ma[u] = mb[u];
-          xa[u] = xb[u];
-        }
-      }
-      const int j = (b == 0 || b == 2) ? 2 * row : 2 * row + 1;
-      cd* dst = b < 2 ? v : g;
-#pragma unroll
-      for (int q = 0; q < MCH; ++q) {
-        if (q < nm) {
-          const cd c0 = Cd[q * 2 * NZ + roff + row];
-          const double dr = (double)S[q][0] + ((double)C[q][0] + (double)A[q][0]);
-          const double di = (double)S[q][1] + ((double)C[q][1] + (double)A[q][1]);
-          dst[(size_t)j * modes + s_mode[q]] = cd{c0.re + dr, c0.im + di};
-        }
-      }
+    switch (nm) {
+      case 1: inc_rows<1>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode); break;
+      case 2: inc_rows<2>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode); break;
+      case 3: inc_rows<3>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode); break;
+      default: inc_rows<4>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode); break;
     }
     __syncthreads();
   }
 }
 
 // ---------------------------------------------------------------------------
-// k_inc_recover: grid (ceil(modes / TM)); tiles of v and omega_y in shared
-// memory, one thread per (mode, re/im) running one descending pass (the
-// derivative recurrence), the other component from its partner lane:
-//   Dv_k -> u_k = (i a Dv - i b g) / k^2, w_k = (i b Dv + i a g) / k^2
-//   Du_k, Dw_k (from u, w at k+1) -> omega_z = -Du + i a v, omega_x = Dw - i b v
-// for every solved mode (not (0,0), not the spanwise Nyquist slot).
+// k_inc_recover: one thread per (mode, re/im) column, grid
+// (ceil(2 modes / RC_THREADS)); u, w, omega_x, omega_z from v and omega_y
+// (getvelocityandvorticity, REF:2347-2407) for every solved mode (not (0,0),
+// not the spanwise Nyquist slot):
+//   u = (i a Dv - i b g) / k^2,            w = (i b Dv + i a g) / k^2,
+//   omega_z = -Du + i a v = (i b Dg - i a D^2 v) / k^2 + i a v,
+//   omega_x =  Dw - i b v = (i b D^2 v + i a Dg) / k^2 - i b v.
+// One descending pass carries Dv, D^2 v and Dg of the thread's component in
+// FP64 registers (the dz recurrence, b_0 halved on output); the partner
+// component comes by shuffle, and multiplying by i folds into the signs of
+// the per-thread coefficients.  13 FP64 operations per element; the
+// recurrence factors 2 (k + 1) are built by integer operations.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(I_THREADS) k_inc_recover(const cd* __restrict__ v, const cd* __restrict__ g,
-                                                           cd* __restrict__ u, cd* __restrict__ w,
-                                                           cd* __restrict__ ox, cd* __restrict__ oz,
-                                                           const double* __restrict__ iapha,
-                                                           const double* __restrict__ ibeta, Dims d) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int N = d.N, NZ = d.NZ, C2 = 2 * TM;
-  const long modes = d.modes();
-  double* V = reinterpret_cast<double*>(smem_raw);  // [NZ][C2]
-  double* G = V + (size_t)NZ * C2;                  // [NZ][C2]
-  const long m0 = (long)blockIdx.x * TM;
-  for (int t = threadIdx.x; t < NZ * C2; t += blockDim.x) {
-    const int c = t % C2, n = t / C2;
-    const long col = 2 * m0 + c;
-    const bool in = col < 2 * modes;
-    V[t] = in ? reinterpret_cast<const double*>(v)[(size_t)n * 2 * modes + col] : 0.0;
-    G[t] = in ? reinterpret_cast<const double*>(g)[(size_t)n * 2 * modes + col] : 0.0;
+constexpr int RC_THREADS = 64;
+
+struct RecoverRegs {
+  double dv1 = 0, dv2 = 0, d2v1 = 0, d2v2 = 0, dg1 = 0, dg2 = 0, vk1 = 0, gk1 = 0;
+};
+
+template <bool ZERO>
+__device__ __forceinline__ void recover_at(int k, bool top, long col, long ncols, bool in, bool live,
+                                           const double* __restrict__ vd, const double* __restrict__ gd,
+                                           double* __restrict__ ud, double* __restrict__ wd,
+                                           double* __restrict__ oxd, double* __restrict__ ozd, double sak,
+                                           double sbk, double sa, double sb, RecoverRegs& R) {
+  const size_t idx = (size_t)k * ncols + col;
+  const double vk = in ? vd[idx] : 0.0, gk = in ? gd[idx] : 0.0;
+  double dv = 0.0, d2v = 0.0, dg = 0.0;
+  if (!top) {
+    const double tk = bits::from_int(2u * (uint32_t)(k + 1));
+    dv = fma(tk, R.vk1, R.dv2);
+    d2v = fma(tk, R.dv1, R.d2v2);
+    dg = fma(tk, R.gk1, R.dg2);
   }
-  __syncthreads();
-  if (threadIdx.x >= C2) return;  // one warp: lanes 2l (re) and 2l+1 (im) of mode m0 + l
-  const int c = threadIdx.x, comp = c & 1;
-  const long m = m0 + c / 2;
-  const bool live = m > 0 && m < modes && (m / d.KX) != d.NYQ;
-  double a = 0.0, b = 0.0, ik2 = 0.0;
+  R.dv2 = R.dv1;
+  R.dv1 = dv;
+  R.d2v2 = R.d2v1;
+  R.d2v1 = d2v;
+  R.dg2 = R.dg1;
+  R.dg1 = dg;
+  R.vk1 = vk;
+  R.gk1 = gk;
+  if (ZERO) {  // the k = 0 outputs of dz are halved
+    dv *= 0.5;
+    d2v *= 0.5;
+    dg *= 0.5;
+  }
+  const double dv_p = __shfl_xor_sync(0xffffffffu, dv, 1);
+  const double d2v_p = __shfl_xor_sync(0xffffffffu, d2v, 1);
+  const double dg_p = __shfl_xor_sync(0xffffffffu, dg, 1);
+  const double v_p = __shfl_xor_sync(0xffffffffu, vk, 1);
+  const double g_p = __shfl_xor_sync(0xffffffffu, gk, 1);
   if (live) {
-    a = iapha[m % d.KX];
-    b = ibeta[m / d.KX];
-    ik2 = 1.0 / (a * a + b * b);
+    ud[idx] = fma(sak, dv_p, -(sbk * g_p));
+    wd[idx] = fma(sbk, dv_p, sak * g_p);
+    ozd[idx] = fma(sbk, dg_p, fma(-sak, d2v_p, sa * v_p));
+    oxd[idx] = fma(sbk, d2v_p, fma(sak, dg_p, -(sb * v_p)));
   }
-  const double s = comp ? 1.0 : -1.0;  // multiplying by i: re <- -im, im <- +re
-  Rec rv, ru, rw;
-  double vk1 = 0.0, uk1 = 0.0, wk1 = 0.0;
+}
+
+__global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict__ v, const cd* __restrict__ g,
+                                                            cd* __restrict__ u, cd* __restrict__ w,
+                                                            cd* __restrict__ ox, cd* __restrict__ oz,
+                                                            const double* __restrict__ iapha,
+                                                            const double* __restrict__ ibeta, Dims d) {
+  const long modes = d.modes(), ncols = 2 * modes;
+  const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in = col < ncols;  // every lane takes part in the shuffles
+  const long m = in ? col >> 1 : 0;
+  const bool live = in && m > 0 && (m / d.KX) != d.NYQ;
+  double sak = 0.0, sbk = 0.0, sa = 0.0, sb = 0.0;
+  if (live) {
+    // (i z)_re = -z_im, (i z)_im = z_re: the sign s of the partner term
+    const double s = (col & 1) ? 1.0 : -1.0;
+    const double a = iapha[m % d.KX], b = ibeta[m / d.KX], ik2 = 1.0 / (a * a + b * b);
+    sa = s * a;
+    sb = s * b;
+    sak = sa * ik2;
+    sbk = sb * ik2;
+  }
+  const double* vd = reinterpret_cast<const double*>(v);
+  const double* gd = reinterpret_cast<const double*>(g);
   double* ud = reinterpret_cast<double*>(u);
   double* wd = reinterpret_cast<double*>(w);
   double* oxd = reinterpret_cast<double*>(ox);
   double* ozd = reinterpret_cast<double*>(oz);
-  for (int k = N; k >= 0; --k) {
-    const bool top = (k == N);
-    const double vk = V[k * C2 + c], gk = G[k * C2 + c];
-    const double h = k == 0 ? 0.5 : 1.0;
-    const double dv = h * rv.step(vk1, k, top);
-    const double du = h * ru.step(uk1, k, top);
-    const double dw = h * rw.step(wk1, k, top);
-    // partner components (the other of re / im of the same mode)
-    const double dv_p = __shfl_xor_sync(0xffffffffu, dv, 1);
-    const double g_p = __shfl_xor_sync(0xffffffffu, gk, 1);
-    const double v_p = __shfl_xor_sync(0xffffffffu, vk, 1);
-    // u = (i a Dv - i b g) / k^2, w = (i b Dv + i a g) / k^2: i x -> s x_partner
-    const double uk = s * (a * dv_p - b * g_p) * ik2;
-    const double wk = s * (b * dv_p + a * g_p) * ik2;
-    if (live) {
-      const size_t idx = ((size_t)k * modes + m) * 2 + comp;
-      ud[idx] = uk;
-      wd[idx] = wk;
-      ozd[idx] = -du + s * a * v_p;  // omega_z = -Du + i a v
-      oxd[idx] = dw - s * b * v_p;   // omega_x = Dw - i b v
-    }
-    vk1 = vk;
-    uk1 = uk;
-    wk1 = wk;
-  }
+  RecoverRegs R;
+  const int N = d.N;
+  for (int k = N; k >= 1; --k)
+    recover_at<false>(k, k == N, col, ncols, in, live, vd, gd, ud, wd, oxd, ozd, sak, sbk, sa, sb, R);
+  recover_at<true>(0, false, col, ncols, in, live, vd, gd, ud, wd, oxd, ozd, sak, sbk, sa, sb, R);
 }
 
 }  // namespace
@@ -365,17 +400,12 @@ int launch_solve_mixed(Handle* h) {
     prof_begin(h, K_INC_SOLVE, &ev);
     k_inc_solve<<<h->nk2, MV_THREADS, smem, st>>>(h->f[F_V], h->f[F_OY], h->f[F_RV], h->f[F_U], h->f[F_RG],
                                                    h->f[F_W], h->incm, h->incx, h->sl, h->group_start,
-                                                   h->group_modes, d, 1.5 * dt, 0.5 * dt);
+                                                   h->group_modes, d, (float)(1.5 * dt), (float)(0.5 * dt));
     prof_end(h, K_INC_SOLVE, ev);
   }
   {
     prof_begin(h, K_INC_RECOVER, &ev);
-    const size_t smem = sizeof(double) * 2 * (size_t)NZ * 2 * TM;
-    if (smem > 48 * 1024 &&
-        !cuda_ok(h, cudaFuncSetAttribute(k_inc_recover, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                 "k_inc_recover smem"))
-      return CHF_E_CUDA;
-    k_inc_recover<<<(unsigned)((modes + TM - 1) / TM), I_THREADS, smem, st>>>(
+    k_inc_recover<<<(unsigned)((2 * modes + RC_THREADS - 1) / RC_THREADS), RC_THREADS, 0, st>>>(
         h->f[F_V], h->f[F_OY], h->f[F_U], h->f[F_W], h->f[F_OX], h->f[F_OZ], h->iapha, h->ibeta, d);
     prof_end(h, K_INC_RECOVER, ev);
   }
