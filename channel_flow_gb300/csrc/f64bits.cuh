@@ -113,6 +113,13 @@ __host__ __device__ __forceinline__ double widen(float f) {
   return u2d(sign | (ed << 52) | ((uint64_t)(v & 0x7fffffu) << 29));
 }
 
+// x / 2 by decrementing the exponent (exact for |x| >= 2^-1021; smaller
+// magnitudes give signed zero)
+__host__ __device__ __forceinline__ double half(double x) {
+  const uint64_t u = d2u(x);
+  return ((u >> 52) & 0x7ff) > 1 ? u2d(u - (1ull << 52)) : u2d(u & 0x8000000000000000ull);
+}
+
 // the binary64 of an integer 1 <= n < 2^31 (exact)
 __host__ __device__ __forceinline__ double from_int(uint32_t n) {
 #ifdef __CUDA_ARCH__

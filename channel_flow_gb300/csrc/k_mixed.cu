@@ -47,41 +47,11 @@ constexpr int CURL_THREADS = 32;  // (mode, re/im) columns per CTA in k_curl
 // FP32 rounding in it.  Only G is differentiated (dz's backward recurrence,
 // REF:570-599, in registers); multiplying by i folds into the signs of the
 // per-thread coefficients, the partner component is read directly.  Pass 1
-// (descending k, 6 FP64 operations per element) rounds h_v, h_g to FP32 by
-// integer operations into hs and finds the column maxima (their powers of
-// two); pass 2 writes the digits, 8 rows per 16-byte store.
-struct CurlRegs {
-  double dg1 = 0, dg2 = 0, gk1 = 0;  // D G at k+1, k+2; G at k+1
-  float mv = 0.f, mg = 0.f;          // column maxima of |h_v|, |h_g|
-};
-
-template <bool ZERO>
-__device__ __forceinline__ void curl_at(int k, bool top, long col, long ncols, int NZ, bool mean, double k2,
-                                        double sa, double sb, const double* __restrict__ lc,
-                                        float* __restrict__ hs, CurlRegs& R) {
-  const size_t base = (size_t)k * ncols;
-  const long pcol = col ^ 1;
-  const double h1p = lc[base + pcol], h3p = lc[(size_t)2 * NZ * ncols + base + pcol];
-  const double gk = fma(sa, h1p, sb * h3p);  // (i a H1 + i b H3) for this component
-  double dg = 0.0;
-  if (!top) dg = fma(bits::from_int(2u * (uint32_t)(k + 1)), R.gk1, R.dg2);
-  R.dg2 = R.dg1;
-  R.dg1 = dg;
-  R.gk1 = gk;
-  if (ZERO) dg *= 0.5;
-  float ov, og;
-  if (mean) {
-    ov = bits::narrow(lc[base + col]);
-    og = bits::narrow(lc[(size_t)2 * NZ * ncols + base + col]);
-  } else {
-    ov = bits::narrow(fma(k2, lc[(size_t)NZ * ncols + base + col], dg));  // h_v = k^2 H2 + D G
-    og = bits::narrow(fma(sa, h3p, -(sb * h1p)));                          // h_g = i a H3 - i b H1
-  }
-  hs[base + col] = ov;
-  hs[(size_t)NZ * ncols + base + col] = og;
-  R.mv = fmaxf(R.mv, fabsf(ov));
-  R.mg = fmaxf(R.mg, fabsf(og));
-}
+// (descending k, 6 FP64 operations per element, CURL_PF rows of H loaded
+// ahead) rounds h_v, h_g to FP32 by integer operations into hs and finds the
+// column maxima (their powers of two); pass 2 writes the digits, 8 rows per
+// 16-byte store.
+constexpr int CURL_PF = 8;  // rows of H loaded ahead of the recurrence
 
 __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict__ lc,
                                                        const double* __restrict__ iapha,
@@ -97,12 +67,50 @@ __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict_
   const double s = (col & 1) ? 1.0 : -1.0;  // (i z)_re = -z_im, (i z)_im = z_re
   const double sa = s * a, sb = s * b;
   const bool mean = (m == 0);
-  CurlRegs R;
-  for (int k = N; k >= 1; --k) curl_at<false>(k, k == N, col, ncols, NZ, mean, k2, sa, sb, lc, hs, R);
-  curl_at<true>(0, false, col, ncols, NZ, mean, k2, sa, sb, lc, hs, R);
+  // the mean column reads its own H1, H3 and passes them through
+  const long pcol = mean ? col : (col ^ 1);
+  const double* H1 = lc;
+  const double* H2 = lc + (size_t)NZ * ncols;
+  const double* H3 = lc + (size_t)2 * NZ * ncols;
+  double dg1 = 0.0, dg2 = 0.0, gk1 = 0.0;  // D G at k+1, k+2; G at k+1
+  float mv = 0.f, mg = 0.f;                // column maxima of |h_v|, |h_g|
+  for (int k0 = N; k0 >= 0; k0 -= CURL_PF) {
+    double h1[CURL_PF], h2[CURL_PF], h3[CURL_PF];
+#pragma unroll
+    for (int i = 0; i < CURL_PF; ++i) {
+      const size_t base = (size_t)max(k0 - i, 0) * ncols;
+      h1[i] = H1[base + pcol];
+      h2[i] = H2[base + col];
+      h3[i] = H3[base + pcol];
+    }
+#pragma unroll
+    for (int i = 0; i < CURL_PF; ++i) {
+      const int k = k0 - i;
+      if (k < 0) break;
+      const double gk = fma(sa, h1[i], sb * h3[i]);  // (i a H1 + i b H3) for this component
+      double dg = k == N ? 0.0 : fma(bits::from_int(2u * (uint32_t)(k + 1)), gk1, dg2);
+      dg2 = dg1;
+      dg1 = dg;
+      gk1 = gk;
+      if (k == 0) dg = bits::half(dg);  // dz halves b_0
+      float ov, og;
+      if (mean) {
+        ov = bits::narrow(h1[i]);
+        og = bits::narrow(h3[i]);
+      } else {
+        ov = bits::narrow(fma(k2, h2[i], dg));           // h_v = k^2 H2 + D G
+        og = bits::narrow(fma(sa, h3[i], -(sb * h1[i])));  // h_g = i a H3 - i b H1
+      }
+      const size_t base = (size_t)k * ncols;
+      hs[base + col] = ov;
+      hs[(size_t)NZ * ncols + base + col] = og;
+      mv = fmaxf(mv, fabsf(ov));
+      mg = fmaxf(mg, fabsf(og));
+    }
+  }
   int e[2] = {0, 0};
-  if (R.mv > 0.f) (void)frexpf(R.mv, &e[0]);
-  if (R.mg > 0.f) (void)frexpf(R.mg, &e[1]);
+  if (mv > 0.f) (void)frexpf(mv, &e[0]);
+  if (mg > 0.f) (void)frexpf(mg, &e[1]);
   bexp[col] = e[0];
   bexp[plan.bexp_stride() + col] = e[1];
   // pass 2: digits, groups of 8 rows (rows >= NZ are zero)

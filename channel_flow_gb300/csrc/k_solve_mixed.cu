@@ -276,57 +276,14 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
 //   omega_z = -Du + i a v = (i b Dg - i a D^2 v) / k^2 + i a v,
 //   omega_x =  Dw - i b v = (i b D^2 v + i a Dg) / k^2 - i b v.
 // One descending pass carries Dv, D^2 v and Dg of the thread's component in
-// FP64 registers (the dz recurrence, b_0 halved on output); the partner
+// FP64 registers (the dz recurrence, b_0 halved on output), RC_PF rows of
+// v and omega_y loaded ahead; the partner
 // component comes by shuffle, and multiplying by i folds into the signs of
 // the per-thread coefficients.  13 FP64 operations per element; the
 // recurrence factors 2 (k + 1) are built by integer operations.
 // ---------------------------------------------------------------------------
 constexpr int RC_THREADS = 64;
-
-struct RecoverRegs {
-  double dv1 = 0, dv2 = 0, d2v1 = 0, d2v2 = 0, dg1 = 0, dg2 = 0, vk1 = 0, gk1 = 0;
-};
-
-template <bool ZERO>
-__device__ __forceinline__ void recover_at(int k, bool top, long col, long ncols, bool in, bool live,
-                                           const double* __restrict__ vd, const double* __restrict__ gd,
-                                           double* __restrict__ ud, double* __restrict__ wd,
-                                           double* __restrict__ oxd, double* __restrict__ ozd, double sak,
-                                           double sbk, double sa, double sb, RecoverRegs& R) {
-  const size_t idx = (size_t)k * ncols + col;
-  const double vk = in ? vd[idx] : 0.0, gk = in ? gd[idx] : 0.0;
-  double dv = 0.0, d2v = 0.0, dg = 0.0;
-  if (!top) {
-    const double tk = bits::from_int(2u * (uint32_t)(k + 1));
-    dv = fma(tk, R.vk1, R.dv2);
-    d2v = fma(tk, R.dv1, R.d2v2);
-    dg = fma(tk, R.gk1, R.dg2);
-  }
-  R.dv2 = R.dv1;
-  R.dv1 = dv;
-  R.d2v2 = R.d2v1;
-  R.d2v1 = d2v;
-  R.dg2 = R.dg1;
-  R.dg1 = dg;
-  R.vk1 = vk;
-  R.gk1 = gk;
-  if (ZERO) {  // the k = 0 outputs of dz are halved
-    dv *= 0.5;
-    d2v *= 0.5;
-    dg *= 0.5;
-  }
-  const double dv_p = __shfl_xor_sync(0xffffffffu, dv, 1);
-  const double d2v_p = __shfl_xor_sync(0xffffffffu, d2v, 1);
-  const double dg_p = __shfl_xor_sync(0xffffffffu, dg, 1);
-  const double v_p = __shfl_xor_sync(0xffffffffu, vk, 1);
-  const double g_p = __shfl_xor_sync(0xffffffffu, gk, 1);
-  if (live) {
-    ud[idx] = fma(sak, dv_p, -(sbk * g_p));
-    wd[idx] = fma(sbk, dv_p, sak * g_p);
-    ozd[idx] = fma(sbk, dg_p, fma(-sak, d2v_p, sa * v_p));
-    oxd[idx] = fma(sbk, d2v_p, fma(sak, dg_p, -(sb * v_p)));
-  }
-}
+constexpr int RC_PF = 8;  // rows of v, omega_y loaded ahead of the recurrences
 
 __global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict__ v, const cd* __restrict__ g,
                                                             cd* __restrict__ u, cd* __restrict__ w,
@@ -336,7 +293,8 @@ __global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict
   const long modes = d.modes(), ncols = 2 * modes;
   const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool in = col < ncols;  // every lane takes part in the shuffles
-  const long m = in ? col >> 1 : 0;
+  const long cl = in ? col : 0;
+  const long m = cl >> 1;
   const bool live = in && m > 0 && (m / d.KX) != d.NYQ;
   double sak = 0.0, sbk = 0.0, sa = 0.0, sb = 0.0;
   if (live) {
@@ -354,11 +312,55 @@ __global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict
   double* wd = reinterpret_cast<double*>(w);
   double* oxd = reinterpret_cast<double*>(ox);
   double* ozd = reinterpret_cast<double*>(oz);
-  RecoverRegs R;
   const int N = d.N;
-  for (int k = N; k >= 1; --k)
-    recover_at<false>(k, k == N, col, ncols, in, live, vd, gd, ud, wd, oxd, ozd, sak, sbk, sa, sb, R);
-  recover_at<true>(0, false, col, ncols, in, live, vd, gd, ud, wd, oxd, ozd, sak, sbk, sa, sb, R);
+  // Dv, D^2 v, Dg at k+1 and k+2; v, omega_y at k+1
+  double dv1 = 0, dv2 = 0, d2v1 = 0, d2v2 = 0, dg1 = 0, dg2 = 0, vk1 = 0, gk1 = 0;
+  for (int k0 = N; k0 >= 0; k0 -= RC_PF) {
+    double vp[RC_PF], gp[RC_PF];
+#pragma unroll
+    for (int i = 0; i < RC_PF; ++i) {
+      const size_t idx = (size_t)max(k0 - i, 0) * ncols + cl;
+      vp[i] = vd[idx];
+      gp[i] = gd[idx];
+    }
+#pragma unroll
+    for (int i = 0; i < RC_PF; ++i) {
+      const int k = k0 - i;
+      if (k < 0) break;
+      double dv = 0.0, d2v = 0.0, dg = 0.0;
+      if (k < N) {
+        const double tk = bits::from_int(2u * (uint32_t)(k + 1));
+        dv = fma(tk, vk1, dv2);
+        d2v = fma(tk, dv1, d2v2);
+        dg = fma(tk, gk1, dg2);
+      }
+      dv2 = dv1;
+      dv1 = dv;
+      d2v2 = d2v1;
+      d2v1 = d2v;
+      dg2 = dg1;
+      dg1 = dg;
+      vk1 = vp[i];
+      gk1 = gp[i];
+      if (k == 0) {  // the k = 0 outputs of dz are halved
+        dv = bits::half(dv);
+        d2v = bits::half(d2v);
+        dg = bits::half(dg);
+      }
+      const double dv_p = __shfl_xor_sync(0xffffffffu, dv, 1);
+      const double d2v_p = __shfl_xor_sync(0xffffffffu, d2v, 1);
+      const double dg_p = __shfl_xor_sync(0xffffffffu, dg, 1);
+      const double v_p = __shfl_xor_sync(0xffffffffu, vp[i], 1);
+      const double g_p = __shfl_xor_sync(0xffffffffu, gp[i], 1);
+      if (live) {
+        const size_t idx = (size_t)k * ncols + col;
+        ud[idx] = fma(sak, dv_p, -(sbk * g_p));
+        wd[idx] = fma(sbk, dv_p, sak * g_p);
+        ozd[idx] = fma(sbk, dg_p, fma(-sak, d2v_p, sa * v_p));
+        oxd[idx] = fma(sbk, d2v_p, fma(sak, dg_p, -(sb * v_p)));
+      }
+    }
+  }
 }
 
 }  // namespace

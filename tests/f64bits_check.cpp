@@ -53,6 +53,8 @@ int main() {
   if (narrow(up) != 2.0f) return fail("carry", up, narrow(up), 2.0);
   const double tiny = std::ldexp(1.0, -126);
   if (narrow(tiny) != static_cast<float>(tiny)) return fail("min normal", tiny, narrow(tiny), tiny);
+  for (double x : {1.0, -3.5, 1e-300, -7e200, 0.0, std::ldexp(1.0, -1021)})
+    if (half(x) != x * 0.5) return fail("half", x, half(x), x * 0.5);
   for (uint32_t n = 1; n < (1u << 20); ++n)
     if (from_int(n) != (double)n) return fail("from_int", n, from_int(n), n);
   if (from_int(0x7fffffffu) != 2147483647.0) return fail("from_int max", 0, 0, 0);
