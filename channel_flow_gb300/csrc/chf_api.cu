@@ -134,6 +134,9 @@ static void release(chf_handle* h) {
   }
   for (auto e : h->event_pool) cudaEventDestroy(e);
   for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->side_stream) cudaStreamDestroy(h->side_stream);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
 }
 
@@ -284,6 +287,10 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
     rc = setup_mixed(h);
     if (rc == CHF_OK) rc = setup_solver_mixed(h);
     if (rc != CHF_OK) return fail(rc);
+    if (!cuda_ok(h, cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming), "cudaEventCreate") ||
+        !cuda_ok(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming), "cudaEventCreate"))
+      return fail(CHF_E_CUDA);
   }
   h->kernels_per_step = cfg->precision == CHF_MIXED ? 13 : 6;
   if (!cuda_ok(h, cudaStreamSynchronize(h->stream), "create sync")) return fail(CHF_E_CUDA);

@@ -136,6 +136,10 @@ struct Handle {
   // statistics
   int kernels_per_step = 0;
   cudaStream_t own_stream = nullptr;
+  // mixed path: the (0,0)-mode solve runs on a side stream beside the other
+  // modes' solve (fork / join events on the handle's stream)
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   // chf_step replays a CUDA graph of two steps.  Each step exchanges the
   // history buffers by pointer (f[F_U] <-> f[F_RV], f[F_W] <-> f[F_RG]), so
@@ -205,7 +209,7 @@ int step_once(Handle* h);
 int setup_solver(Handle* h);
 int setup_solver_mixed(Handle* h);
 int launch_solve_fp64(Handle* h);
-int launch_solve_mean(Handle* h);   // the (0,0) mode alone
+int launch_solve_mean(Handle* h, cudaStream_t st);  // the (0,0) mode alone, on st
 int launch_solve_mixed(Handle* h);  // k_solve_mixed.cu
 int launch_diagnostics(Handle* h, chf_diag* out);
 

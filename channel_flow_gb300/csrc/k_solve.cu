@@ -712,7 +712,7 @@ int setup_solver(Handle* h) {
 }
 
 // groups g0 .. nk2 (the last CTA is the (0,0) mode)
-static int launch_solve_from(Handle* h, int g0) {
+static int launch_solve_from(Handle* h, int g0, cudaStream_t st) {
   const Dims& d = h->d;
   SolveArgs a;
   a.v = h->f[F_V];
@@ -760,15 +760,15 @@ static int launch_solve_from(Handle* h, int g0) {
     return CHF_E_CUDA;
   cudaEvent_t ev;
   prof_begin(h, g0 == 0 ? K_SOLVE : K_SOLVE_MEAN, &ev);
-  kern<<<h->nk2 + 1 - g0, S_THREADS, smem, h->stream>>>(a);
+  kern<<<h->nk2 + 1 - g0, S_THREADS, smem, st>>>(a);
   prof_end(h, g0 == 0 ? K_SOLVE : K_SOLVE_MEAN, ev);
   if (!cuda_ok(h, cudaGetLastError(), "k_solve")) return CHF_E_CUDA;
   return CHF_OK;
 }
 
-int launch_solve_fp64(Handle* h) { return launch_solve_from(h, 0); }
+int launch_solve_fp64(Handle* h) { return launch_solve_from(h, 0, h->stream); }
 
-int launch_solve_mean(Handle* h) { return launch_solve_from(h, h->nk2); }
+int launch_solve_mean(Handle* h, cudaStream_t st) { return launch_solve_from(h, h->nk2, st); }
 
 int launch_diagnostics(Handle* h, chf_diag* out) {
   const Dims& d = h->d;

@@ -393,6 +393,18 @@ int launch_solve_mixed(Handle* h) {
   const double dt = h->cfg.dt;
   cudaStream_t st = h->stream;
   cudaEvent_t ev;
+  // the (0,0) mode touches only mode-0 entries and the mean arrays, which
+  // the kernels below neither write nor use: it runs beside them on the side
+  // stream (in order on the handle's stream while kernels are being timed)
+  const bool fork = h->side_stream && !h->profiling;
+  if (fork) {
+    if (!cuda_ok(h, cudaEventRecord(h->ev_fork, st), "solve fork") ||
+        !cuda_ok(h, cudaStreamWaitEvent(h->side_stream, h->ev_fork, 0), "solve fork"))
+      return CHF_E_CUDA;
+    const int rc = launch_solve_mean(h, h->side_stream);
+    if (rc != CHF_OK) return rc;
+    if (!cuda_ok(h, cudaEventRecord(h->ev_join, h->side_stream), "solve join")) return CHF_E_CUDA;
+  }
   if (h->nk2 > 0) {
     const size_t smem = (sizeof(cd) + sizeof(CoefHL) + sizeof(float2)) * MCH * 2 * (size_t)NZ;
     if (smem > 48 * 1024 &&
@@ -412,8 +424,9 @@ int launch_solve_mixed(Handle* h) {
     prof_end(h, K_INC_RECOVER, ev);
   }
   if (!cuda_ok(h, cudaGetLastError(), "mixed solve")) return CHF_E_CUDA;
+  if (fork) return cuda_ok(h, cudaStreamWaitEvent(st, h->ev_join, 0), "solve join") ? CHF_OK : CHF_E_CUDA;
   // the (0,0) mode: the FP64 solve kernel, its last CTA only
-  return launch_solve_mean(h);
+  return launch_solve_mean(h, st);
 }
 
 }  // namespace chf
