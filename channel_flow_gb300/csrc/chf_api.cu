@@ -242,6 +242,9 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
       !cuda_ok(h, cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "cudaStreamCreate"))
     return fail(CHF_E_CUDA);
   h->stream = h->own_stream;
+  if (!cuda_ok(h, cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, cfg->device),
+               "cudaDeviceGetAttribute"))
+    return fail(CHF_E_CUDA);
   h->prof.resize(K_COUNT);
   for (int k = 0; k < K_COUNT; ++k) h->prof[k] = {kKernelNames[k], 0, 0.0};
   const size_t fe = d.field_elems();
@@ -401,8 +404,10 @@ int chf_step(chf_handle* h, int nsteps) {
   return CHF_OK;
 }
 
-// Device-side error word: tensor-core kernels record a bounded-wait timeout
-// there (11: operand copy, 12: MMA completion) instead of hanging.
+// Device-side error word: the tensor-core GEMM records a bounded-wait
+// timeout there instead of hanging (11: a free ring stage, 12: a free
+// accumulator set, 13: operands, 14: the final MMA drain, 15: accumulators
+// ready, 16: copies landing at exit, 17: the resident A tile at exit).
 static int check_status(chf_handle* h) {
   int st = 0;
   if (!cuda_ok(h, cudaMemcpyAsync(&st, h->dev_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream),

@@ -34,14 +34,14 @@ struct Dims {
 };
 
 // Tensor-core GEMM plans (k_tcgemm.cu): K in chunks of at most TC_KC.
-constexpr int TC_KC = 64;
+constexpr int TC_KC = 32;
 constexpr int FX_PLANES = 4;     // digit planes per operand
 constexpr int FX_NT = 64;        // columns per B tile
 struct FxPlan {
   int mvalid, mtiles, kpad, ntiles, nchunks;
   long ncols;
-  int kc[16];
-  size_t a_chunk_off[16], b_chunk_off[16];
+  int kc[24];  // K <= 680 (the exactness bound) in chunks of TC_KC
+  size_t a_chunk_off[24], b_chunk_off[24];
   size_t a_tile_bytes, b_tile_bytes;  // one 128-row A tile / one 64-column B tile
   __host__ __device__ size_t b_field_bytes() const { return (size_t)ntiles * b_tile_bytes; }
   __host__ __device__ size_t bexp_stride() const { return (size_t)ntiles * FX_NT; }
@@ -78,6 +78,7 @@ struct Handle {
   chf_config cfg;
   Dims d;
   int device = 0;
+  int num_sms = 1;  // multiprocessors of the device (persistent-kernel grids)
   cudaStream_t stream = nullptr;
   std::string err;
   bool uploaded = false;

@@ -130,5 +130,48 @@ __host__ __device__ __forceinline__ double from_int(uint32_t n) {
   return u2d(((uint64_t)(1023 + top) << 52) | (((uint64_t)n << (52 - top)) & 0xfffffffffffffull));
 }
 
+__host__ __device__ __forceinline__ int clz64(uint64_t a) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)a);
+#else
+  return __builtin_clzll(a);
+#endif
+}
+
+// t 2^n as a binary64, exact for |t| < 2^53 (results below 2^-1022 give
+// signed zero, above the binary64 range infinity)
+__host__ __device__ __forceinline__ double scaled_i64(long long t, int n) {
+  if (t == 0) return 0.0;
+  const uint64_t sign = t < 0 ? 0x8000000000000000ull : 0ull;
+  const uint64_t a = t < 0 ? (uint64_t)(-t) : (uint64_t)t;
+  const int top = 63 - clz64(a);  // a in [2^top, 2^(top+1)), top <= 52
+  const int eb = 1023 + top + n;
+  if (eb <= 0) return u2d(sign);
+  if (eb >= 2047) return u2d(sign | 0x7ff0000000000000ull);
+  return u2d(sign | ((uint64_t)eb << 52) | ((a << (52 - top)) & 0xfffffffffffffull));
+}
+
+// t 2^n rounded to the nearest binary32 (ties to even), |t| < 2^62 (results
+// below 2^-126 give signed zero, above the binary32 range infinity)
+__host__ __device__ __forceinline__ float scaled_i64_f(long long t, int n) {
+  if (t == 0) return 0.f;
+  const uint32_t sign = t < 0 ? 1u : 0u;
+  const uint64_t a = t < 0 ? (uint64_t)(-t) : (uint64_t)t;
+  int top = 63 - clz64(a);
+  uint64_t m;  // 24-bit significand
+  if (top <= 23) {
+    m = a << (23 - top);
+  } else {
+    const int sh = top - 23;
+    const uint64_t r = a + ((1ull << (sh - 1)) - 1) + ((a >> sh) & 1);  // round to nearest even
+    m = r >> sh;
+    if (m >> 24) {  // rounding carried into a new leading bit
+      m >>= 1;
+      ++top;
+    }
+  }
+  return make_f(sign, 127 + top + n, (uint32_t)m & 0x7fffffu);
+}
+
 }  // namespace bits
 }  // namespace chf

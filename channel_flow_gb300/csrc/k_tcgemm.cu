@@ -54,6 +54,7 @@
 #include <vector>
 
 #include "chf_internal.h"
+#include "f64bits.cuh"
 #include "tc_dev.cuh"
 
 namespace chf {
@@ -79,162 +80,294 @@ void fx_digits_host(double x, int e, double* dg) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// GEMM.  grid (ntiles, mtiles, nfields), 128 threads, dynamic shared memory
-// FX_PLANES planes of 128 x TC_KC (A) and of 64 x TC_KC (B) bf16.
+// GEMM: persistent and warp-specialised, one CTA per SM (all 512 TMEM
+// columns).  CTA c works on the 128-row tile mt = c % mtiles and deals the
+// (field, 64-column tile) items of that tile round-robin with the other CTAs
+// of the same mt.  Shared memory holds either
+//   resident: the CTA's whole A tile image (loaded once) plus a ring of
+//             WS_STAGES B chunk stages (K chunks of TC_KC), or
+//   streamed: a ring of WS_STAGES stages each holding the A and B chunks
+// (resident when it fits: A is the transform matrix, the same for every item,
+// and re-reading it per item would make the GEMM L2-bound).
+//   warp 0    producer: per K chunk of an item waits for a free stage, then
+//             moves the chunk's plane images with cp.async.bulk (completion
+//             counted in bytes on the stage's "full" barrier);
+//   warp 1    MMA issuer: waits for a free accumulator set (two sets of four
+//             64-column level accumulators, so one item's epilogue overlaps
+//             the next item's MMAs), per chunk waits for "full", issues the 10
+//             level MMAs per K16 slice (descriptors formed once per chunk,
+//             advanced by a constant per slice) and commits to the stage's
+//             "empty" barrier; after the last chunk it commits to "tfull";
+//   warps 2-9 epilogue: wait for "tfull", read the levels back with
+//             tcgen05.ld (warp w reads TMEM lanes 32 (w % 4) .., columns
+//             32 ((w - 2) / 4) ..), release the set on "tempty" and form the
+//             outputs from the exact 64-bit level sum.
+// Every wait is bounded (1 s of wall time); a role that times out records
+// the failure, the others see it and stop, the producer waits for its copies
+// in flight and the MMA issuer drains its outstanding MMAs (both bounded)
+// before the tensor memory is freed.
 // ---------------------------------------------------------------------------
 // instruction descriptor: D = F32, A = B = BF16, both K-major, M = 128, N = 64
 constexpr uint32_t IDESC_FX = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr int WS_STAGES = 4;
+constexpr int WS_EPI_WARPS = 8;
+constexpr int WS_THREADS = 64 + 32 * WS_EPI_WARPS;
+constexpr uint32_t WS_A_PLANE = 128u * TC_KC * 2u;
+constexpr uint32_t WS_B_PLANE = (uint32_t)FX_NT * TC_KC * 2u;
+constexpr uint32_t WS_B_STAGE = (uint32_t)FX_PLANES * WS_B_PLANE;
+constexpr uint32_t WS_AB_STAGE = (uint32_t)FX_PLANES * (WS_A_PLANE + WS_B_PLANE);
+constexpr uint32_t WS_TMEM_COLS = 2u * FX_TMEM_COLS;  // two accumulator sets
+constexpr size_t WS_SMEM_LIMIT = 225u * 1024u;        // dynamic, below the 227 KB opt-in
+
+__host__ __device__ inline size_t ws_a_resident_bytes(const FxPlan& p) { return (p.a_tile_bytes + 1023) / 1024 * 1024; }
+__host__ __device__ inline bool ws_resident(const FxPlan& p) {
+  return ws_a_resident_bytes(p) + (size_t)WS_STAGES * WS_B_STAGE <= WS_SMEM_LIMIT;
+}
+
+// one output from the four exact level sums: t 2^n, |t| < 2^46, with
+// t = acc_0 2^21 + acc_1 2^14 + acc_2 2^7 + acc_3, rounded (FP32) or exact
+// (FP64) by bit operations on the 64-bit integer
+__device__ __forceinline__ long long fx_level_sum(const uint32_t* acc) {
+  return ((long long)__float2int_rn(__uint_as_float(acc[0])) << 21) +
+         ((long long)__float2int_rn(__uint_as_float(acc[1])) << 14) +
+         ((long long)__float2int_rn(__uint_as_float(acc[2])) << 7) +
+         (long long)__float2int_rn(__uint_as_float(acc[3]));
+}
+template <typename OutT>
+__device__ __forceinline__ OutT fx_out(const uint32_t* acc, int n);
+template <>
+__device__ __forceinline__ float fx_out<float>(const uint32_t* acc, int n) {
+  return bits::scaled_i64_f(fx_level_sum(acc), n);
+}
+template <>
+__device__ __forceinline__ double fx_out<double>(const uint32_t* acc, int n) {
+  return bits::scaled_i64(fx_level_sum(acc), n);
+}
+
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
 
 template <typename OutT>
-__device__ __forceinline__ void store_fx(OutT* p, long long t, int n);
-// t 2^n, correctly rounded to FP32 (n in the normal exponent range)
-template <>
-__device__ __forceinline__ void store_fx<float>(float* p, long long t, int n) {
-  const float v = __ll2float_rn(t);
-  const int h = n / 2;  // two exact power-of-two factors keep each in range
-  *p = v * __int_as_float((127 + h) << 23) * __int_as_float((127 + n - h) << 23);
-}
-// t 2^n exactly in FP64 (|t| < 2^46)
-template <>
-__device__ __forceinline__ void store_fx<double>(double* p, long long t, int n) {
-  *p = (double)t * __longlong_as_double((long long)(1023 + n) << 52);
-}
-
-template <typename OutT>
-__global__ void __launch_bounds__(TC_THREADS) k_tc_gemm_fx(const __grid_constant__ FxPlan plan,
-                                                           const uint8_t* __restrict__ aimg,
-                                                           const int* __restrict__ aexp,
-                                                           const uint8_t* __restrict__ bimg,
-                                                           const int* __restrict__ bexp,
-                                                           const __grid_constant__ Ptr8<OutT> outs,
-                                                           size_t ldc, int* status) {
+__global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_constant__ FxPlan plan,
+                                                              const uint8_t* __restrict__ aimg,
+                                                              const int* __restrict__ aexp,
+                                                              const uint8_t* __restrict__ bimg,
+                                                              const int* __restrict__ bexp,
+                                                              const __grid_constant__ Ptr8<OutT> outs,
+                                                              size_t ldc, int nfields, int* status) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t bar_load, bar_mma;
+  __shared__ __align__(8) uint64_t full[WS_STAGES], empty[WS_STAGES], tfull[2], tempty[2], drain, abar;
   __shared__ uint32_t tmem_base;
   __shared__ int s_fail;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int nt = blockIdx.x, mt = blockIdx.y, f = blockIdx.z;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   constexpr int NP = FX_PLANES;
-  constexpr uint32_t a_plane_max = 128u * TC_KC * 2u;
-  constexpr uint32_t b_plane_max = (uint32_t)FX_NT * TC_KC * 2u;
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + NP * a_plane_max;
+  const bool resident = ws_resident(plan);
+  const int mt = (int)(blockIdx.x % plan.mtiles);
+  const long j0 = blockIdx.x / plan.mtiles, jstep = gridDim.x / plan.mtiles;
+  const long njobs = (long)nfields * plan.ntiles;  // (field, column tile) items of this row tile
+  uint8_t* sAres = smem;                                            // resident A tile
+  uint8_t* ring = resident ? smem + ws_a_resident_bytes(plan) : smem;  // stages
+  const uint32_t stage_bytes = resident ? WS_B_STAGE : WS_AB_STAGE;
   if (tid == 0) {
     s_fail = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar_load)));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar_mma)));
+    for (int i = 0; i < WS_STAGES; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
+    }
+    for (int i = 0; i < 2; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&tfull[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tempty[i])), "r"(32 * WS_EPI_WARPS));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&drain)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&abar)));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base)),
-                 "r"(FX_TMEM_COLS));
+                 "r"(WS_TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base;
+  volatile int* fail = &s_fail;
   const uint8_t* atile = aimg + (size_t)mt * plan.a_tile_bytes;
-  const uint8_t* btile = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes;
-  for (int ch = 0; ch < plan.nchunks; ++ch) {
-    const int kc = plan.kc[ch];
-    const uint32_t apb = 128u * kc * 2u, bpb = (uint32_t)FX_NT * kc * 2u;
-    if (tid == 0 && !s_fail) {
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&bar_load)),
-                   "r"(NP * (apb + bpb))
-                   : "memory");
-      for (int pl = 0; pl < NP; ++pl) {
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_u32(sA + pl * a_plane_max)),
-            "l"(atile + plan.a_chunk_off[ch] + (size_t)pl * apb), "r"(apb), "r"(smem_u32(&bar_load))
-            : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_u32(sB + pl * b_plane_max)),
-            "l"(btile + plan.b_chunk_off[ch] + (size_t)pl * bpb), "r"(bpb), "r"(smem_u32(&bar_load))
-            : "memory");
+  if (warp == 0) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      if (resident) {
+        expect_tx(smem_u32(&abar), (uint32_t)plan.a_tile_bytes);
+        bulk_copy(smem_u32(sAres), atile, (uint32_t)plan.a_tile_bytes, smem_u32(&abar));
       }
-      if (!mbar_wait(smem_u32(&bar_load), ch & 1)) {
-        s_fail = 1;
-      } else {
-        // K-adjacent core matrices: 16 (A, 128 rows) or 8 (B, 64 columns)
-        // groups of 8 rows x 16 bytes apart; adjacent 8-row groups 128 B apart
-        const uint32_t lbo_a = 16u * 128u, lbo_b = 8u * 128u, sbo = 128u;
-        for (int s = 0; s < kc / 16; ++s) {
-#pragma unroll
-          for (int L = 0; L < FX_LEVELS; ++L) {
-#pragma unroll
-            for (int i = 0; i <= L; ++i) {
-              const int j = L - i;
-              uint64_t da = sdesc(smem_u32(sA + i * a_plane_max) + s * 2 * lbo_a, lbo_a, sbo);
-              uint64_t db = sdesc(smem_u32(sB + j * b_plane_max) + s * 2 * lbo_b, lbo_b, sbo);
-              uint32_t acc = (ch > 0 || s > 0 || i > 0) ? 1u : 0u;
-              asm volatile(
-                  "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(
-                      tmem + (uint32_t)(L * FX_NT)),
-                  "l"(da), "l"(db), "r"(IDESC_FX), "r"(acc));
-            }
+      uint32_t g = 0;  // chunks issued by this CTA
+      for (long j = j0; j < njobs && !*fail; j += jstep) {
+        const int f = (int)(j / plan.ntiles), nt = (int)(j % plan.ntiles);
+        const uint8_t* btile = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes;
+        for (int ch = 0; ch < plan.nchunks; ++ch, ++g) {
+          const uint32_t s = g % WS_STAGES, ph = (g / WS_STAGES) & 1u;
+          if (!mbar_wait(smem_u32(&empty[s]), ph ^ 1u)) {
+            *fail = 1;
+            break;
+          }
+          const int kc = plan.kc[ch];
+          const uint32_t apb = 128u * kc * 2u, bpb = (uint32_t)FX_NT * kc * 2u;
+          uint8_t* st = ring + (size_t)s * stage_bytes;
+          uint8_t* sB = resident ? st : st + NP * WS_A_PLANE;
+          const uint32_t fb = smem_u32(&full[s]);
+          expect_tx(fb, NP * (bpb + (resident ? 0u : apb)));
+          for (int pl = 0; pl < NP; ++pl) {
+            if (!resident) bulk_copy(smem_u32(st + pl * WS_A_PLANE), atile + plan.a_chunk_off[ch] + (size_t)pl * apb, apb, fb);
+            bulk_copy(smem_u32(sB + pl * WS_B_PLANE), btile + plan.b_chunk_off[ch] + (size_t)pl * bpb, bpb, fb);
           }
         }
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_u32(&bar_mma))
-            : "memory");
-        // the next chunk overwrites the operands: wait until the MMAs read them
-        if (!mbar_wait(smem_u32(&bar_mma), ch & 1)) s_fail = 2;
       }
+      // no copy may still be landing when the CTA exits: the last chunk
+      // issued into each stage (and the resident A tile) has arrived (a no-op
+      // after a normal run, where the MMA issuer consumed everything)
+      for (uint32_t k = g > (uint32_t)WS_STAGES ? g - WS_STAGES : 0; k < g; ++k)
+        if (!mbar_wait(smem_u32(&full[k % WS_STAGES]), (k / WS_STAGES) & 1u)) *fail = 6;
+      if (resident && !mbar_wait(smem_u32(&abar), 0)) *fail = 7;
     }
-    __syncthreads();
-    if (s_fail) break;
-  }
-  const bool ok = !s_fail;
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  if (ok) {
-    const int row = warp * 32 + (tid & 31);
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      // K-adjacent core matrices: 16 (A, 128 rows) or 8 (B, 64 columns)
+      // groups of 8 rows x 16 bytes apart; adjacent 8-row groups 128 B apart.
+      // One K16 slice advances the start address by 2 core matrices: 256 / 128
+      // in the descriptor's 16-byte units.
+      const uint32_t lbo_a = 16u * 128u, lbo_b = 8u * 128u, sbo = 128u;
+      bool ok = !resident || mbar_wait(smem_u32(&abar), 0);
+      if (!ok) *fail = 3;
+      uint32_t g = 0, tc = 0;
+      for (long j = j0; ok && j < njobs && !*fail; j += jstep, ++tc) {
+        const uint32_t b = tc & 1u, tph = (tc >> 1) & 1u;
+        if (!mbar_wait(smem_u32(&tempty[b]), tph ^ 1u)) {
+          *fail = 2;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t tacc = tmem + b * FX_TMEM_COLS;
+        for (int ch = 0; ch < plan.nchunks; ++ch, ++g) {
+          const uint32_t s = g % WS_STAGES, ph = (g / WS_STAGES) & 1u;
+          if (!mbar_wait(smem_u32(&full[s]), ph)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const int kc = plan.kc[ch];
+          const uint8_t* st = ring + (size_t)s * stage_bytes;
+          const uint8_t* sA = resident ? sAres + plan.a_chunk_off[ch] : st;
+          const uint32_t aplane = resident ? 128u * kc * 2u : WS_A_PLANE;
+          const uint8_t* sB = resident ? st : st + NP * WS_A_PLANE;
+          uint64_t da[NP], db[NP];
+#pragma unroll
+          for (int pl = 0; pl < NP; ++pl) {
+            da[pl] = sdesc(smem_u32(sA + pl * aplane), lbo_a, sbo);
+            db[pl] = sdesc(smem_u32(sB + pl * WS_B_PLANE), lbo_b, sbo);
+          }
+          for (int k16 = 0; k16 < kc / 16; ++k16) {
+            const bool first = (ch == 0 && k16 == 0);
+#pragma unroll
+            for (int L = 0; L < FX_LEVELS; ++L) {
+#pragma unroll
+              for (int i = 0; i <= L; ++i) {
+                const uint32_t accum = (first && i == 0) ? 0u : 1u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tacc + (uint32_t)(L * FX_NT)),
+                    "l"(da[i] + (uint64_t)(k16 * 256)), "l"(db[L - i] + (uint64_t)(k16 * 128)), "r"(IDESC_FX),
+                    "r"(accum));
+              }
+            }
+          }
+          mma_commit(smem_u32(&empty[s]));  // the stage is free once these MMAs have read it
+        }
+        if (!ok) {
+          *fail = 3;
+          break;
+        }
+        mma_commit(smem_u32(&tfull[b]));
+      }
+      // every MMA this thread issued has completed once "drain" arrives
+      mma_commit(smem_u32(&drain));
+      if (!mbar_wait(smem_u32(&drain), 0)) *fail = 4;
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int q = warp & 3;                     // the TMEM lane quarter this warp may access
+    const int cbase = 32 * ((warp - 2) / 4);    // its 32 of the 64 columns
+    const int row = q * 32 + lane;
     const int m = mt * 128 + row;
     const bool mrow = m < plan.mvalid;
     const int fm = mrow ? aexp[m] : 0;
-    OutT* out = outs.p[f];
-    const int* ecol = bexp + (size_t)f * plan.bexp_stride() + (size_t)nt * FX_NT;
-    for (int c0 = 0; c0 < FX_NT; c0 += 16) {
-      uint32_t r[FX_LEVELS][16];
-#pragma unroll
-      for (int L = 0; L < FX_LEVELS; ++L) {
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(L * FX_NT + c0);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-            "[%16];"
-            : "=r"(r[L][0]), "=r"(r[L][1]), "=r"(r[L][2]), "=r"(r[L][3]), "=r"(r[L][4]), "=r"(r[L][5]),
-              "=r"(r[L][6]), "=r"(r[L][7]), "=r"(r[L][8]), "=r"(r[L][9]), "=r"(r[L][10]), "=r"(r[L][11]),
-              "=r"(r[L][12]), "=r"(r[L][13]), "=r"(r[L][14]), "=r"(r[L][15])
-            : "r"(taddr));
+    uint32_t tc = 0;
+    for (long j = j0; j < njobs; j += jstep, ++tc) {
+      // decisions stay warp-uniform: tcgen05.ld needs the whole warp
+      if (__shfl_sync(0xffffffffu, *fail, 0)) break;
+      const uint32_t b = tc & 1u, tph = (tc >> 1) & 1u;
+      if (!__all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull[b]), tph))) {
+        if (lane == 0) *fail = 5;
+        break;
       }
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
-      if (mrow) {
-        const size_t col = (size_t)nt * FX_NT + c0;
-        OutT* dst = out + (size_t)m * ldc + col;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int f = (int)(j / plan.ntiles), nt = (int)(j % plan.ntiles);
+      OutT* out = outs.p[f];
+      // column exponents of this warp's 32 columns, one per lane
+      const int ecl = bexp[(size_t)f * plan.bexp_stride() + (size_t)nt * FX_NT + cbase + lane];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          if (col + q < (size_t)plan.ncols) {
-            // each level holds an integer below 2^24 exactly
-            const long long t = ((long long)__float2int_rn(__uint_as_float(r[0][q])) << 21) +
-                                ((long long)__float2int_rn(__uint_as_float(r[1][q])) << 14) +
-                                ((long long)__float2int_rn(__uint_as_float(r[2][q])) << 7) +
-                                (long long)__float2int_rn(__uint_as_float(r[3][q]));
-            store_fx(dst + q, t, fm + ecol[c0 + q] - 35);
+      for (int g2 = 0; g2 < 2; ++g2) {
+        const int c0 = cbase + 16 * g2;
+        uint32_t r[FX_LEVELS][16];
+#pragma unroll
+        for (int L = 0; L < FX_LEVELS; ++L) {
+          const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * FX_TMEM_COLS + (uint32_t)(L * FX_NT + c0);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+              "[%16];"
+              : "=r"(r[L][0]), "=r"(r[L][1]), "=r"(r[L][2]), "=r"(r[L][3]), "=r"(r[L][4]), "=r"(r[L][5]),
+                "=r"(r[L][6]), "=r"(r[L][7]), "=r"(r[L][8]), "=r"(r[L][9]), "=r"(r[L][10]), "=r"(r[L][11]),
+                "=r"(r[L][12]), "=r"(r[L][13]), "=r"(r[L][14]), "=r"(r[L][15])
+              : "r"(taddr));
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        if (g2 == 1) {  // this warp's part of the set is in registers: release it
+          asm volatile("tcgen05.fence::before_thread_sync;");
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+        }
+        int ec[16];
+#pragma unroll
+        for (int qq = 0; qq < 16; ++qq) ec[qq] = __shfl_sync(0xffffffffu, ecl, 16 * g2 + qq);
+        if (mrow) {
+          const size_t col = (size_t)nt * FX_NT + c0;
+          OutT* dst = out + (size_t)m * ldc + col;
+#pragma unroll
+          for (int qq = 0; qq < 16; ++qq) {
+            if (col + qq < (size_t)plan.ncols) {
+              const uint32_t acc[FX_LEVELS] = {r[0][qq], r[1][qq], r[2][qq], r[3][qq]};
+              dst[qq] = fx_out<OutT>(acc, fm + ec[qq] - 35);
+            }
           }
         }
       }
     }
-  } else if (tid == 0) {
-    atomicExch(status, s_fail == 1 ? 11 : 12);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
+  if (tid == 0 && s_fail) atomicExch(status, 10 + s_fail);
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(FX_TMEM_COLS));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(WS_TMEM_COLS));
 }
 
 // ---------------------------------------------------------------------------
@@ -353,15 +486,19 @@ int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int
     h->err = "k_tc_gemm_fx: K is too long for exact sums";
     return CHF_E_INVALID;
   }
-  const size_t smem = (size_t)FX_PLANES * (128 + FX_NT) * TC_KC * 2;
+  const size_t smem = ws_resident(p) ? ws_a_resident_bytes(p) + (size_t)WS_STAGES * WS_B_STAGE
+                                     : (size_t)WS_STAGES * WS_AB_STAGE;
   if (!cuda_ok(h, cudaFuncSetAttribute(k_tc_gemm_fx<OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem),
                "k_tc_gemm_fx smem"))
     return CHF_E_CUDA;
-  dim3 grid(p.ntiles, p.mtiles, nfields);
+  // whole multiples of the row tiles, each CTA on one row tile
+  const long items = (long)nfields * p.ntiles * p.mtiles;
+  const int grid = (int)(std::min<long>(items, (long)std::max(h->num_sms, p.mtiles)) / p.mtiles * p.mtiles);
   cudaEvent_t ev;
   prof_begin(h, kid, &ev);
-  k_tc_gemm_fx<OutT><<<grid, TC_THREADS, smem, h->stream>>>(p, aimg, aexp, bimg, bexp, outs, ldc, h->dev_status);
+  k_tc_gemm_fx<OutT><<<grid, WS_THREADS, smem, h->stream>>>(p, aimg, aexp, bimg, bexp, outs, ldc, nfields,
+                                                            h->dev_status);
   prof_end(h, kid, ev);
   return cuda_ok(h, cudaGetLastError(), "k_tc_gemm_fx") ? CHF_OK : CHF_E_CUDA;
 }

@@ -58,6 +58,21 @@ int main() {
   for (uint32_t n = 1; n < (1u << 20); ++n)
     if (from_int(n) != (double)n) return fail("from_int", n, from_int(n), n);
   if (from_int(0x7fffffffu) != 2147483647.0) return fail("from_int max", 0, 0, 0);
+  // scaled integers (the exact-GEMM epilogue): t 2^n
+  std::uniform_int_distribution<long long> ti(-(1ll << 46), (1ll << 46));
+  std::uniform_int_distribution<int> sh(-60, 10);
+  for (int i = 0; i < 2000000; ++i) {
+    long long t = ti(rng);
+    if (i % 4 == 1) t >>= (i % 40);  // small magnitudes too
+    const int n = sh(rng);
+    const double want = std::ldexp((double)t, n);
+    if (scaled_i64(t, n) != want) return fail("scaled_i64", (double)t, scaled_i64(t, n), want);
+    const float wf = static_cast<float>(std::ldexp((double)static_cast<float>(t), n));  // RN-even once
+    if (scaled_i64_f(t, n) != wf) return fail("scaled_i64_f", (double)t, scaled_i64_f(t, n), wf);
+  }
+  if (scaled_i64_f((1ll << 24) + 1, 0) != 16777216.f || scaled_i64_f((1ll << 24) + 3, 0) != 16777220.f ||
+      scaled_i64_f(-((1ll << 25) - 1), 0) != -33554432.f)
+    return fail("ties", 0, 0, 0);
   std::printf("ok\n");
   return 0;
 }
