@@ -125,8 +125,8 @@ __host__ __device__ inline bool ws_resident(const FxPlan& p) {
 }
 
 // one output from the four exact level sums: t 2^n, |t| < 2^46, with
-// t = acc_0 2^21 + acc_1 2^14 + acc_2 2^7 + acc_3, rounded (FP32) or exact
-// (FP64) by bit operations on the 64-bit integer
+// t = acc_0 2^21 + acc_1 2^14 + acc_2 2^7 + acc_3 (the levels can cancel, so
+// t is formed exactly before the single rounding)
 __device__ __forceinline__ long long fx_level_sum(const uint32_t* acc) {
   return ((long long)__float2int_rn(__uint_as_float(acc[0])) << 21) +
          ((long long)__float2int_rn(__uint_as_float(acc[1])) << 14) +
@@ -135,10 +135,18 @@ __device__ __forceinline__ long long fx_level_sum(const uint32_t* acc) {
 }
 template <typename OutT>
 __device__ __forceinline__ OutT fx_out(const uint32_t* acc, int n);
+// FP32: t = t_h 2^23 + t_l with |t_h| < 2^23 and 0 <= t_l < 2^23, both exact
+// in binary32, so one FMA rounds the exact t once (to nearest even); the
+// scaling by 2^n is two exact power-of-two multiplies
 template <>
 __device__ __forceinline__ float fx_out<float>(const uint32_t* acc, int n) {
-  return bits::scaled_i64_f(fx_level_sum(acc), n);
+  const long long t = fx_level_sum(acc);
+  const float v = __fmaf_rn(__int2float_rn((int)(t >> 23)), 8388608.0f, __int2float_rn((int)(t & 0x7fffff)));
+  const int h = n / 2;  // two factors keep each power of two in range
+  return v * __int_as_float((127 + h) << 23) * __int_as_float((127 + n - h) << 23);
 }
+// FP64: exact, built from the 64-bit integer by bit operations (off the
+// narrow FP64 pipe)
 template <>
 __device__ __forceinline__ double fx_out<double>(const uint32_t* acc, int n) {
   return bits::scaled_i64(fx_level_sum(acc), n);
@@ -352,12 +360,23 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
         if (mrow) {
           const size_t col = (size_t)nt * FX_NT + c0;
           OutT* dst = out + (size_t)m * ldc + col;
+          OutT v[16];
 #pragma unroll
           for (int qq = 0; qq < 16; ++qq) {
-            if (col + qq < (size_t)plan.ncols) {
-              const uint32_t acc[FX_LEVELS] = {r[0][qq], r[1][qq], r[2][qq], r[3][qq]};
-              dst[qq] = fx_out<OutT>(acc, fm + ec[qq] - 35);
-            }
+            const uint32_t acc[FX_LEVELS] = {r[0][qq], r[1][qq], r[2][qq], r[3][qq]};
+            v[qq] = fx_out<OutT>(acc, fm + ec[qq] - 35);
+          }
+          // a thread's 16 outputs are consecutive in its row: 16-byte stores
+          // when the group is whole and aligned, element stores otherwise
+          if (col + 16 <= (size_t)plan.ncols && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0) {
+            uint4* d4 = reinterpret_cast<uint4*>(dst);
+            const uint4* v4 = reinterpret_cast<const uint4*>(v);
+#pragma unroll
+            for (int k = 0; k < (int)(16 * sizeof(OutT) / 16); ++k) d4[k] = v4[k];
+          } else {
+#pragma unroll
+            for (int qq = 0; qq < 16; ++qq)
+              if (col + qq < (size_t)plan.ncols) dst[qq] = v[qq];
           }
         }
       }
