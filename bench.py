@@ -81,7 +81,7 @@ def workload_name(cfg, precision, zpad):
 # --------------------------------------------------------------------------
 # algorithmic work per kernel launch (bytes read + written once, FP64 flops)
 # --------------------------------------------------------------------------
-def kernel_work(cfg, zpad=0):
+def kernel_work(cfg, zpad=0, precision="fp64"):
     N = cfg.nnz
     NZ = N + 1
     KX, KY = cfg.nnx // 2, cfg.nny
@@ -114,6 +114,28 @@ def kernel_work(cfg, zpad=0):
     nsolve = int((k2 != 0.0).sum())
     w["k_solve"] = ((nk2 + 1) * stride * 8 + 12 * NZ * modes * c,
                     nsolve * (8 * (ne * ne + no * no) + 2 * fft_flops(2 * N)))
+    if precision != "mixed":
+        return w
+    # mixed path: FP32 x/y work halves the bytes; the z transforms are exact
+    # GEMMs on 4 bf16 digit planes (B images in, FP32/FP64 out); the solve
+    # reads A^-1 (B - A) as (hi, lo) floats and A^-1 as floats per k^2 group
+    for k in ("k_yinv", "k_xprod", "k_yfwd"):
+        w[k] = (w[k][0] // 2, w[k][1])
+    cols = 2 * modes
+
+    def kp(k):
+        return (k + 15) // 16 * 16
+
+    img = 4 * 2  # four bf16 planes per element
+    w["k_tc_split_z1"] = (6 * NZ * cols * 8 + 6 * kp(NZ) * cols * img, 0)
+    w["k_tc_gemm_z1"] = (6 * kp(NZ) * cols * img + 6 * MP * cols * 4, 6 * 10 * 2 * 128 * cols * kp(NZ) * 2)
+    w["k_tc_split_z2"] = (3 * MP * cols * 4 + 3 * kp(MP) * cols * img, 0)
+    w["k_tc_gemm_z2"] = (3 * kp(MP) * cols * img + 3 * NZ * cols * 8, 3 * 10 * 2 * 128 * cols * kp(MP) * 2)
+    w["k_curl"] = (3 * NZ * cols * 8 + 2 * kp(NZ) * cols * img, nsolve * NZ * 12)
+    w["k_tc_gemm_gl"] = (2 * kp(NZ) * cols * img + 2 * NZ * cols * 8, 2 * 10 * 2 * 128 * cols * kp(NZ) * 2)
+    w["k_inc_solve"] = (nk2 * stride * (8 + 4) + 8 * NZ * modes * c,
+                        nsolve * 2 * (2 * (ne * ne + no * no)) * 2)
+    w["k_inc_recover"] = (6 * NZ * modes * c, nsolve * NZ * 26)
     return w
 
 
@@ -348,7 +370,7 @@ def main():
             dist.destroy_process_group()
         return 0
     # ---- roofline of the dominant kernel
-    work = kernel_work(cfg, args.zpad)
+    work = kernel_work(cfg, args.zpad, args.precision)
     kname = max((k for k in prof if prof[k][0] > 0), key=lambda k: prof[k][1])
     launches, kms = prof[kname]
     avg_ms = kms / launches
@@ -376,7 +398,9 @@ def main():
         "metric": "steps/s", "value": value, "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32 FFTs/products + bf16x3 tcgen05 GEMMs (f32 accum) + f64 solves",
+        "dtype": "f64" if args.precision == "fp64" else ("f64 state; f32 x/y FFTs and products; exact fixed-point "
+                                                         "tcgen05 z transforms (bf16 digits, exact f32 level sums); "
+                                                         "f64 curl and recurrences; compensated f32 increment solve"),
         "data": "synthetic (seeded laminar profile + 10% divergence-free perturbation)",
         "config": {"workload": workload_name(cfg, args.precision, args.zpad),
                    "grid_points": cfg.points, "precision": args.precision,
