@@ -20,7 +20,7 @@ STATUS = {0: "CHF_OK", -1: "CHF_E_INVALID", -2: "CHF_E_CUDA", -3: "CHF_E_NOMEM",
 
 # Every entry point declared in include/chflow.h.
 EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
-           "chf_download_state", "chf_getnonlinear", "chf_solve", "chf_step",
+           "chf_download_state", "chf_getnonlinear", "chf_solve", "chf_step", "chf_step_host",
            "chf_synchronize", "chf_diagnostics", "chf_kernels_per_step", "chf_device_field",
            "chf_set_stream", "chf_profile_enable", "chf_profile_reset", "chf_profile_read",
            "chf_diagnostics_static", "chf_write_restart", "chf_read_restart",
@@ -76,6 +76,7 @@ def load_library(path: str = None):
     for name in ("chf_getnonlinear", "chf_solve", "chf_synchronize"):
         getattr(L, name).argtypes = [vp]
     L.chf_step.argtypes = [vp, ctypes.c_int]
+    L.chf_step_host.argtypes = [vp, ctypes.c_int] + [dp] * 14
     L.chf_diagnostics.argtypes = [vp, ctypes.POINTER(CDiag)]
     L.chf_kernels_per_step.argtypes = [vp]
     L.chf_device_field.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp)]
@@ -181,6 +182,22 @@ class Channel:
         self._check(self.L.chf_download_state(
             self.h, *[_dptr(out[k]) for k in FIELD_NAMES], *[_dptr(out[k]) for k in MEAN_NAMES]))
         return out
+
+    def step_host(self, st: dict, n: int = 1) -> dict:
+        """Advance the host module arrays in ``st`` by ``n`` steps in place
+        (chf_step_host: upload, steps and download overlapped; page-locked
+        arrays give the full link bandwidth).  Every array is required,
+        C-contiguous float64 and writable."""
+        arrs = []
+        for k, shape in [(k, self.shape) for k in FIELD_NAMES] + [(k, (self.cfg.nnz + 1, 2)) for k in MEAN_NAMES]:
+            a = st.get(k)
+            if a is None or a.dtype != np.float64 or not a.flags.c_contiguous or not a.flags.writeable:
+                raise ChannelError(-1, f"{k}: a writable C-contiguous float64 array is required")
+            if a.shape != shape:
+                raise ChannelError(-1, f"{k}: shape {a.shape} != {shape}")
+            arrs.append(a)
+        self._check(self.L.chf_step_host(self.h, int(n), *[_dptr(a) for a in arrs]))
+        return st
 
     def getnonlinear(self):
         self._check(self.L.chf_getnonlinear(self.h))

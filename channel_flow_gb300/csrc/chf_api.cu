@@ -134,6 +134,10 @@ static void release(chf_handle* h) {
   }
   for (auto e : h->event_pool) cudaEventDestroy(e);
   for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
+  for (cudaEvent_t e : {h->ev_ready, h->ev_inputs, h->ev_hist_in, h->ev_nonlinear, h->ev_vg, h->ev_done})
+    if (e) cudaEventDestroy(e);
+  if (h->copy_in) cudaStreamDestroy(h->copy_in);
+  if (h->copy_out) cudaStreamDestroy(h->copy_out);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->side_stream) cudaStreamDestroy(h->side_stream);
@@ -295,6 +299,11 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
         !cuda_ok(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming), "cudaEventCreate"))
       return fail(CHF_E_CUDA);
   }
+  if (!cuda_ok(h, cudaStreamCreateWithFlags(&h->copy_in, cudaStreamNonBlocking), "cudaStreamCreate") ||
+      !cuda_ok(h, cudaStreamCreateWithFlags(&h->copy_out, cudaStreamNonBlocking), "cudaStreamCreate"))
+    return fail(CHF_E_CUDA);
+  for (cudaEvent_t* e : {&h->ev_ready, &h->ev_inputs, &h->ev_hist_in, &h->ev_nonlinear, &h->ev_vg, &h->ev_done})
+    if (!cuda_ok(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate")) return fail(CHF_E_CUDA);
   h->kernels_per_step = cfg->precision == CHF_MIXED ? 13 : 6;
   if (!cuda_ok(h, cudaStreamSynchronize(h->stream), "create sync")) return fail(CHF_E_CUDA);
   *out = h;
@@ -402,6 +411,98 @@ int chf_step(chf_handle* h, int nsteps) {
     if (rc != CHF_OK) return rc;
   }
   return CHF_OK;
+}
+
+static int check_status(chf_handle* h);
+
+// One blocking call that advances host-resident module arrays in place:
+// upload, nsteps steps, download, with the copies overlapped with the steps.
+//   copy_in : the six nonlinear inputs and the mean arrays (the first
+//             nonlinear term waits for them), then the N^{n-1} histories
+//             (only the solve reads them: they land during the nonlinear term);
+//   copy_out: after the last nonlinear term, the new histories (during the
+//             solve); after the mixed path's increment solve, v and omega_y
+//             (during the recovery); at the end u, w, omega_x, omega_z and the
+//             mean arrays.
+// Every module array crosses the link once each way, as with
+// chf_upload_state + chf_step + chf_download_state, whose results this
+// reproduces bit for bit.
+static bool ev_rec(chf_handle* h, cudaEvent_t e, cudaStream_t s) {
+  return cuda_ok(h, cudaEventRecord(e, s), "cudaEventRecord");
+}
+static bool ev_wait(chf_handle* h, cudaStream_t s, cudaEvent_t e) {
+  return cuda_ok(h, cudaStreamWaitEvent(s, e, 0), "cudaStreamWaitEvent");
+}
+
+int chf_step_host(chf_handle* h, int nsteps, double* vnp1, double* omegaynp1, double* unp1, double* wnp1,
+                  double* omegaxnp1, double* omegaznp1, double* rhsvn, double* rhsomegayn, double* clamb1n,
+                  double* clamb1nm1, double* clamb3n, double* clamb3nm1, double* au0, double* w0) {
+  if (!h) return CHF_E_INVALID;
+  double* fh[F_COUNT] = {vnp1, omegaynp1, unp1, wnp1, omegaxnp1, omegaznp1, rhsvn, rhsomegayn};
+  double* mh[M_COUNT] = {clamb1n, clamb1nm1, clamb3n, clamb3nm1, au0, w0};
+  for (double* p : fh)
+    if (!p) {
+      h->err = "chf_step_host: every module array is required";
+      return CHF_E_INVALID;
+    }
+  for (double* p : mh)
+    if (!p) {
+      h->err = "chf_step_host: every module array is required";
+      return CHF_E_INVALID;
+    }
+  if (nsteps < 1) {
+    h->err = "nsteps must be >= 1";
+    return CHF_E_INVALID;
+  }
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
+  const bool mixed = h->cfg.precision == CHF_MIXED;
+  const size_t fb = sizeof(cd) * h->d.field_elems(), mb = sizeof(double) * 2 * h->d.NZ;
+  cudaStream_t S = h->stream, ci = h->copy_in, co = h->copy_out;
+  auto up = [&](void* dst, const void* src, size_t n) {
+    return cuda_ok(h, cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, ci), "upload");
+  };
+  auto down = [&](void* dst, const void* src, size_t n) {
+    return cuda_ok(h, cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, co), "download");
+  };
+  // the device buffers may still be in use by earlier work on the handle's stream
+  if (!ev_rec(h, h->ev_ready, S) || !ev_wait(h, ci, h->ev_ready) || !ev_wait(h, co, h->ev_ready)) return CHF_E_CUDA;
+  for (int i : {F_U, F_V, F_W, F_OX, F_OY, F_OZ})
+    if (!up(h->f[i], fh[i], fb)) return CHF_E_CUDA;
+  for (int i = 0; i < M_COUNT; ++i)
+    if (!up(h->mean[i], mh[i], mb)) return CHF_E_CUDA;
+  if (!ev_rec(h, h->ev_inputs, ci)) return CHF_E_CUDA;
+  if (!up(h->f[F_RV], fh[F_RV], fb) || !up(h->f[F_RG], fh[F_RG], fb) || !ev_rec(h, h->ev_hist_in, ci))
+    return CHF_E_CUDA;
+  h->uploaded = true;
+  if (!ev_wait(h, S, h->ev_inputs)) return CHF_E_CUDA;
+  for (int s = 0; s < nsteps; ++s) {
+    const bool last = s == nsteps - 1;
+    int rc = mixed ? launch_nonlinear_mixed(h) : launch_nonlinear_fp64(h);
+    if (rc != CHF_OK) return rc;
+    if (s == 0 && !ev_wait(h, S, h->ev_hist_in)) return CHF_E_CUDA;
+    if (last) {  // the new histories are final; the host buffers were read by the upload
+      if (!ev_rec(h, h->ev_nonlinear, S) || !ev_wait(h, co, h->ev_nonlinear) || !ev_wait(h, co, h->ev_hist_in) ||
+          !down(fh[F_RV], h->f[F_RV], fb) || !down(fh[F_RG], h->f[F_RG], fb))
+        return CHF_E_CUDA;
+    }
+    h->after_inc = (last && mixed) ? h->ev_vg : nullptr;
+    rc = mixed ? launch_solve_mixed(h) : launch_solve_fp64(h);
+    h->after_inc = nullptr;
+    if (rc != CHF_OK) return rc;
+    if (last && mixed &&
+        (!ev_wait(h, co, h->ev_vg) || !down(fh[F_V], h->f[F_V], fb) || !down(fh[F_OY], h->f[F_OY], fb)))
+      return CHF_E_CUDA;
+  }
+  if (!ev_rec(h, h->ev_done, S) || !ev_wait(h, co, h->ev_done)) return CHF_E_CUDA;
+  for (int i : {F_U, F_W, F_OX, F_OZ})
+    if (!down(fh[i], h->f[i], fb)) return CHF_E_CUDA;
+  if (!mixed)
+    for (int i : {F_V, F_OY})
+      if (!down(fh[i], h->f[i], fb)) return CHF_E_CUDA;
+  for (int i = 0; i < M_COUNT; ++i)
+    if (!down(mh[i], h->mean[i], mb)) return CHF_E_CUDA;
+  if (!cuda_ok(h, cudaStreamSynchronize(co), "cudaStreamSynchronize")) return CHF_E_CUDA;
+  return check_status(h);
 }
 
 // Device-side error word: the tensor-core GEMM records a bounded-wait

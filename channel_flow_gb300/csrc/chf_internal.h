@@ -141,6 +141,13 @@ struct Handle {
   // modes' solve (fork / join events on the handle's stream)
   cudaStream_t side_stream = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // chf_step_host: copy streams in / out and the events that order them
+  // against the handle's stream; after_inc, when set, is recorded right after
+  // the mixed path's increment solve (v, omega_y final from there on)
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t ev_ready = nullptr, ev_inputs = nullptr, ev_hist_in = nullptr, ev_nonlinear = nullptr,
+              ev_vg = nullptr, ev_done = nullptr;
+  cudaEvent_t after_inc = nullptr;
 
   // chf_step replays a CUDA graph of two steps.  Each step exchanges the
   // history buffers by pointer (f[F_U] <-> f[F_RV], f[F_W] <-> f[F_RG]), so

@@ -113,16 +113,54 @@ struct CoefHL {
 
 constexpr int CB = 4;  // matrix columns per load batch (two batches in flight)
 
-// S + C += (mh + ml)(ch + cl), compensated: p + e = mh ch exactly, the cross
-// terms join e, TwoSum keeps the rounding error of S + p.
-__device__ __forceinline__ void comp_mac(float mh, float ml, float ch, float cl, float& S, float& C) {
-  const float p = __fmul_rn(mh, ch);
-  float e = __fmaf_rn(mh, ch, -p);
-  e = __fmaf_rn(mh, cl, e);
-  e = __fmaf_rn(ml, ch, e);
-  const df32 sm = df_two_sum(S, p);
-  S = sm.hi;
-  C = __fadd_rn(C, __fadd_rn(sm.lo, e));
+// Packed FP32 pairs (sm_100+ f32x2 instructions): the real and imaginary
+// parts of a coefficient travel together, two IEEE round-to-nearest
+// operations per instruction, bit-identical to the scalar forms.
+using f32x2 = unsigned long long;
+__device__ __forceinline__ f32x2 pk(float lo, float hi) {
+  f32x2 d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+__device__ __forceinline__ void upk(f32x2 v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// S + C += (mh + ml)(ch + cl) for a (re, im) pair, compensated: p - ne' is
+// mh ch exactly (ne' = -(mh ch - p) from one FMA with -mh), the cross terms
+// join it (still negated), TwoSum keeps the rounding error of S + p.
+// nmh = -mh, nml = -ml.
+__device__ __forceinline__ void comp_mac2(f32x2 mh, f32x2 nmh, f32x2 nml, f32x2 ch, f32x2 cl, f32x2& S,
+                                          f32x2& C) {
+  const f32x2 p = mul2(mh, ch);
+  f32x2 ne = fma2(nmh, ch, p);
+  ne = fma2(nmh, cl, ne);
+  ne = fma2(nml, ch, ne);
+  const f32x2 s = add2(S, p);
+  const f32x2 bb = sub2(s, S);
+  const f32x2 err = add2(sub2(S, sub2(s, bb)), sub2(p, bb));
+  S = s;
+  C = add2(C, sub2(err, ne));
 }
 
 // Rows of one pass of k_inc_solve for NM staged modes: thread t owns row t of
@@ -145,9 +183,9 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
     const int roff = b == 0 ? 0 : b == 1 ? nev : b == 2 ? NZ : NZ + new_;
     const float2* Mb = Mg + boff + row;
     const float* Xb = Xg + boff + row;
-    float S[NM][2], C[NM][2], A[NM][2];
+    f32x2 S[NM], C[NM], A[NM];  // (re, im) pairs
 #pragma unroll
-    for (int q = 0; q < NM; ++q) S[q][0] = S[q][1] = C[q][0] = C[q][1] = A[q][0] = A[q][1] = 0.f;
+    for (int q = 0; q < NM; ++q) S[q] = C[q] = A[q] = 0ull;
     // columns c < r0 of X meet the zero wall entries of the staged rhs
     float2 ma[CB];
     float xa[CB];
@@ -156,6 +194,8 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
       ma[u] = u < n ? __ldg(Mb + (size_t)u * n) : make_float2(0.f, 0.f);
       xa[u] = u < n ? __ldg(Xb + (size_t)u * n) : 0.f;
     }
+    const f32x2* Cs2 = reinterpret_cast<const f32x2*>(Cs);  // (hr, hi), (lr, li) per entry
+    const f32x2* Rs2 = reinterpret_cast<const f32x2*>(Rs);
     for (int c0 = 0; c0 < n; c0 += CB) {
       float2 mb[CB];
       float xb[CB];
@@ -168,15 +208,13 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
 #pragma unroll
       for (int u = 0; u < CB; ++u) {
         if (c0 + u < n) {
+          const f32x2 mh = pk(ma[u].x, ma[u].x), nmh = pk(-ma[u].x, -ma[u].x), nml = pk(-ma[u].y, -ma[u].y);
+          const f32x2 xx = pk(xa[u], xa[u]);
 #pragma unroll
           for (int q = 0; q < NM; ++q) {
             const int si = q * 2 * NZ + roff + c0 + u;
-            const CoefHL cc = Cs[si];
-            const float2 rr = Rs[si];
-            comp_mac(ma[u].x, ma[u].y, cc.hr, cc.lr, S[q][0], C[q][0]);
-            comp_mac(ma[u].x, ma[u].y, cc.hi, cc.li, S[q][1], C[q][1]);
-            A[q][0] = __fmaf_rn(xa[u], rr.x, A[q][0]);
-            A[q][1] = __fmaf_rn(xa[u], rr.y, A[q][1]);
+            comp_mac2(mh, nmh, nml, Cs2[2 * si], Cs2[2 * si + 1], S[q], C[q]);
+            A[q] = fma2(xx, Rs2[si], A[q]);
           }
         }
       }
@@ -191,13 +229,17 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
 #pragma unroll
     for (int q = 0; q < NM; ++q) {
       const cd c0 = Cd[q * 2 * NZ + roff + row];
+      float Sv[2], Cv[2], Av[2];
+      upk(S[q], Sv[0], Sv[1]);
+      upk(C[q], Cv[0], Cv[1]);
+      upk(A[q], Av[0], Av[1]);
       double x[2];
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         // delta = S + A + C as a double-float, then x = c + delta with two
         // FP64 additions (the float -> double moves are integer operations)
-        const df32 t = df_two_sum(S[q][k], A[q][k]);
-        const df32 dd = df_fast_two_sum(t.hi, __fadd_rn(t.lo, C[q][k]));
+        const df32 t = df_two_sum(Sv[k], Av[k]);
+        const df32 dd = df_fast_two_sum(t.hi, __fadd_rn(t.lo, Cv[k]));
         x[k] = ((k == 0 ? c0.re : c0.im) + bits::widen(dd.hi)) + bits::widen(dd.lo);
       }
       dst[(size_t)j * modes + s_mode[q]] = cd{x[0], x[1]};
@@ -416,6 +458,7 @@ int launch_solve_mixed(Handle* h) {
                                                    h->f[F_W], h->incm, h->incx, h->sl, h->group_start,
                                                    h->group_modes, d, (float)(1.5 * dt), (float)(0.5 * dt));
     prof_end(h, K_INC_SOLVE, ev);
+    if (h->after_inc && !cuda_ok(h, cudaEventRecord(h->after_inc, st), "increment solve event")) return CHF_E_CUDA;
   }
   {
     prof_begin(h, K_INC_RECOVER, &ev);

@@ -121,6 +121,25 @@ int chf_solve(chf_handle* h);
  * on, or when the stream is already under capture by the caller. */
 int chf_step(chf_handle* h, int nsteps);
 
+/* nsteps iterations of the main loop body (poiseuilleflow.f90:219-474) on
+ * host-resident module arrays, updated in place: the reference driver's
+ * step, whose arrays live in host memory.  Blocking.  Equivalent to
+ * chf_upload_state + chf_step(nsteps) + chf_download_state on the same
+ * arrays (bit-identical results), with the copies overlapped with the
+ * computation: the N^{n-1} histories upload during the first nonlinear term,
+ * the new histories and (mixed path) vnp1 / omegaynp1 download during the
+ * last solve.  Every pointer is required (CHF_E_INVALID otherwise); page-
+ * locked host memory gives the full link bandwidth.  Steps launch directly
+ * (no CUDA graph). */
+int chf_step_host(chf_handle* h, int nsteps,
+                  double* vnp1, double* omegaynp1,
+                  double* unp1, double* wnp1,
+                  double* omegaxnp1, double* omegaznp1,
+                  double* rhsvn, double* rhsomegayn,
+                  double* clamb1n, double* clamb1nm1,
+                  double* clamb3n, double* clamb3nm1,
+                  double* au0, double* w0);
+
 int chf_synchronize(chf_handle* h);
 
 /* Diagnostics of the current state (synchronous). */
