@@ -136,6 +136,8 @@ static void release(chf_handle* h) {
   for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
   for (cudaEvent_t e : {h->ev_ready, h->ev_inputs, h->ev_hist_in, h->ev_nonlinear, h->ev_vg, h->ev_done})
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->ev_field)
+    if (e) cudaEventDestroy(e);
   if (h->copy_in) cudaStreamDestroy(h->copy_in);
   if (h->copy_out) cudaStreamDestroy(h->copy_out);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -304,6 +306,8 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
     return fail(CHF_E_CUDA);
   for (cudaEvent_t* e : {&h->ev_ready, &h->ev_inputs, &h->ev_hist_in, &h->ev_nonlinear, &h->ev_vg, &h->ev_done})
     if (!cuda_ok(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate")) return fail(CHF_E_CUDA);
+  for (cudaEvent_t& e : h->ev_field)
+    if (!cuda_ok(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate")) return fail(CHF_E_CUDA);
   h->kernels_per_step = cfg->precision == CHF_MIXED ? 13 : 6;
   if (!cuda_ok(h, cudaStreamSynchronize(h->stream), "create sync")) return fail(CHF_E_CUDA);
   *out = h;
@@ -417,9 +421,10 @@ static int check_status(chf_handle* h);
 
 // One blocking call that advances host-resident module arrays in place:
 // upload, nsteps steps, download, with the copies overlapped with the steps.
-//   copy_in : the six nonlinear inputs and the mean arrays (the first
-//             nonlinear term waits for them), then the N^{n-1} histories
-//             (only the solve reads them: they land during the nonlinear term);
+//   copy_in : the mean arrays and the six nonlinear inputs, one event per
+//             field (the mixed path's first stages run field by field as
+//             they land), then the N^{n-1} histories (only the solve reads
+//             them: they land during the nonlinear term);
 //   copy_out: after the last nonlinear term, the new histories (during the
 //             solve); after the mixed path's increment solve, v and omega_y
 //             (during the recovery); at the end u, w, omega_x, omega_z and the
@@ -466,18 +471,25 @@ int chf_step_host(chf_handle* h, int nsteps, double* vnp1, double* omegaynp1, do
   };
   // the device buffers may still be in use by earlier work on the handle's stream
   if (!ev_rec(h, h->ev_ready, S) || !ev_wait(h, ci, h->ev_ready) || !ev_wait(h, co, h->ev_ready)) return CHF_E_CUDA;
-  for (int i : {F_U, F_V, F_W, F_OX, F_OY, F_OZ})
-    if (!up(h->f[i], fh[i], fb)) return CHF_E_CUDA;
   for (int i = 0; i < M_COUNT; ++i)
     if (!up(h->mean[i], mh[i], mb)) return CHF_E_CUDA;
+  {
+    const int order[6] = {F_U, F_V, F_W, F_OX, F_OY, F_OZ};
+    for (int k = 0; k < 6; ++k)
+      if (!up(h->f[order[k]], fh[order[k]], fb) || !ev_rec(h, h->ev_field[k], ci)) return CHF_E_CUDA;
+  }
   if (!ev_rec(h, h->ev_inputs, ci)) return CHF_E_CUDA;
   if (!up(h->f[F_RV], fh[F_RV], fb) || !up(h->f[F_RG], fh[F_RG], fb) || !ev_rec(h, h->ev_hist_in, ci))
     return CHF_E_CUDA;
   h->uploaded = true;
-  if (!ev_wait(h, S, h->ev_inputs)) return CHF_E_CUDA;
+  // the mixed path's first stages follow the fields as they land
+  if (!mixed && !ev_wait(h, S, h->ev_inputs)) return CHF_E_CUDA;
+  if (mixed) {  // the mean arrays precede the fields on the copy stream
+    if (!ev_wait(h, S, h->ev_field[0])) return CHF_E_CUDA;
+  }
   for (int s = 0; s < nsteps; ++s) {
     const bool last = s == nsteps - 1;
-    int rc = mixed ? launch_nonlinear_mixed(h) : launch_nonlinear_fp64(h);
+    int rc = mixed ? launch_nonlinear_mixed(h, s == 0 ? h->ev_field : nullptr) : launch_nonlinear_fp64(h);
     if (rc != CHF_OK) return rc;
     if (s == 0 && !ev_wait(h, S, h->ev_hist_in)) return CHF_E_CUDA;
     if (last) {  // the new histories are final; the host buffers were read by the upload

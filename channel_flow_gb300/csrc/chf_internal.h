@@ -148,6 +148,7 @@ struct Handle {
   cudaEvent_t ev_ready = nullptr, ev_inputs = nullptr, ev_hist_in = nullptr, ev_nonlinear = nullptr,
               ev_vg = nullptr, ev_done = nullptr;
   cudaEvent_t after_inc = nullptr;
+  cudaEvent_t ev_field[6] = {};  // the six nonlinear inputs landed (u, v, w, omega_x, omega_y, omega_z)
 
   // chf_step replays a CUDA graph of two steps.  Each step exchanges the
   // history buffers by pointer (f[F_U] <-> f[F_RV], f[F_W] <-> f[F_RG]), so
@@ -210,12 +211,18 @@ template <typename InT>
 int launch_tc_split_fx(Handle* h, const FxPlan& p, const Ptr8<const InT>& ins, int kvalid, uint8_t* bimg,
                        int* bexp, int nfields, int kid);
 int setup_mixed(Handle* h);
-int launch_nonlinear_mixed(Handle* h);
+// field_ready (optional): six events, one per nonlinear input in the order
+// u, v, w, omega_x, omega_y, omega_z; when given, each field's share of the
+// first stages waits for its own event only (chf_step_host's upload)
+int launch_nonlinear_mixed(Handle* h, const cudaEvent_t* field_ready = nullptr);
 // one time step (getnonlinear + solve) on h->stream (chf_api.cu)
 int step_once(Handle* h);
 // launchers (k_solve.cu)
 int setup_solver(Handle* h);
 int setup_solver_mixed(Handle* h);
+bool xy_register_path(const Dims& d);
+int launch_yinv_fields(Handle* h, cf* wz, cf* wy, const cf* tw_py, int f0, int nf);
+int launch_xprod_yfwd(Handle* h, cf* wz, cf* wy, const cf* tw_py, const cf* tw_px);
 int launch_solve_fp64(Handle* h);
 int launch_solve_mean(Handle* h, cudaStream_t st);  // the (0,0) mode alone, on st
 int launch_solve_mixed(Handle* h);  // k_solve_mixed.cu

@@ -242,7 +242,7 @@ int setup_mixed(Handle* h) {
   return CHF_OK;
 }
 
-int launch_nonlinear_mixed(Handle* h) {
+int launch_nonlinear_mixed(Handle* h, const cudaEvent_t* field_ready) {
   const Dims& d = h->d;
   const long modes = d.modes(), cols = 2 * modes;
   int rc;
@@ -250,15 +250,38 @@ int launch_nonlinear_mixed(Handle* h) {
   Ptr8<const double> in6{};
   const int order[6] = {F_U, F_V, F_W, F_OX, F_OY, F_OZ};
   for (int i = 0; i < 6; ++i) in6.p[i] = reinterpret_cast<const double*>(h->f[order[i]]);
-  if ((rc = launch_tc_split_fx<double>(h, h->tz1, in6, d.NZ, h->bimg, h->bexp, 6, K_SPLIT_Z1)) != CHF_OK)
-    return rc;
   Ptr8<float> o6{};
   for (int i = 0; i < 6; ++i) o6.p[i] = reinterpret_cast<float*>(h->wz32 + (size_t)i * d.MP * modes);
-  if ((rc = launch_tc_gemm_fx<float>(h, h->tz1, h->az1, h->aexp1, h->bimg, h->bexp, o6, 6, cols,
-                                     K_GEMM_Z1)) != CHF_OK)
-    return rc;
-  // y and x transforms with the products, FP32
-  if ((rc = launch_xy<float>(h, h->wz32, h->wy32, h->twf_py, h->twf_px)) != CHF_OK) return rc;
+  if (field_ready && xy_register_path(d)) {
+    // field by field as the inputs land: digits, product-grid values and the
+    // inverse y transform of field i need field i only
+    for (int i = 0; i < 6; ++i) {
+      if (!cuda_ok(h, cudaStreamWaitEvent(h->stream, field_ready[i], 0), "field wait")) return CHF_E_CUDA;
+      Ptr8<const double> in1{};
+      in1.p[0] = in6.p[i];
+      Ptr8<float> o1{};
+      o1.p[0] = o6.p[i];
+      uint8_t* bimg = h->bimg + (size_t)i * h->tz1.b_field_bytes();
+      int* bexp = h->bexp + (size_t)i * h->tz1.bexp_stride();
+      if ((rc = launch_tc_split_fx<double>(h, h->tz1, in1, d.NZ, bimg, bexp, 1, K_SPLIT_Z1)) != CHF_OK ||
+          (rc = launch_tc_gemm_fx<float>(h, h->tz1, h->az1, h->aexp1, bimg, bexp, o1, 1, cols, K_GEMM_Z1)) !=
+              CHF_OK ||
+          (rc = launch_yinv_fields(h, h->wz32, h->wy32, h->twf_py, i, 1)) != CHF_OK)
+        return rc;
+    }
+    if ((rc = launch_xprod_yfwd(h, h->wz32, h->wy32, h->twf_py, h->twf_px)) != CHF_OK) return rc;
+  } else {
+    if (field_ready)
+      for (int i = 0; i < 6; ++i)
+        if (!cuda_ok(h, cudaStreamWaitEvent(h->stream, field_ready[i], 0), "field wait")) return CHF_E_CUDA;
+    if ((rc = launch_tc_split_fx<double>(h, h->tz1, in6, d.NZ, h->bimg, h->bexp, 6, K_SPLIT_Z1)) != CHF_OK)
+      return rc;
+    if ((rc = launch_tc_gemm_fx<float>(h, h->tz1, h->az1, h->aexp1, h->bimg, h->bexp, o6, 6, cols,
+                                       K_GEMM_Z1)) != CHF_OK)
+      return rc;
+    // y and x transforms with the products, FP32
+    if ((rc = launch_xy<float>(h, h->wz32, h->wy32, h->twf_py, h->twf_px)) != CHF_OK) return rc;
+  }
   // z: values -> coefficients 0..N
   Ptr8<const float> in3{};
   for (int i = 0; i < 3; ++i) in3.p[i] = reinterpret_cast<const float*>(h->wz32 + (size_t)i * d.MP * modes);

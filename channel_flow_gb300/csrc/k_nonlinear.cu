@@ -657,32 +657,54 @@ int run_zcurl(Handle* h) {
 
 }  // namespace
 
+// The FP32 register-FFT path of the x/y transforms, in two parts so that a
+// caller can run the inverse y transform field by field (fields f0 ..
+// f0 + nf - 1 of the six) and the products and forward transforms once.
+bool xy_register_path(const Dims& d) { return d.PX == 192 && d.PY == 192 && d.KX % YCols<float>::value == 0; }
+
+int launch_yinv_fields(Handle* h, cf* wz, cf* wy, const cf* tw_py, int f0, int nf) {
+  const Dims& d = h->d;
+  constexpr int YC = YCols<float>::value;
+  cudaEvent_t ev;
+  prof_begin(h, K_YINV, &ev);
+  k_yinv_w<float><<<dim3(d.KX / YC, d.MP, nf), YC * 32, 0, h->stream>>>(
+      wz + (size_t)f0 * d.MP * d.modes(), wy + (size_t)f0 * d.MP * d.PY * d.KX, d, tw_py);
+  prof_end(h, K_YINV, ev);
+  return cuda_ok(h, cudaGetLastError(), "k_yinv_w") ? CHF_OK : CHF_E_CUDA;
+}
+
+int launch_xprod_yfwd(Handle* h, cf* wz, cf* wy, const cf* tw_py, const cf* tw_px) {
+  const Dims& d = h->d;
+  constexpr int YC = YCols<float>::value;
+  cudaStream_t st = h->stream;
+  cudaEvent_t ev;
+  const long nrows = (long)d.MP * d.PY;
+  prof_begin(h, K_XPROD, &ev);
+  k_xprod_w<float><<<(unsigned)((nrows + W_WARPS - 1) / W_WARPS), W_WARPS * 32, 0, st>>>(
+      wy, nrows, (size_t)d.MP * d.PY * d.KX, (float)h->cfg.re_p, tw_px);
+  prof_end(h, K_XPROD, ev);
+  if (!cuda_ok(h, cudaGetLastError(), "k_xprod_w")) return CHF_E_CUDA;
+  const float scale = (float)(1.0 / ((double)d.PX * (double)d.PY));
+  prof_begin(h, K_YFWD, &ev);
+  k_yfwd_w<float><<<dim3(d.KX / YC, d.MP, 3), YC * 32, 0, st>>>(wy, wz, d, tw_py, scale);
+  prof_end(h, K_YFWD, ev);
+  return cuda_ok(h, cudaGetLastError(), "k_yfwd_w") ? CHF_OK : CHF_E_CUDA;
+}
+
 template <typename T>
 int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const cplx<T>* tw_px) {
   const Dims& d = h->d;
   cudaStream_t st = h->stream;
-  if (sizeof(T) == 4 && d.PX == 192 && d.PY == 192 && d.KX % YCols<T>::value == 0) {
+  if (sizeof(T) == 4 && xy_register_path(d)) {
     // register-FFT specialisation of the 128-point directions, FP32 only: in
     // FP64 (the FP64 pipe is the bound) the cross-lane radix-2 network costs
     // more FP64 instructions than the radix-4 shared-memory stages below
-    cudaEvent_t ev;
-    prof_begin(h, K_YINV, &ev);
-    constexpr int YC = YCols<T>::value;
-    k_yinv_w<T><<<dim3(d.KX / YC, d.MP, 6), YC * 32, 0, st>>>(wz, wy, d, tw_py);
-    prof_end(h, K_YINV, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_yinv_w")) return CHF_E_CUDA;
-    const long nrows = (long)d.MP * d.PY;
-    prof_begin(h, K_XPROD, &ev);
-    k_xprod_w<T><<<(unsigned)((nrows + W_WARPS - 1) / W_WARPS), W_WARPS * 32, 0, st>>>(
-        wy, nrows, (size_t)d.MP * d.PY * d.KX, (T)h->cfg.re_p, tw_px);
-    prof_end(h, K_XPROD, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_xprod_w")) return CHF_E_CUDA;
-    const T scale = (T)(1.0 / ((double)d.PX * (double)d.PY));
-    prof_begin(h, K_YFWD, &ev);
-    k_yfwd_w<T><<<dim3(d.KX / YC, d.MP, 3), YC * 32, 0, st>>>(wy, wz, d, tw_py, scale);
-    prof_end(h, K_YFWD, ev);
-    if (!cuda_ok(h, cudaGetLastError(), "k_yfwd_w")) return CHF_E_CUDA;
-    return CHF_OK;
+    cf* wzf = reinterpret_cast<cf*>(wz);
+    cf* wyf = reinterpret_cast<cf*>(wy);
+    const cf* twy = reinterpret_cast<const cf*>(tw_py);
+    const cf* twx = reinterpret_cast<const cf*>(tw_px);
+    const int rc = launch_yinv_fields(h, wzf, wyf, twy, 0, 6);
+    return rc == CHF_OK ? launch_xprod_yfwd(h, wzf, wyf, twy, twx) : rc;
   }
   const int kxb = pick_kxb<T>(d);
   const int xr = pick_xr<T>(d);
