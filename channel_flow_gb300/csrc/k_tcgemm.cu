@@ -287,10 +287,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
           }
           for (int k16 = 0; k16 < kc / 16; ++k16) {
             const bool first = (ch == 0 && k16 == 0);
+            // products d_i e_(L-i) in rounds over i, so that consecutive MMAs
+            // accumulate into different levels (no read-after-write on one
+            // accumulator between neighbours); each level's first MMA (i = 0)
+            // comes in round 0
 #pragma unroll
-            for (int L = 0; L < FX_LEVELS; ++L) {
+            for (int i = 0; i < FX_LEVELS; ++i) {
 #pragma unroll
-              for (int i = 0; i <= L; ++i) {
+              for (int L = i; L < FX_LEVELS; ++L) {
                 const uint32_t accum = (first && i == 0) ? 0u : 1u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
