@@ -92,15 +92,17 @@ void fx_digits_host(double x, int e, double* dg) {
 //   warp 0    producer: per K chunk of an item waits for a free stage, then
 //             moves the chunk's plane images with cp.async.bulk (completion
 //             counted in bytes on the stage's "full" barrier);
-//   warp 1    MMA issuer: waits for a free accumulator set (two sets of four
-//             64-column level accumulators, so one item's epilogue overlaps
-//             the next item's MMAs), per chunk waits for "full", issues the 10
-//             level MMAs per K16 slice (descriptors formed once per chunk,
-//             advanced by a constant per slice) and commits to the stage's
-//             "empty" barrier; after the last chunk it commits to "tfull";
-//   warps 2-9 epilogue: wait for "tfull", read the levels back with
+//   warps 1-2 MMA issuers (levels {0, 3} and {1, 2}, 5 of the 10 products
+//             each: one thread's MMA issue rate, not the tensor pipe, bounds
+//             these 128x64x16 MMAs): wait for a free accumulator set (two sets
+//             of four 64-column level accumulators, so one item's epilogue
+//             overlaps the next item's MMAs), per chunk wait for "full", issue
+//             their level MMAs per K16 slice (descriptors formed once per chunk,
+//             advanced by a constant per slice) and commit to the stage's
+//             "empty" barrier; after the last chunk they commit to "tfull";
+//   warps 3-10 epilogue: wait for "tfull", read the levels back with
 //             tcgen05.ld (warp w reads TMEM lanes 32 (w % 4) .., columns
-//             32 ((w - 2) / 4) ..), release the set on "tempty" and form the
+//             32 ((w - 3) / 4) ..), release the set on "tempty" and form the
 //             outputs from the exact 64-bit level sum.
 // Every wait is bounded (1 s of wall time); a role that times out records
 // the failure, the others see it and stop, the producer waits for its copies
@@ -110,8 +112,10 @@ void fx_digits_host(double x, int e, double* dg) {
 // instruction descriptor: D = F32, A = B = BF16, both K-major, M = 128, N = 64
 constexpr uint32_t IDESC_FX = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 constexpr int WS_STAGES = 4;
+constexpr int WS_MMA_WARPS = 2;  // issuers: levels {0, 3} and {1, 2}, 5 products each
 constexpr int WS_EPI_WARPS = 8;
-constexpr int WS_THREADS = 64 + 32 * WS_EPI_WARPS;
+constexpr int WS_EPI0 = 1 + WS_MMA_WARPS;  // first epilogue warp
+constexpr int WS_THREADS = 32 * (WS_EPI0 + WS_EPI_WARPS);
 constexpr uint32_t WS_A_PLANE = 128u * TC_KC * 2u;
 constexpr uint32_t WS_B_PLANE = (uint32_t)FX_NT * TC_KC * 2u;
 constexpr uint32_t WS_B_STAGE = (uint32_t)FX_PLANES * WS_B_PLANE;
@@ -175,7 +179,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
                                                               const __grid_constant__ Ptr8<OutT> outs,
                                                               size_t ldc, int nfields, int* status) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t full[WS_STAGES], empty[WS_STAGES], tfull[2], tempty[2], drain, abar;
+  __shared__ __align__(8) uint64_t full[WS_STAGES], empty[WS_STAGES], tfull[2], tempty[2], drain[WS_MMA_WARPS], abar;
   __shared__ uint32_t tmem_base;
   __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -191,13 +195,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
     s_fail = 0;
     for (int i = 0; i < WS_STAGES; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&empty[i])), "r"(WS_MMA_WARPS));
     }
     for (int i = 0; i < 2; ++i) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&tfull[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tfull[i])), "r"(WS_MMA_WARPS));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tempty[i])), "r"(32 * WS_EPI_WARPS));
     }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&drain)));
+    for (int i = 0; i < WS_MMA_WARPS; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&drain[i])));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&abar)));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
@@ -248,8 +253,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
         if (!mbar_wait(smem_u32(&full[k % WS_STAGES]), (k / WS_STAGES) & 1u)) *fail = 6;
       if (resident && !mbar_wait(smem_u32(&abar), 0)) *fail = 7;
     }
-  } else if (warp == 1) {
-    // ---------------- MMA issuer ----------------
+  } else if (warp < WS_EPI0) {
+    // ---------------- MMA issuers ----------------
+    // issuer 0 owns the level-0 and level-3 accumulators, issuer 1 levels 1
+    // and 2: disjoint accumulators, 5 products per K16 slice each
+    const int mw = warp - 1;
     if (lane == 0) {
       // K-adjacent core matrices: 16 (A, 128 rows) or 8 (B, 64 columns)
       // groups of 8 rows x 16 bytes apart; adjacent 8-row groups 128 B apart.
@@ -295,6 +303,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
             for (int i = 0; i < FX_LEVELS; ++i) {
 #pragma unroll
               for (int L = i; L < FX_LEVELS; ++L) {
+                if ((L == 0 || L == 3) != (mw == 0)) continue;
                 const uint32_t accum = (first && i == 0) ? 0u : 1u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -313,13 +322,13 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
         mma_commit(smem_u32(&tfull[b]));
       }
       // every MMA this thread issued has completed once "drain" arrives
-      mma_commit(smem_u32(&drain));
-      if (!mbar_wait(smem_u32(&drain), 0)) *fail = 4;
+      mma_commit(smem_u32(&drain[mw]));
+      if (!mbar_wait(smem_u32(&drain[mw]), 0)) *fail = 4;
     }
   } else {
     // ---------------- epilogue ----------------
     const int q = warp & 3;                     // the TMEM lane quarter this warp may access
-    const int cbase = 32 * ((warp - 2) / 4);    // its 32 of the 64 columns
+    const int cbase = 32 * ((warp - WS_EPI0) / 4);  // its 32 of the 64 columns
     const int row = q * 32 + lane;
     const int m = mt * 128 + row;
     const bool mrow = m < plan.mvalid;
