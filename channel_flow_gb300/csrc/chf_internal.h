@@ -129,6 +129,10 @@ struct Handle {
   uint8_t* bimg = nullptr;    // per-step B images
   int *aexp1 = nullptr, *aexp2 = nullptr, *aexp3 = nullptr;  // row exponents of the A images
   int* bexp = nullptr;        // per-step column exponents of the fixed-point B images
+  // row N of the Z2 and GL transforms (their GEMMs cover rows 0..N-1): the
+  // rows' digit planes [4][kpad] and exponents
+  float *z2_tail = nullptr, *gl_tail = nullptr;
+  int z2_tail_exp = 0, gl_tail_exp = 0;
   size_t bimg_bytes = 0;
   cf* wz32 = nullptr;         // 6 x [MP][KY][KX]
   cf* wy32 = nullptr;         // 6 x [MP][PY][KX]
@@ -207,9 +211,18 @@ std::vector<uint8_t> make_a_image_fx(const FxPlan& p, const std::vector<double>&
 template <typename OutT>
 int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int* aexp, const uint8_t* bimg,
                       const int* bexp, const Ptr8<OutT>& outs, int nfields, size_t ldc, int kid);
+// One GEMM output row computed beside the split instead of by an extra row
+// tile: the row's digit planes (device, plane-major, kpad each), its exponent,
+// and per field the FP64 destination of the row.
+struct FxTail {
+  const float* adig = nullptr;
+  int aexp = 0;
+  Ptr8<double> out{};
+};
+std::vector<float> a_row_digits(const FxPlan& p, const std::vector<double>& a, int K, int row, int& row_exp);
 template <typename InT>
 int launch_tc_split_fx(Handle* h, const FxPlan& p, const Ptr8<const InT>& ins, int kvalid, uint8_t* bimg,
-                       int* bexp, int nfields, int kid);
+                       int* bexp, int nfields, int kid, const FxTail& tail = FxTail{});
 int setup_mixed(Handle* h);
 // field_ready (optional): six events, one per nonlinear input in the order
 // u, v, w, omega_x, omega_y, omega_z; when given, each field's share of the

@@ -50,14 +50,17 @@ constexpr int CURL_THREADS = 32;  // (mode, re/im) columns per CTA in k_curl
 // (descending k, 6 FP64 operations per element, CURL_PF rows of H loaded
 // ahead) rounds h_v, h_g to FP32 by integer operations into hs and finds the
 // column maxima (their powers of two); pass 2 writes the digits, 8 rows per
-// 16-byte store.
+// 16-byte store, and forms the GL row N (the wall z = -1) exactly as the GEMM
+// would, which then covers the points 0..N-1 only.
 constexpr int CURL_PF = 8;  // rows of H loaded ahead of the recurrence
 
 __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict__ lc,
                                                        const double* __restrict__ iapha,
                                                        const double* __restrict__ ibeta, Dims d,
                                                        const __grid_constant__ FxPlan plan, float* __restrict__ hs,
-                                                       uint8_t* __restrict__ bimg, int* __restrict__ bexp) {
+                                                       uint8_t* __restrict__ bimg, int* __restrict__ bexp,
+                                                       const float* __restrict__ gl_tail, int gl_tail_exp,
+                                                       double* __restrict__ glv_n, double* __restrict__ glg_n) {
   const long modes = d.modes(), ncols = 2 * modes;
   const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncols) return;
@@ -113,8 +116,10 @@ __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict_
   if (mg > 0.f) (void)frexpf(mg, &e[1]);
   bexp[col] = e[0];
   bexp[plan.bexp_stride() + col] = e[1];
-  // pass 2: digits, groups of 8 rows (rows >= NZ are zero)
+  // pass 2: digits, groups of 8 rows (rows >= NZ are zero), and the level
+  // sums of the GL row N (the wall z = -1), which the GL GEMM leaves out
   const int nt = (int)(col / FX_NT), r = (int)(col % FX_NT);
+  float lev[2][FX_PLANES] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
   for (int g = 0; g < plan.kpad / 8; ++g) {
     const int ch = (8 * g) / TC_KC, kl = 8 * g - ch * TC_KC;
     const uint32_t pbytes = (uint32_t)FX_NT * plan.kc[ch] * 2u;
@@ -130,6 +135,7 @@ __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict_
         tc::fx_digits_f(x, e[f], dg);
 #pragma unroll
         for (int i = 0; i < FX_PLANES; ++i) hd[i][q] = tc::bf16_bits(dg[i]);
+        tc::fx_tail_mac(gl_tail, plan.kpad, k, dg, lev[f]);
       }
       uint8_t* base = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes + plan.b_chunk_off[ch];
 #pragma unroll
@@ -143,6 +149,8 @@ __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict_
       }
     }
   }
+  glv_n[col] = tc::fx_tail_value(lev[0], gl_tail_exp + e[0] - 35);
+  glg_n[col] = tc::fx_tail_value(lev[1], gl_tail_exp + e[1] - 35);
 }
 
 // (0,0)-mode histories: the GL GEMM left the GL values of H1(0,0), H3(0,0)
@@ -182,9 +190,13 @@ int setup_mixed(Handle* h) {
   // z transforms with exact accumulation (fixed-point digits, k_tcgemm.cu);
   // the GL evaluation of h_v, h_g is not differentiated afterwards and keeps
   // the floating bf16x3 split
+  // Z2 and GL cover rows 0..N-1 (one 128-row tile for nnz = 128): row N, the
+  // last coefficient / the wall point z = -1, is formed beside the digits by
+  // k_tc_split_fx and k_curl with the same exact level sums, instead of by a
+  // second row tile of MMAs
   h->tz1 = make_fx_plan(MP, NZ, cols);
-  h->tz2 = make_fx_plan(NZ, MP, cols);
-  h->tgl = make_fx_plan(NZ, NZ, cols);
+  h->tz2 = make_fx_plan(N, MP, cols);
+  h->tgl = make_fx_plan(N, NZ, cols);
   std::vector<double> a1((size_t)MP * NZ), a2((size_t)NZ * MP), a3((size_t)NZ * NZ);
   for (int p = 0; p < MP; ++p)
     for (int n = 0; n < NZ; ++n) a1[(size_t)p * NZ + n] = cospi_ratio((long)n * p, MZ);
@@ -207,11 +219,20 @@ int setup_mixed(Handle* h) {
     return cuda_ok(h, cudaMemcpy(*dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice), what);
   };
   if (!upload(&h->az1, make_a_image_fx(h->tz1, a1, MP, NZ, e1), "A image z1") ||
-      !upload(&h->az2, make_a_image_fx(h->tz2, a2, NZ, MP, e2), "A image z2") ||
-      !upload(&h->agl, make_a_image_fx(h->tgl, a3, NZ, NZ, e3), "A image gl") ||
+      !upload(&h->az2, make_a_image_fx(h->tz2, a2, N, MP, e2), "A image z2") ||
+      !upload(&h->agl, make_a_image_fx(h->tgl, a3, N, NZ, e3), "A image gl") ||
       !upload_int(&h->aexp1, e1, "A exponents z1") || !upload_int(&h->aexp2, e2, "A exponents z2") ||
       !upload_int(&h->aexp3, e3, "A exponents gl"))
     return CHF_E_NOMEM;
+  {  // row N of Z2 and GL as digit planes, computed beside the split / curl
+    auto up_digits = [h](float** dst, const std::vector<float>& v, const char* what) {
+      if (!cuda_ok(h, cudaMalloc((void**)dst, sizeof(float) * v.size()), what)) return false;
+      return cuda_ok(h, cudaMemcpy(*dst, v.data(), sizeof(float) * v.size(), cudaMemcpyHostToDevice), what);
+    };
+    if (!up_digits(&h->z2_tail, a_row_digits(h->tz2, a2, MP, N, h->z2_tail_exp), "z2 row N") ||
+        !up_digits(&h->gl_tail, a_row_digits(h->tgl, a3, NZ, N, h->gl_tail_exp), "GL row N"))
+      return CHF_E_CUDA;
+  }
   if (!cuda_ok(h, cudaMalloc((void**)&h->bexp,
                             sizeof(int) * 6 * std::max(h->tz1.bexp_stride(), h->tz2.bexp_stride())),
                "B exponents"))
@@ -285,10 +306,17 @@ int launch_nonlinear_mixed(Handle* h, const cudaEvent_t* field_ready) {
   // z: values -> coefficients 0..N
   Ptr8<const float> in3{};
   for (int i = 0; i < 3; ++i) in3.p[i] = reinterpret_cast<const float*>(h->wz32 + (size_t)i * d.MP * modes);
-  if ((rc = launch_tc_split_fx<float>(h, h->tz2, in3, d.MP, h->bimg, h->bexp, 3, K_SPLIT_Z2)) != CHF_OK)
+  Ptr8<double> o3{}, row_n{};
+  for (int i = 0; i < 3; ++i) {
+    o3.p[i] = h->lc64 + (size_t)i * d.NZ * cols;
+    row_n.p[i] = o3.p[i] + (size_t)d.N * cols;
+  }
+  FxTail tail;
+  tail.adig = h->z2_tail;
+  tail.aexp = h->z2_tail_exp;
+  tail.out = row_n;
+  if ((rc = launch_tc_split_fx<float>(h, h->tz2, in3, d.MP, h->bimg, h->bexp, 3, K_SPLIT_Z2, tail)) != CHF_OK)
     return rc;
-  Ptr8<double> o3{};
-  for (int i = 0; i < 3; ++i) o3.p[i] = h->lc64 + (size_t)i * d.NZ * cols;
   if ((rc = launch_tc_gemm_fx<double>(h, h->tz2, h->az2, h->aexp2, h->bimg, h->bexp, o3, 3, cols,
                                       K_GEMM_Z2)) != CHF_OK)
     return rc;
@@ -299,7 +327,9 @@ int launch_nonlinear_mixed(Handle* h, const cudaEvent_t* field_ready) {
     // FP32 scratch for h_v, h_g: the product-grid buffer, free once the z2
     // digits are formed (2 NZ <= 6 MP rows of modes complex values)
     k_curl<<<(unsigned)((cols + CURL_THREADS - 1) / CURL_THREADS), CURL_THREADS, 0, h->stream>>>(
-        h->lc64, h->iapha, h->ibeta, d, h->tgl, reinterpret_cast<float*>(h->wz32), h->bimg, h->bexp);
+        h->lc64, h->iapha, h->ibeta, d, h->tgl, reinterpret_cast<float*>(h->wz32), h->bimg, h->bexp,
+        h->gl_tail, h->gl_tail_exp, reinterpret_cast<double*>(h->f[F_U]) + (size_t)d.N * cols,
+        reinterpret_cast<double*>(h->f[F_W]) + (size_t)d.N * cols);
     prof_end(h, K_CURL32, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_curl")) return CHF_E_CUDA;
   }

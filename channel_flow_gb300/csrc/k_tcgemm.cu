@@ -410,10 +410,16 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
 // at a time as one 16-byte store per plane (consecutive threads fill
 // consecutive core-matrix rows).  grid (ntiles, 1, nfields), FX_NT threads.
 // ---------------------------------------------------------------------------
+// tail (optional): one more output row that the GEMM's plan leaves out,
+// computed exactly as the GEMM would (the row's digit planes tail.adig, its
+// exponent tail.aexp; levels i + j <= 3 summed exactly in FP32, combined in
+// 64 bits) from the column's digits formed in the second pass, written as
+// FP64 to tail.out.p[f][col].
 template <typename InT>
 __global__ void __launch_bounds__(FX_NT) k_tc_split_fx(const __grid_constant__ FxPlan plan,
                                                        const __grid_constant__ Ptr8<const InT> ins, int kvalid,
-                                                       uint8_t* __restrict__ bimg, int* __restrict__ bexp) {
+                                                       uint8_t* __restrict__ bimg, int* __restrict__ bexp,
+                                                       const __grid_constant__ FxTail tail) {
   const int nt = blockIdx.x, f = blockIdx.z, r = threadIdx.x;
   const InT* in = ins.p[f];
   const long col = (long)nt * FX_NT + r;
@@ -421,6 +427,7 @@ __global__ void __launch_bounds__(FX_NT) k_tc_split_fx(const __grid_constant__ F
   float mx = 0.f;
   if (live)
     for (int k = 0; k < kvalid; ++k) mx = fmaxf(mx, fabsf((float)in[(size_t)k * plan.ncols + col]));
+  float lev[FX_PLANES] = {0.f, 0.f, 0.f, 0.f};
   int e = 0;
   if (mx > 0.f) (void)frexpf(mx, &e);  // mx = m 2^e, m in [0.5, 1)
   bexp[(size_t)f * plan.bexp_stride() + col] = e;
@@ -435,6 +442,7 @@ __global__ void __launch_bounds__(FX_NT) k_tc_split_fx(const __grid_constant__ F
       fx_digits_f(x, e, dg);
 #pragma unroll
       for (int i = 0; i < FX_PLANES; ++i) h[i][q] = bf16_bits(dg[i]);
+      if (tail.adig) fx_tail_mac(tail.adig, plan.kpad, k, dg, lev);
     }
     const int ch = (8 * g) / TC_KC;
     const int kl = 8 * g - ch * TC_KC;
@@ -452,6 +460,7 @@ __global__ void __launch_bounds__(FX_NT) k_tc_split_fx(const __grid_constant__ F
       *reinterpret_cast<uint4*>(base + (size_t)pl * pbytes + off) = v;
     }
   }
+  if (tail.adig && live) tail.out.p[f][col] = fx_tail_value(lev, tail.aexp + e - 35);
 }
 
 FxPlan make_fx_plan(int mvalid, int kvalid, long ncols) {
@@ -510,6 +519,22 @@ std::vector<uint8_t> make_a_image_fx(const FxPlan& p, const std::vector<double>&
   return img;
 }
 
+// Host: the digit planes (plane-major, kpad each) and exponent of row `row` of a
+// dense row-major M x K double matrix, as make_a_image_fx would cut it.
+std::vector<float> a_row_digits(const FxPlan& p, const std::vector<double>& a, int K, int row, int& row_exp) {
+  double mx = 0.0;
+  for (int k = 0; k < K; ++k) mx = std::max(mx, std::fabs(a[(size_t)row * K + k]));
+  row_exp = 0;
+  if (mx > 0) (void)std::frexp(mx, &row_exp);
+  std::vector<float> dig((size_t)FX_PLANES * p.kpad, 0.f);
+  for (int k = 0; k < K; ++k) {
+    double dg[FX_PLANES];
+    fx_digits_host(a[(size_t)row * K + k], row_exp, dg);
+    for (int i = 0; i < FX_PLANES; ++i) dig[(size_t)i * p.kpad + k] = (float)dg[i];
+  }
+  return dig;
+}
+
 template <typename OutT>
 int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int* aexp, const uint8_t* bimg,
                       const int* bexp, const Ptr8<OutT>& outs, int nfields, size_t ldc, int kid) {
@@ -537,11 +562,11 @@ int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int
 
 template <typename InT>
 int launch_tc_split_fx(Handle* h, const FxPlan& p, const Ptr8<const InT>& ins, int kvalid, uint8_t* bimg,
-                       int* bexp, int nfields, int kid) {
+                       int* bexp, int nfields, int kid, const FxTail& tail) {
   dim3 grid(p.ntiles, 1, nfields);
   cudaEvent_t ev;
   prof_begin(h, kid, &ev);
-  k_tc_split_fx<InT><<<grid, FX_NT, 0, h->stream>>>(p, ins, kvalid, bimg, bexp);
+  k_tc_split_fx<InT><<<grid, FX_NT, 0, h->stream>>>(p, ins, kvalid, bimg, bexp, tail);
   prof_end(h, kid, ev);
   return cuda_ok(h, cudaGetLastError(), "k_tc_split_fx") ? CHF_OK : CHF_E_CUDA;
 }
@@ -551,8 +576,8 @@ template int launch_tc_gemm_fx<float>(Handle*, const FxPlan&, const uint8_t*, co
 template int launch_tc_gemm_fx<double>(Handle*, const FxPlan&, const uint8_t*, const int*, const uint8_t*,
                                        const int*, const Ptr8<double>&, int, size_t, int);
 template int launch_tc_split_fx<float>(Handle*, const FxPlan&, const Ptr8<const float>&, int, uint8_t*, int*,
-                                       int, int);
+                                       int, int, const FxTail&);
 template int launch_tc_split_fx<double>(Handle*, const FxPlan&, const Ptr8<const double>&, int, uint8_t*,
-                                        int*, int, int);
+                                        int*, int, int, const FxTail&);
 
 }  // namespace chf

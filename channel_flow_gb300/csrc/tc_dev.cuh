@@ -65,6 +65,27 @@ __device__ __forceinline__ void fx_digits_f(float x, int e, float* dg) {
   }
 }
 
+// one element of an extra output row: the level sums lev[L] += sum_{i+j=L}
+// a_i b_j of the row's digits a (plane-major, kpad each, at k) and the
+// column's digits b; every product and level sum is an integer below 2^24,
+// so the FP32 FMAs are exact
+__device__ __forceinline__ void fx_tail_mac(const float* __restrict__ adig, int kpad, int k, const float* b,
+                                            float* lev) {
+  const float a0 = adig[k], a1 = adig[kpad + k], a2 = adig[2 * kpad + k], a3 = adig[3 * kpad + k];
+  lev[0] = fmaf(a0, b[0], lev[0]);
+  lev[1] = fmaf(a0, b[1], fmaf(a1, b[0], lev[1]));
+  lev[2] = fmaf(a0, b[2], fmaf(a1, b[1], fmaf(a2, b[0], lev[2])));
+  lev[3] = fmaf(a0, b[3], fmaf(a1, b[2], fmaf(a2, b[1], fmaf(a3, b[0], lev[3]))));
+}
+
+// the four level sums combined exactly (t = lev0 2^21 + lev1 2^14 + lev2 2^7
+// + lev3 in 64 bits) and scaled by 2^n, exactly in FP64 (|t| < 2^46)
+__device__ __forceinline__ double fx_tail_value(const float* lev, int n) {
+  const long long t = ((long long)__float2int_rn(lev[0]) << 21) + ((long long)__float2int_rn(lev[1]) << 14) +
+                      ((long long)__float2int_rn(lev[2]) << 7) + (long long)__float2int_rn(lev[3]);
+  return (double)t * __longlong_as_double((long long)(1023 + n) << 52);
+}
+
 __device__ __forceinline__ uint16_t bf16_bits(float f) {
   return __bfloat16_as_ushort(__float2bfloat16_rn(f));  // exact: |f| <= 128, integer
 }
