@@ -128,11 +128,12 @@ def kernel_work(cfg, zpad=0, precision="fp64"):
 
     img = 4 * 2  # four bf16 planes per element
     w["k_tc_split_z1"] = (6 * NZ * cols * 8 + 6 * kp(NZ) * cols * img, 0)
-    w["k_tc_gemm_z1"] = (6 * kp(NZ) * cols * img + 6 * MP * cols * 4, 6 * 10 * 2 * 128 * cols * kp(NZ) * 2)
+    w["k_tc_gemm_z1"] = (6 * kp(NZ) * cols * img + 6 * MP * cols * 4, 6 * 10 * 2 * 256 * cols * kp(NZ))
     w["k_tc_split_z2"] = (3 * MP * cols * 4 + 3 * kp(MP) * cols * img, 0)
-    w["k_tc_gemm_z2"] = (3 * kp(MP) * cols * img + 3 * NZ * cols * 8, 3 * 10 * 2 * 128 * cols * kp(MP) * 2)
+    # Z2 and GL run one 128-row tile (rows 0..N-1); row N is formed beside the digits
+    w["k_tc_gemm_z2"] = (3 * kp(MP) * cols * img + 3 * N * cols * 8, 3 * 10 * 2 * N * cols * kp(MP))
     w["k_curl"] = (3 * NZ * cols * 8 + 2 * kp(NZ) * cols * img, nsolve * NZ * 12)
-    w["k_tc_gemm_gl"] = (2 * kp(NZ) * cols * img + 2 * NZ * cols * 8, 2 * 10 * 2 * 128 * cols * kp(NZ) * 2)
+    w["k_tc_gemm_gl"] = (2 * kp(NZ) * cols * img + 2 * N * cols * 8, 2 * 10 * 2 * N * cols * kp(NZ))
     w["k_inc_solve"] = (nk2 * stride * (8 + 4) + 8 * NZ * modes * c,
                         nsolve * 2 * (2 * (ne * ne + no * no)) * 2)
     w["k_inc_recover"] = (6 * NZ * modes * c, nsolve * NZ * 26)
