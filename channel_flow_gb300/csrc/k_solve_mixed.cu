@@ -17,7 +17,7 @@
 //                  (hi, lo) splits of M and c, about 2^-44 relative) + A^-1 r
 //                  (FP32), x = c + delta in FP64
 //   k_inc_recover  u, w, omega_x, omega_z from v and omega_y (getvelocityandvorticity,
-//                  REF:2347-2407), FP64 recurrences, one thread per (mode, re/im)
+//                  REF:2347-2407), FP64 recurrences, four threads per mode
 // FP64 arithmetic and double <-> float conversions share GB300's narrow FP64
 // pipe, so the conversions here are integer operations (f64bits.cuh).
 // The (0,0) mode (REF:401-474) stays with k_solve (FP64, one CTA).
@@ -310,22 +310,26 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
 }
 
 // ---------------------------------------------------------------------------
-// k_inc_recover: one thread per (mode, re/im) column, grid
-// (ceil(2 modes / RC_THREADS)); u, w, omega_x, omega_z from v and omega_y
-// (getvelocityandvorticity, REF:2347-2407) for every solved mode (not (0,0),
-// not the spanwise Nyquist slot):
+// k_inc_recover: four threads per mode (lane = 4 mode + 2 parity + re/im),
+// grid (ceil(4 modes / RC_THREADS)); u, w, omega_x, omega_z from v and
+// omega_y (getvelocityandvorticity, REF:2347-2407) for every solved mode
+// (not (0,0), not the spanwise Nyquist slot):
 //   u = (i a Dv - i b g) / k^2,            w = (i b Dv + i a g) / k^2,
 //   omega_z = -Du + i a v = (i b Dg - i a D^2 v) / k^2 + i a v,
 //   omega_x =  Dw - i b v = (i b D^2 v + i a Dg) / k^2 - i b v.
-// One descending pass carries Dv, D^2 v and Dg of the thread's component in
-// FP64 registers (the dz recurrence, b_0 halved on output), RC_PF rows of
-// v and omega_y loaded ahead; the partner
-// component comes by shuffle, and multiplying by i folds into the signs of
-// the per-thread coefficients.  13 FP64 operations per element; the
-// recurrence factors 2 (k + 1) are built by integer operations.
+// The dz recurrences (b_0 halved on output) run in FP64 registers on
+// descending rows; the even-k and odd-k chains of Dv and Dg are independent,
+// so the pair of parity threads of a component runs them in lockstep (even
+// rows 2s below the top, odd rows one below those); D^2 v at row k needs Dv
+// at row k + 1 from the other chain, exchanged by one shuffle per step (the
+// odd thread takes the even thread's current value, the even thread the odd
+// thread's previous one).  The other re/im component comes by shuffle, and
+// multiplying by i folds into the signs of the per-thread coefficients.  13
+// FP64 operations per element; the factors 2 (k + 1) are built by integer
+// operations; RC_PF steps of v and omega_y loaded ahead.
 // ---------------------------------------------------------------------------
 constexpr int RC_THREADS = 64;
-constexpr int RC_PF = 8;  // rows of v, omega_y loaded ahead of the recurrences
+constexpr int RC_PF = 8;  // steps of v, omega_y loaded ahead of the recurrences
 
 __global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict__ v, const cd* __restrict__ g,
                                                             cd* __restrict__ u, cd* __restrict__ w,
@@ -333,15 +337,17 @@ __global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict
                                                             const double* __restrict__ iapha,
                                                             const double* __restrict__ ibeta, Dims d) {
   const long modes = d.modes(), ncols = 2 * modes;
-  const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool in = col < ncols;  // every lane takes part in the shuffles
-  const long cl = in ? col : 0;
-  const long m = cl >> 1;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int comp = (int)(t & 1), par = (int)((t >> 1) & 1);
+  const long mt = t >> 2;
+  const bool in = mt < modes;  // every lane takes part in the shuffles
+  const long m = in ? mt : 0;
+  const long col = 2 * m + comp;
   const bool live = in && m > 0 && (m / d.KX) != d.NYQ;
   double sak = 0.0, sbk = 0.0, sa = 0.0, sb = 0.0;
   if (live) {
     // (i z)_re = -z_im, (i z)_im = z_re: the sign s of the partner term
-    const double s = (col & 1) ? 1.0 : -1.0;
+    const double s = comp ? 1.0 : -1.0;
     const double a = iapha[m % d.KX], b = ibeta[m / d.KX], ik2 = 1.0 / (a * a + b * b);
     sa = s * a;
     sb = s * b;
@@ -355,35 +361,44 @@ __global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict
   double* oxd = reinterpret_cast<double*>(ox);
   double* ozd = reinterpret_cast<double*>(oz);
   const int N = d.N;
-  // Dv, D^2 v, Dg at k+1 and k+2; v, omega_y at k+1
-  double dv1 = 0, dv2 = 0, d2v1 = 0, d2v2 = 0, dg1 = 0, dg2 = 0, vk1 = 0, gk1 = 0;
-  for (int k0 = N; k0 >= 0; k0 -= RC_PF) {
-    double vp[RC_PF], gp[RC_PF];
+  const int ktop = ((N - par) & ~1) | par;  // the largest k <= N with k = par (mod 2)
+  const int nsteps = N / 2 + 1;             // the even chain's rows N, N-2, ..., 0 (N is even)
+  // this chain's Dv, D^2 v, Dg at k + 2; the other chain's Dv at k + 1
+  double dv2 = 0.0, d2v2 = 0.0, dg2 = 0.0, dvx = 0.0;
+  for (int s0 = 0; s0 < nsteps; s0 += RC_PF) {
+    double vk[RC_PF], gk[RC_PF], vu[RC_PF], gu[RC_PF];
 #pragma unroll
     for (int i = 0; i < RC_PF; ++i) {
-      const size_t idx = (size_t)max(k0 - i, 0) * ncols + cl;
-      vp[i] = vd[idx];
-      gp[i] = gd[idx];
+      const int k = min(max(ktop - 2 * (s0 + i), 0), N);
+      const size_t idx = (size_t)k * ncols + col, iup = (size_t)min(k + 1, N) * ncols + col;
+      vk[i] = vd[idx];
+      gk[i] = gd[idx];
+      vu[i] = vd[iup];
+      gu[i] = gd[iup];
     }
 #pragma unroll
     for (int i = 0; i < RC_PF; ++i) {
-      const int k = k0 - i;
-      if (k < 0) break;
-      double dv = 0.0, d2v = 0.0, dg = 0.0;
-      if (k < N) {
+      const int st = s0 + i;
+      if (st >= nsteps) break;
+      const int k = ktop - 2 * st;  // -1 for the odd chain's last step
+      const bool row = k >= 0;
+      double dv = 0.0, dg = 0.0;
+      if (row && k < N) {
         const double tk = bits::from_int(2u * (uint32_t)(k + 1));
-        dv = fma(tk, vk1, dv2);
-        d2v = fma(tk, dv1, d2v2);
-        dg = fma(tk, gk1, dg2);
+        dv = fma(tk, vu[i], dv2);
+        dg = fma(tk, gu[i], dg2);
       }
-      dv2 = dv1;
-      dv1 = dv;
-      d2v2 = d2v1;
-      d2v1 = d2v;
-      dg2 = dg1;
-      dg1 = dg;
-      vk1 = vp[i];
-      gk1 = gp[i];
+      // exchange with the other chain: the odd thread needs the even thread's
+      // Dv of this step (row k + 1), the even thread keeps the odd thread's
+      // for its next step (also its row k + 1 then)
+      const double xv = __shfl_xor_sync(0xffffffffu, dv, 2);
+      if (par == 1) dvx = xv;
+      double d2v = 0.0;
+      if (row && k < N) d2v = fma(bits::from_int(2u * (uint32_t)(k + 1)), dvx, d2v2);
+      if (par == 0) dvx = xv;
+      dv2 = dv;
+      d2v2 = d2v;
+      dg2 = dg;
       if (k == 0) {  // the k = 0 outputs of dz are halved
         dv = bits::half(dv);
         d2v = bits::half(d2v);
@@ -392,9 +407,9 @@ __global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict
       const double dv_p = __shfl_xor_sync(0xffffffffu, dv, 1);
       const double d2v_p = __shfl_xor_sync(0xffffffffu, d2v, 1);
       const double dg_p = __shfl_xor_sync(0xffffffffu, dg, 1);
-      const double v_p = __shfl_xor_sync(0xffffffffu, vp[i], 1);
-      const double g_p = __shfl_xor_sync(0xffffffffu, gp[i], 1);
-      if (live) {
+      const double v_p = __shfl_xor_sync(0xffffffffu, vk[i], 1);
+      const double g_p = __shfl_xor_sync(0xffffffffu, gk[i], 1);
+      if (live && row) {
         const size_t idx = (size_t)k * ncols + col;
         ud[idx] = fma(sak, dv_p, -(sbk * g_p));
         wd[idx] = fma(sbk, dv_p, sak * g_p);
@@ -462,7 +477,7 @@ int launch_solve_mixed(Handle* h) {
   }
   {
     prof_begin(h, K_INC_RECOVER, &ev);
-    k_inc_recover<<<(unsigned)((2 * modes + RC_THREADS - 1) / RC_THREADS), RC_THREADS, 0, st>>>(
+    k_inc_recover<<<(unsigned)((4 * modes + RC_THREADS - 1) / RC_THREADS), RC_THREADS, 0, st>>>(
         h->f[F_V], h->f[F_OY], h->f[F_U], h->f[F_W], h->f[F_OX], h->f[F_OZ], h->iapha, h->ibeta, d);
     prof_end(h, K_INC_RECOVER, ev);
   }
