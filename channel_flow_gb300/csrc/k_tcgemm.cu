@@ -410,6 +410,22 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
 // at a time as one 16-byte store per plane (consecutive threads fill
 // consecutive core-matrix rows).  grid (ntiles, 1, nfields), FX_NT threads.
 // ---------------------------------------------------------------------------
+// max_k |(float) x_k| of a column.  For FP64 data the maximum is taken on the
+// magnitudes' bit patterns (non-negative doubles order like their bits, and
+// rounding to FP32 is monotone), so only the maximum is converted: the FP64
+// pipe, which also executes the conversions, sees one per column.
+__device__ __forceinline__ float column_absmax(const float* __restrict__ in, size_t ld, long col, int n) {
+  float mx = 0.f;
+  for (int k = 0; k < n; ++k) mx = fmaxf(mx, fabsf(in[(size_t)k * ld + col]));
+  return mx;
+}
+__device__ __forceinline__ float column_absmax(const double* __restrict__ in, size_t ld, long col, int n) {
+  unsigned long long mb = 0ull;
+  for (int k = 0; k < n; ++k)
+    mb = max(mb, (unsigned long long)__double_as_longlong(in[(size_t)k * ld + col]) & 0x7fffffffffffffffull);
+  return (float)__longlong_as_double((long long)mb);
+}
+
 // tail (optional): one more output row that the GEMM's plan leaves out,
 // computed exactly as the GEMM would (the row's digit planes tail.adig, its
 // exponent tail.aexp; levels i + j <= 3 summed exactly in FP32, combined in
@@ -424,9 +440,7 @@ __global__ void __launch_bounds__(FX_NT) k_tc_split_fx(const __grid_constant__ F
   const InT* in = ins.p[f];
   const long col = (long)nt * FX_NT + r;
   const bool live = col < plan.ncols;
-  float mx = 0.f;
-  if (live)
-    for (int k = 0; k < kvalid; ++k) mx = fmaxf(mx, fabsf((float)in[(size_t)k * plan.ncols + col]));
+  const float mx = live ? column_absmax(in, (size_t)plan.ncols, col, kvalid) : 0.f;
   float lev[FX_PLANES] = {0.f, 0.f, 0.f, 0.f};
   int e = 0;
   if (mx > 0.f) (void)frexpf(mx, &e);  // mx = m 2^e, m in [0.5, 1)
