@@ -401,38 +401,28 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zfwd(const cd* __restrict__ wz, 
 }
 
 // ---------------------------------------------------------------------------
-// Length-192 specialisations (3/2-padded 128-point directions), one warp per
-// line with the register FFT of fft_warp.cuh.  Rows written by k_yinv_w and
-// read by k_xprod_w / k_yfwd_w are in the permuted order 32 k1 + lane of that
-// header; every consumer is row-wise, so the order never matters.
+// Length-192 specialisations (3/2-padded 128-point directions), FP32, one
+// warp per line with the packed register FFT of fft_warp.cuh.  Rows written
+// by k_yinv_w and read by k_xprod_w / k_yfwd_w are in the permuted order
+// 32 k1 + lane of that header; every consumer is row-wise, so the order never
+// matters.
 // ---------------------------------------------------------------------------
 constexpr int W_WARPS = 8;    // warps (lines) per CTA in the x kernel
-// kx columns (one warp each) per CTA in the y kernels: 16 for FP32, 8 for FP64
-// (the [192][cols+1] tile stays under the 48 KB static shared-memory limit)
-template <typename T>
-struct YCols {
-  static constexpr int value = sizeof(T) == 4 ? 16 : 8;
-};
-
-template <typename T>
-__device__ __forceinline__ void load_tw192(cplx<T>* s_tw, const cplx<T>* __restrict__ tw) {
-  for (int t = threadIdx.x; t < 192; t += blockDim.x) s_tw[t] = tw[t];
-}
+constexpr int YW_COLS = 16;   // kx columns (one warp each) per CTA in the y kernels
 
 // x: c2r (three packed pairs), Lamb products, r2c; KX = 64, PX = 192.
 // grid ceil(nrows / W_WARPS), W_WARPS * 32 threads.
-template <typename T>
-__global__ void __launch_bounds__(W_WARPS * 32) k_xprod_w(cplx<T>* __restrict__ wy, long nrows,
-                                                         size_t fstride, T re_p,
-                                                         const cplx<T>* __restrict__ tw) {
-  using C = cplx<T>;
-  __shared__ C s_tw[192];
-  load_tw192(s_tw, tw);
+__global__ void __launch_bounds__(W_WARPS * 32) k_xprod_w(cf* __restrict__ wy, long nrows, size_t fstride,
+                                                         float re_p, const cf* __restrict__ tw) {
+  using C = cf;
+  __shared__ Fft192Table s_inv, s_fwd;
+  fft192_table<+1>(&s_inv, tw);
+  fft192_table<-1>(&s_fwd, tw);
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const long r = (long)blockIdx.x * W_WARPS + (threadIdx.x >> 5);
   if (r >= nrows) return;
-  C pk[3][6];
+  Line6 pk3[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const C* F = wy + (size_t)(2 * c) * fstride + (size_t)r * 64;
@@ -443,116 +433,147 @@ __global__ void __launch_bounds__(W_WARPS * 32) k_xprod_w(cplx<T>* __restrict__ 
     C f1s = shfl_i(f1, src), g1s = shfl_i(g1, src);
     C f0s = shfl_i(f0, src), g0s = shfl_i(g0, src);
     C f32 = shfl_i(f1, 0), g32 = shfl_i(g1, 0);  // mode 32 (for lane 0)
-    C* v = pk[c];
-    v[0] = lane == 0 ? C{f0.re, g0.re} : C{f0.re - g0.im, f0.im + g0.re};  // F + iG (mean: real parts)
-    v[1] = C{f1.re - g1.im, f1.im + g1.re};
-    v[2] = C{(T)0, (T)0};
-    v[3] = C{(T)0, (T)0};
-    v[4] = lane == 0 ? C{(T)0, (T)0} : C{f1s.re + g1s.im, g1s.re - f1s.im};  // conj F + i conj G
-    v[5] = lane == 0 ? C{f32.re + g32.im, g32.re - f32.im} : C{f0s.re + g0s.im, g0s.re - f0s.im};
-    fft192_natural_to_perm<T, +1>(v, s_tw);
+    // F + iG (mean: real parts) at positions l, 32 + l; zero at 64 .. 127;
+    // conj F + i conj G at 128 + l, 160 + l
+    const C v0 = lane == 0 ? C{f0.re, g0.re} : C{f0.re - g0.im, f0.im + g0.re};
+    const C v1{f1.re - g1.im, f1.im + g1.re};
+    const C v4 = lane == 0 ? C{0.f, 0.f} : C{f1s.re + g1s.im, g1s.re - f1s.im};
+    const C v5 = lane == 0 ? C{f32.re + g32.im, g32.re - f32.im} : C{f0s.re + g0s.im, g0s.re - f0s.im};
+    Line6& a = pk3[c];
+    a.r[0] = pk(v0.re, v1.re);
+    a.i[0] = pk(v0.im, v1.im);
+    a.r[1] = a.i[1] = 0ull;
+    a.r[2] = pk(v4.re, v5.re);
+    a.i[2] = pk(v4.im, v5.im);
+    fft192_natural_to_perm_x2<+1, true>(a, s_inv);
   }
-  C z1[6], z2[6];
+  // products, two elements per instruction:
+  //   H1 + i H2 = (oy w - re_p - oz v) + i (oz u - ox w),  H3 = ox v - oy u
+  Line6 z1, z2;
+  const f32x2 nrp = pk(-re_p, -re_p);
 #pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    const T u = pk[0][k].re, v = pk[0][k].im, w = pk[1][k].re, ox = pk[1][k].im;
-    const T oy = pk[2][k].re, oz = pk[2][k].im;
-    z1[k] = C{(oy * w - re_p) - oz * v, oz * u - ox * w};
-    z2[k] = C{ox * v - oy * u, (T)0};
+  for (int j = 0; j < 3; ++j) {
+    const f32x2 u = pk3[0].r[j], v = pk3[0].i[j], w = pk3[1].r[j], ox = pk3[1].i[j];
+    const f32x2 oy = pk3[2].r[j], oz = pk3[2].i[j];
+    z1.r[j] = sub2(fma2(oy, w, nrp), mul2(oz, v));
+    z1.i[j] = sub2(mul2(oz, u), mul2(ox, w));
+    z2.r[j] = sub2(mul2(ox, v), mul2(oy, u));
+    z2.i[j] = 0ull;
   }
-  fft192_perm_to_natural<T, -1>(z1, s_tw);
-  fft192_perm_to_natural<T, -1>(z2, s_tw);
-  // unpack H1, H2 from Z = FFT(H1 + i H2): Z[-k] for k = l (reg 0) and 32 + l (reg 1)
+  fft192_perm_to_natural_x2<-1>(z1, s_fwd);
+  fft192_perm_to_natural_x2<-1>(z2, s_fwd);
+  // unpack H1, H2 from Z = FFT(H1 + i H2): Z[-k] for k = l (element 0) and 32 + l (element 1)
   const int src = (32 - lane) & 31;
-  C m5 = shfl_i(z1[5], src), m4 = shfl_i(z1[4], src), m50 = shfl_i(z1[5], 0);
-  C A0 = z1[0], B0 = lane == 0 ? z1[0] : m5;   // Z[192 - l]
-  C A1 = z1[1], B1 = lane == 0 ? m50 : m4;     // Z[160 - l]
+  const C z10 = line_get(z1, 0), z11 = line_get(z1, 1), z14 = line_get(z1, 4), z15 = line_get(z1, 5);
+  C m5 = shfl_i(z15, src), m4 = shfl_i(z14, src), m50 = shfl_i(z15, 0);
+  C A0 = z10, B0 = lane == 0 ? z10 : m5;   // Z[192 - l]
+  C A1 = z11, B1 = lane == 0 ? m50 : m4;   // Z[160 - l]
   C* o0 = wy + (size_t)r * 64;
   C* o1 = wy + fstride + (size_t)r * 64;
   C* o2 = wy + 2 * fstride + (size_t)r * 64;
-  const T h = (T)0.5;
+  const float h = 0.5f;
   o0[lane] = C{h * (A0.re + B0.re), h * (A0.im - B0.im)};
   o1[lane] = C{h * (A0.im + B0.im), -h * (A0.re - B0.re)};
   o0[32 + lane] = C{h * (A1.re + B1.re), h * (A1.im - B1.im)};
   o1[32 + lane] = C{h * (A1.im + B1.im), -h * (A1.re - B1.re)};
-  o2[lane] = z2[0];
-  o2[32 + lane] = z2[1];
+  o2[lane] = line_get(z2, 0);
+  o2[32 + lane] = line_get(z2, 1);
 }
 
 // y inverse: per (field, plane, 16 kx columns); KY = 128, PY = 192.
-// grid (KX / 16, MP, 6), 512 threads.
-template <typename T, int YW_COLS = YCols<T>::value>
-__global__ void __launch_bounds__(YW_COLS * 32) k_yinv_w(const cplx<T>* __restrict__ wz,
-                                                        cplx<T>* __restrict__ wy, Dims d,
-                                                        const cplx<T>* __restrict__ tw) {
-  using C = cplx<T>;
-  __shared__ C s_tw[192];
-  __shared__ C tile[192][YW_COLS + 1];
-  load_tw192(s_tw, tw);
+// grid (KX / 16, MP, 6), 512 threads.  The tile holds real and imaginary
+// parts in separate planes (the packed lines pair elements, not re / im).
+__global__ void __launch_bounds__(YW_COLS * 32) k_yinv_w(const cf* __restrict__ wz, cf* __restrict__ wy, Dims d,
+                                                        const cf* __restrict__ tw) {
+  __shared__ Fft192Table s_t;
+  __shared__ float tre[192][YW_COLS + 1], tim[192][YW_COLS + 1];
+  fft192_table<+1>(&s_t, tw);
   const int f = blockIdx.z, p = blockIdx.y, kx0 = blockIdx.x * YW_COLS;
   const long modes = d.modes();
-  const C* src = wz + ((size_t)f * d.MP + p) * modes;
+  const cf* src = wz + ((size_t)f * d.MP + p) * modes;
   for (int t = threadIdx.x; t < 128 * YW_COLS; t += blockDim.x) {
     const int c = t % YW_COLS, ky = t / YW_COLS;
-    tile[ky][c] = src[(size_t)ky * d.KX + kx0 + c];
+    const cf x = src[(size_t)ky * d.KX + kx0 + c];
+    tre[ky][c] = x.re;
+    tim[ky][c] = x.im;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
-  C v[6];
-  const C z{(T)0, (T)0};
-  v[0] = tile[lane][c];                          // ky = l
-  v[1] = tile[32 + lane][c];                     // ky = 32 + l
-  v[2] = z;                                      // ky = 64 (Nyquist, zeroed) and padding
-  v[3] = z;
-  v[4] = lane == 0 ? z : tile[64 + lane][c];     // ky = 64 + l (negative modes)
-  v[5] = tile[96 + lane][c];                     // ky = 96 + l
-  fft192_natural_to_perm<T, +1>(v, s_tw);
+  // ky = l, 32 + l; 64 (Nyquist, zeroed) and padding; 64 + l (negative modes, l > 0), 96 + l
+  Line6 a;
+  a.r[0] = pk(tre[lane][c], tre[32 + lane][c]);
+  a.i[0] = pk(tim[lane][c], tim[32 + lane][c]);
+  a.r[1] = a.i[1] = 0ull;
+  a.r[2] = pk(lane == 0 ? 0.f : tre[64 + lane][c], tre[96 + lane][c]);
+  a.i[2] = pk(lane == 0 ? 0.f : tim[64 + lane][c], tim[96 + lane][c]);
+  fft192_natural_to_perm_x2<+1, true>(a, s_t);
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < 6; ++k) tile[32 * k + lane][c] = v[k];
+  for (int j = 0; j < 3; ++j) {
+    upk(a.r[j], tre[64 * j + lane][c], tre[64 * j + 32 + lane][c]);
+    upk(a.i[j], tim[64 * j + lane][c], tim[64 * j + 32 + lane][c]);
+  }
   __syncthreads();
-  C* dst = wy + ((size_t)f * d.MP + p) * (size_t)192 * d.KX;
+  cf* dst = wy + ((size_t)f * d.MP + p) * (size_t)192 * d.KX;
   for (int t = threadIdx.x; t < 192 * YW_COLS; t += blockDim.x) {
     const int cc = t % YW_COLS, q = t / YW_COLS;
-    dst[(size_t)q * d.KX + kx0 + cc] = tile[q][cc];
+    dst[(size_t)q * d.KX + kx0 + cc] = cf{tre[q][cc], tim[q][cc]};
   }
 }
 
 // y forward: per (component, plane, 16 kx columns); keeps ky = 0..64 and
 // the negative modes, scaled by 1/(PX PY).  grid (KX / 16, MP, 3), 512 threads.
-template <typename T, int YW_COLS = YCols<T>::value>
-__global__ void __launch_bounds__(YW_COLS * 32) k_yfwd_w(const cplx<T>* __restrict__ wy,
-                                                        cplx<T>* __restrict__ wz, Dims d,
-                                                        const cplx<T>* __restrict__ tw, T scale) {
-  using C = cplx<T>;
-  __shared__ C s_tw[192];
-  __shared__ C tile[192][YW_COLS + 1];
-  load_tw192(s_tw, tw);
+__global__ void __launch_bounds__(YW_COLS * 32) k_yfwd_w(const cf* __restrict__ wy, cf* __restrict__ wz, Dims d,
+                                                        const cf* __restrict__ tw, float scale) {
+  __shared__ Fft192Table s_t;
+  __shared__ float tre[192][YW_COLS + 1], tim[192][YW_COLS + 1];
+  fft192_table<-1>(&s_t, tw);
   const int f = blockIdx.z, p = blockIdx.y, kx0 = blockIdx.x * YW_COLS;
   const long modes = d.modes();
-  const C* src = wy + ((size_t)f * d.MP + p) * (size_t)192 * d.KX;
+  const cf* src = wy + ((size_t)f * d.MP + p) * (size_t)192 * d.KX;
   for (int t = threadIdx.x; t < 192 * YW_COLS; t += blockDim.x) {
     const int c = t % YW_COLS, q = t / YW_COLS;
-    tile[q][c] = src[(size_t)q * d.KX + kx0 + c];
+    const cf x = src[(size_t)q * d.KX + kx0 + c];
+    tre[q][c] = x.re;
+    tim[q][c] = x.im;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
-  C v[6];
+  Line6 a;
 #pragma unroll
-  for (int k = 0; k < 6; ++k) v[k] = tile[32 * k + lane][c];
-  fft192_perm_to_natural<T, -1>(v, s_tw);
+  for (int j = 0; j < 3; ++j) {
+    a.r[j] = pk(tre[64 * j + lane][c], tre[64 * j + 32 + lane][c]);
+    a.i[j] = pk(tim[64 * j + lane][c], tim[64 * j + 32 + lane][c]);
+  }
+  fft192_perm_to_natural_x2<-1>(a, s_t);
+  const f32x2 sc = pk(scale, scale);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    a.r[j] = mul2(a.r[j], sc);
+    a.i[j] = mul2(a.i[j], sc);
+  }
   __syncthreads();
   // natural spectral position 32 j + l -> ky slot
-  tile[lane][c] = C{v[0].re * scale, v[0].im * scale};                 // ky = l
-  tile[32 + lane][c] = C{v[1].re * scale, v[1].im * scale};            // ky = 32 + l
-  if (lane == 0) tile[64][c] = C{v[2].re * scale, v[2].im * scale};    // ky = 64 <- padded mode +64
-  if (lane > 0) tile[64 + lane][c] = C{v[4].re * scale, v[4].im * scale};  // ky = 64 + l
-  tile[96 + lane][c] = C{v[5].re * scale, v[5].im * scale};            // ky = 96 + l
+  const cf v0 = line_get(a, 0), v1 = line_get(a, 1), v2 = line_get(a, 2), v4 = line_get(a, 4),
+           v5 = line_get(a, 5);
+  tre[lane][c] = v0.re;  // ky = l
+  tim[lane][c] = v0.im;
+  tre[32 + lane][c] = v1.re;  // ky = 32 + l
+  tim[32 + lane][c] = v1.im;
+  if (lane == 0) {  // ky = 64 <- padded mode +64
+    tre[64][c] = v2.re;
+    tim[64][c] = v2.im;
+  } else {  // ky = 64 + l
+    tre[64 + lane][c] = v4.re;
+    tim[64 + lane][c] = v4.im;
+  }
+  tre[96 + lane][c] = v5.re;  // ky = 96 + l
+  tim[96 + lane][c] = v5.im;
   __syncthreads();
-  C* dst = wz + ((size_t)f * d.MP + p) * modes;
+  cf* dst = wz + ((size_t)f * d.MP + p) * modes;
   for (int t = threadIdx.x; t < 128 * YW_COLS; t += blockDim.x) {
     const int cc = t % YW_COLS, ky = t / YW_COLS;
-    dst[(size_t)ky * d.KX + kx0 + cc] = tile[ky][cc];
+    dst[(size_t)ky * d.KX + kx0 + cc] = cf{tre[ky][cc], tim[ky][cc]};
   }
 }
 
@@ -660,14 +681,14 @@ int run_zcurl(Handle* h) {
 // The FP32 register-FFT path of the x/y transforms, in two parts so that a
 // caller can run the inverse y transform field by field (fields f0 ..
 // f0 + nf - 1 of the six) and the products and forward transforms once.
-bool xy_register_path(const Dims& d) { return d.PX == 192 && d.PY == 192 && d.KX % YCols<float>::value == 0; }
+bool xy_register_path(const Dims& d) { return d.PX == 192 && d.PY == 192 && d.KX % YW_COLS == 0; }
 
 int launch_yinv_fields(Handle* h, cf* wz, cf* wy, const cf* tw_py, int f0, int nf) {
   const Dims& d = h->d;
-  constexpr int YC = YCols<float>::value;
+  constexpr int YC = YW_COLS;
   cudaEvent_t ev;
   prof_begin(h, K_YINV, &ev);
-  k_yinv_w<float><<<dim3(d.KX / YC, d.MP, nf), YC * 32, 0, h->stream>>>(
+  k_yinv_w<<<dim3(d.KX / YC, d.MP, nf), YC * 32, 0, h->stream>>>(
       wz + (size_t)f0 * d.MP * d.modes(), wy + (size_t)f0 * d.MP * d.PY * d.KX, d, tw_py);
   prof_end(h, K_YINV, ev);
   return cuda_ok(h, cudaGetLastError(), "k_yinv_w") ? CHF_OK : CHF_E_CUDA;
@@ -675,18 +696,18 @@ int launch_yinv_fields(Handle* h, cf* wz, cf* wy, const cf* tw_py, int f0, int n
 
 int launch_xprod_yfwd(Handle* h, cf* wz, cf* wy, const cf* tw_py, const cf* tw_px) {
   const Dims& d = h->d;
-  constexpr int YC = YCols<float>::value;
+  constexpr int YC = YW_COLS;
   cudaStream_t st = h->stream;
   cudaEvent_t ev;
   const long nrows = (long)d.MP * d.PY;
   prof_begin(h, K_XPROD, &ev);
-  k_xprod_w<float><<<(unsigned)((nrows + W_WARPS - 1) / W_WARPS), W_WARPS * 32, 0, st>>>(
+  k_xprod_w<<<(unsigned)((nrows + W_WARPS - 1) / W_WARPS), W_WARPS * 32, 0, st>>>(
       wy, nrows, (size_t)d.MP * d.PY * d.KX, (float)h->cfg.re_p, tw_px);
   prof_end(h, K_XPROD, ev);
   if (!cuda_ok(h, cudaGetLastError(), "k_xprod_w")) return CHF_E_CUDA;
   const float scale = (float)(1.0 / ((double)d.PX * (double)d.PY));
   prof_begin(h, K_YFWD, &ev);
-  k_yfwd_w<float><<<dim3(d.KX / YC, d.MP, 3), YC * 32, 0, st>>>(wy, wz, d, tw_py, scale);
+  k_yfwd_w<<<dim3(d.KX / YC, d.MP, 3), YC * 32, 0, st>>>(wy, wz, d, tw_py, scale);
   prof_end(h, K_YFWD, ev);
   return cuda_ok(h, cudaGetLastError(), "k_yfwd_w") ? CHF_OK : CHF_E_CUDA;
 }

@@ -27,6 +27,7 @@
 
 #include "chf_internal.h"
 #include "df32.cuh"
+#include "f32x2.cuh"
 #include "f64bits.cuh"
 
 namespace chf {
@@ -113,38 +114,8 @@ struct CoefHL {
 
 constexpr int CB = 4;  // matrix columns per load batch (two batches in flight)
 
-// Packed FP32 pairs (sm_100+ f32x2 instructions): the real and imaginary
-// parts of a coefficient travel together, two IEEE round-to-nearest
-// operations per instruction, bit-identical to the scalar forms.
-using f32x2 = unsigned long long;
-__device__ __forceinline__ f32x2 pk(float lo, float hi) {
-  f32x2 d;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
-  return d;
-}
-__device__ __forceinline__ void upk(f32x2 v, float& lo, float& hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
-  f32x2 d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
-  f32x2 d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
-  f32x2 d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
-  f32x2 d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
+// Packed FP32 pairs (f32x2.cuh): the real and imaginary parts of a
+// coefficient travel together.
 
 // S + C += (mh + ml)(ch + cl) for a (re, im) pair, compensated: p - ne' is
 // mh ch exactly (ne' = -(mh ch - p) from one FMA with -mh), the cross terms
