@@ -97,8 +97,11 @@ struct Handle {
   int nk2 = 0;
   double* k2vals = nullptr;   // nk2
   double* xinv = nullptr;     // nk2 * sl.stride
-  float2* incm = nullptr;     // mixed solve: A^-1 (B - A) per k^2 as (hi, lo) float pairs
-  float* incx = nullptr;      // mixed solve: A^-1 per k^2 as floats
+  // mixed solve (k_solve_mixed.cu), per k^2: A^-1 (B - A) as (hi, lo)
+  // floats, A^-1 as floats, and per row the exponent of sum |hi| over the row
+  float2* incm = nullptr;
+  float* incx = nullptr;
+  signed char* incr_exp = nullptr;
   double* xmean = nullptr;    // inverse of the (0,0) operator, NZ x NZ column-major
   int* group_start = nullptr; // nk2 + 1 (modes grouped by k^2)
   int* group_modes = nullptr; // solved modes, sorted by k^2 index

@@ -14,8 +14,8 @@
 // M = A^-1 (B - A) maps coefficients to coefficients and has no such
 // cancellation (its rows sum to within ~10x of the result).  A step is then
 //   k_inc_solve    one CTA per k^2 group: delta = M c (compensated FP32 on
-//                  (hi, lo) splits of M and c, about 2^-44 relative) + A^-1 r
-//                  (FP32), x = c + delta in FP64
+//                  (hi, lo) splits of M and c, summed against a power-of-two
+//                  offset) + A^-1 r (FP32), x = c + delta in FP64
 //   k_inc_recover  u, w, omega_x, omega_z from v and omega_y (getvelocityandvorticity,
 //                  REF:2347-2407), FP64 recurrences, four threads per mode
 // FP64 arithmetic and double <-> float conversions share GB300's narrow FP64
@@ -26,7 +26,6 @@
 #include <algorithm>
 
 #include "chf_internal.h"
-#include "df32.cuh"
 #include "f32x2.cuh"
 #include "f64bits.cuh"
 
@@ -93,6 +92,27 @@ __global__ void __launch_bounds__(256) k_build_incr(const double* __restrict__ t
   }
 }
 
+// Row exponents of the increment operators, grid (nk2, 4 blocks): for row r
+// of a block of M, sum_c |hi(r, c)| < 2^e (e = -100 for a zero row), as a
+// signed byte at the row's place among the group's 2 NZ rows (v even, v odd,
+// omega even, omega odd).
+__global__ void __launch_bounds__(128) k_incr_rowexp(const float2* __restrict__ incm, SolveLayout sl,
+                                                     signed char* __restrict__ rowexp) {
+  const int g = blockIdx.x, blk = blockIdx.y;
+  const int n = blk == 0 ? sl.ne_v : blk == 1 ? sl.no_v : blk == 2 ? sl.ne_w : sl.no_w;
+  const int roff = blk == 0 ? 0 : blk == 1 ? sl.ne_v : blk == 2 ? sl.ne_v + sl.no_v : sl.ne_v + sl.no_v + sl.ne_w;
+  const BlockOffsets bo = block_offsets(sl);
+  const float2* M = incm + (size_t)g * sl.stride + (blk == 0 ? bo.ve : blk == 1 ? bo.vo : blk == 2 ? bo.we : bo.wo);
+  const int rows = sl.ne_v + sl.no_v + sl.ne_w + sl.no_w;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    double sum = 0.0;
+    for (int c = 0; c < n; ++c) sum += fabs((double)M[(size_t)c * n + r].x);
+    int e = -100;
+    if (sum > 0.0) (void)frexp(sum, &e);  // sum = m 2^e, m in [0.5, 1)
+    rowexp[(size_t)g * rows + roff + r] = (signed char)max(-100, min(100, e));
+  }
+}
+
 // ---------------------------------------------------------------------------
 // k_inc_solve: one CTA per k^2 group (mean excluded), MCH modes of the group
 // per pass.  Per mode the CTA stages in shared memory
@@ -101,37 +121,37 @@ __global__ void __launch_bounds__(256) k_build_incr(const double* __restrict__ t
 //   * the AB2 term r = dt (3/2 N^n - 1/2 N^{n-1}) at the Gauss-Lobatto
 //     points, folded (even rows 1/2 (r_p + r_{N-p}), odd rows
 //     1/2 (r_p - r_{N-p}), p = row) with the wall rows zero, as floats;
-// then one thread per block row forms
+// and per block the exponent e_c of the largest |hi| (max < 2^e_c); then one
+// thread per block row forms
 //   delta = M c + X r
-// M c with compensated FP32 arithmetic (the exact product of the high parts
-// added by TwoSum, the cross terms and rounding errors into a second
-// accumulator; about 2^-44 relative), X r in plain FP32 (r is O(dt) and
-// X r has no cancellation), and writes x = c + delta in FP64.
+// and writes x = c + delta in FP64.  M c is compensated: the products of the
+// high parts p = mh ch are summed into S, which starts at the power of two
+//   sigma = 2^(e_r + e_c + 3) >= 8 sum_c |mh ch|      (sum_c |mh| < 2^e_r),
+// so that S and every S + p stay within (3/4, 5/4) sigma: s = S + p, then
+// S - s is exact (Sterbenz) and fma(mh, ch, S - s) is the product's rounding
+// error plus the part of p that S could not hold, rounded once.  That term
+// and the cross products mh cl + ml ch go to a second FP32 accumulator C,
+// with X r in plain FP32 (r is O(dt) and X r has no cancellation), and
+// delta = (S - sigma) + C with S - sigma exact: M c to about
+// 2^-40 sum_c |M_rc| max|c|, X r to FP32 rounding.
 // ---------------------------------------------------------------------------
 struct CoefHL {
   float hr, hi, lr, li;  // high and low parts of the real and imaginary parts
 };
 
-constexpr int CB = 4;  // matrix columns per load batch (two batches in flight)
+constexpr int CB = 3;  // matrix columns per load batch (two batches in flight)
 
 // Packed FP32 pairs (f32x2.cuh): the real and imaginary parts of a
 // coefficient travel together.
 
-// S + C += (mh + ml)(ch + cl) for a (re, im) pair, compensated: p - ne' is
-// mh ch exactly (ne' = -(mh ch - p) from one FMA with -mh), the cross terms
-// join it (still negated), TwoSum keeps the rounding error of S + p.
-// nmh = -mh, nml = -ml.
-__device__ __forceinline__ void comp_mac2(f32x2 mh, f32x2 nmh, f32x2 nml, f32x2 ch, f32x2 cl, f32x2& S,
-                                          f32x2& C) {
-  const f32x2 p = mul2(mh, ch);
-  f32x2 ne = fma2(nmh, ch, p);
-  ne = fma2(nmh, cl, ne);
-  ne = fma2(nml, ch, ne);
-  const f32x2 s = add2(S, p);
-  const f32x2 bb = sub2(s, S);
-  const f32x2 err = add2(sub2(S, sub2(s, bb)), sub2(p, bb));
+// S, C for one matrix entry (mh + ml) and one coefficient (ch + cl), real and
+// imaginary parts as a pair: S += mh ch, C += (mh ch - (s - S)) + mh cl + ml ch
+// (S against its offset sigma, so s - S is exact).  mh, ml broadcast.
+__device__ __forceinline__ void sig_mac2(f32x2 mh, f32x2 ml, f32x2 ch, f32x2 cl, f32x2& S, f32x2& C) {
+  const f32x2 s = add2(S, mul2(mh, ch));
+  const f32x2 u = fma2(mh, ch, sub2(S, s));
   S = s;
-  C = add2(C, sub2(err, ne));
+  C = fma2(ml, ch, fma2(mh, cl, add2(C, u)));
 }
 
 // Rows of one pass of k_inc_solve for NM staged modes: thread t owns row t of
@@ -140,7 +160,8 @@ template <int NM>
 __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g, const float2* __restrict__ Mg,
                                          const float* __restrict__ Xg, const SolveLayout& sl,
                                          const BlockOffsets& bo, int NZ, long modes, const cd* Cd,
-                                         const CoefHL* Cs, const float2* Rs, const int* s_mode) {
+                                         const CoefHL* Cs, const float2* Rs, const int* s_mode,
+                                         const signed char* __restrict__ rexp, const int* s_cexp) {
   const int nev = sl.ne_v, nov = sl.no_v, new_ = sl.ne_w, now_ = sl.no_w;
   const int rows = nev + nov + new_ + now_;
   for (int t = threadIdx.x; t < rows; t += blockDim.x) {
@@ -154,9 +175,15 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
     const int roff = b == 0 ? 0 : b == 1 ? nev : b == 2 ? NZ : NZ + new_;
     const float2* Mb = Mg + boff + row;
     const float* Xb = Xg + boff + row;
-    f32x2 S[NM], C[NM], A[NM];  // (re, im) pairs
+    f32x2 S[NM], C[NM];  // (re, im) pairs
+    const int er = rexp[roff + row];
 #pragma unroll
-    for (int q = 0; q < NM; ++q) S[q] = C[q] = A[q] = 0ull;
+    for (int q = 0; q < NM; ++q) {  // S starts at sigma of mode q for this row
+      const int e = max(-120, min(120, er + s_cexp[4 * q + b] + 3));
+      const float sg = __int_as_float((127 + e) << 23);
+      S[q] = pk(sg, sg);
+      C[q] = 0ull;
+    }
     // columns c < r0 of X meet the zero wall entries of the staged rhs
     float2 ma[CB];
     float xa[CB];
@@ -179,13 +206,13 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
 #pragma unroll
       for (int u = 0; u < CB; ++u) {
         if (c0 + u < n) {
-          const f32x2 mh = pk(ma[u].x, ma[u].x), nmh = pk(-ma[u].x, -ma[u].x), nml = pk(-ma[u].y, -ma[u].y);
+          const f32x2 mh = pk(ma[u].x, ma[u].x), ml = pk(ma[u].y, ma[u].y);
           const f32x2 xx = pk(xa[u], xa[u]);
 #pragma unroll
           for (int q = 0; q < NM; ++q) {
             const int si = q * 2 * NZ + roff + c0 + u;
-            comp_mac2(mh, nmh, nml, Cs2[2 * si], Cs2[2 * si + 1], S[q], C[q]);
-            A[q] = fma2(xx, Rs2[si], A[q]);
+            sig_mac2(mh, ml, Cs2[2 * si], Cs2[2 * si + 1], S[q], C[q]);
+            C[q] = fma2(xx, Rs2[si], C[q]);
           }
         }
       }
@@ -200,18 +227,18 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
 #pragma unroll
     for (int q = 0; q < NM; ++q) {
       const cd c0 = Cd[q * 2 * NZ + roff + row];
-      float Sv[2], Cv[2], Av[2];
+      float Sv[2], Cv[2];
       upk(S[q], Sv[0], Sv[1]);
       upk(C[q], Cv[0], Cv[1]);
-      upk(A[q], Av[0], Av[1]);
       double x[2];
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
-        // delta = S + A + C as a double-float, then x = c + delta with two
-        // FP64 additions (the float -> double moves are integer operations)
-        const df32 t = df_two_sum(Sv[k], Av[k]);
-        const df32 dd = df_fast_two_sum(t.hi, __fadd_rn(t.lo, Cv[k]));
-        x[k] = ((k == 0 ? c0.re : c0.im) + bits::widen(dd.hi)) + bits::widen(dd.lo);
+        // S - sigma (exact): S lies within (7/8, 9/8) sigma, so sigma is S's
+        // power of two, rounded up when S's significand is at least 1.5
+        const float d = Sv[k] - __int_as_float((__float_as_int(Sv[k]) + 0x400000) & 0xff800000);
+        // x = c + delta with two FP64 additions (the float -> double moves
+        // are integer operations)
+        x[k] = ((k == 0 ? c0.re : c0.im) + bits::widen(d)) + bits::widen(Cv[k]);
       }
       dst[(size_t)j * modes + s_mode[q]] = cd{x[0], x[1]};
     }
@@ -222,7 +249,8 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
                                                              const cd* __restrict__ rv, const cd* __restrict__ uh,
                                                              const cd* __restrict__ rg, const cd* __restrict__ wh,
                                                              const float2* __restrict__ incm,
-                                                             const float* __restrict__ incx, SolveLayout sl,
+                                                             const float* __restrict__ incx,
+                                                             const signed char* __restrict__ rowexp, SolveLayout sl,
                                                              const int* __restrict__ group_start,
                                                              const int* __restrict__ group_modes, Dims d,
                                                              float c3, float c1) {
@@ -233,6 +261,7 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
   CoefHL* Cs = reinterpret_cast<CoefHL*>(Cd + MCH * 2 * NZ);  // [MCH][2 NZ] their (hi, lo) splits
   float2* Rs = reinterpret_cast<float2*>(Cs + MCH * 2 * NZ);  // [MCH][2 NZ] folded AB2 term
   __shared__ int s_mode[MCH];
+  __shared__ int s_cexp[MCH * 4];  // largest |hi| per (mode, block): float bits, then its exponent
   const int grp = blockIdx.x;
   const int gs = group_start[grp], ge = group_start[grp + 1];
   const BlockOffsets bo = block_offsets(sl);
@@ -241,6 +270,7 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
   for (int base = gs; base < ge; base += MCH) {
     const int nm = min(MCH, ge - base);
     if (threadIdx.x < nm) s_mode[threadIdx.x] = group_modes[base + threadIdx.x];
+    if (threadIdx.x < MCH * 4) s_cexp[threadIdx.x] = 0;
     __syncthreads();
     for (int e = threadIdx.x; e < nm * 2 * NZ; e += blockDim.x) {
       const int q = e / (2 * NZ), i = e % (2 * NZ), f = i / NZ, k = i % NZ;
@@ -251,6 +281,7 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
       bits::split(x.re, h.hr, h.lr);
       bits::split(x.im, h.hi, h.li);
       Cs[slot] = h;
+      atomicMax(&s_cexp[4 * q + 2 * f + (k & 1)], __float_as_int(fmaxf(fabsf(h.hr), fabsf(h.hi))));
     }
     // the AB2 term in FP32 (X r is an FP32 product of an O(dt) term)
     for (int e = threadIdx.x; e < nm * 2 * ne; e += blockDim.x) {
@@ -270,11 +301,19 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
       if (r < N / 2) out[ne + r] = wall ? make_float2(0.f, 0.f) : make_float2(0.5f * (pr - qr), 0.5f * (pi - qi));
     }
     __syncthreads();
+    if (threadIdx.x < nm * 4) {  // max < 2^e
+      int e = -60;
+      const float mx = __int_as_float(s_cexp[threadIdx.x]);
+      if (mx > 0.f) (void)frexpf(mx, &e);
+      s_cexp[threadIdx.x] = max(-60, e);
+    }
+    __syncthreads();
+    const signed char* rexp = rowexp + (size_t)grp * 2 * NZ;
     switch (nm) {
-      case 1: inc_rows<1>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode); break;
-      case 2: inc_rows<2>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode); break;
-      case 3: inc_rows<3>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode); break;
-      default: inc_rows<4>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode); break;
+      case 1: inc_rows<1>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      case 2: inc_rows<2>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      case 3: inc_rows<3>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      default: inc_rows<4>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
     }
     __syncthreads();
   }
@@ -398,7 +437,8 @@ int setup_solver_mixed(Handle* h) {
   const size_t n = sl.stride * (size_t)h->nk2;
   if (n == 0) return CHF_OK;
   if (!cuda_ok(h, cudaMalloc((void**)&h->incm, sizeof(float2) * n), "increment operators") ||
-      !cuda_ok(h, cudaMalloc((void**)&h->incx, sizeof(float) * n), "increment operators"))
+      !cuda_ok(h, cudaMalloc((void**)&h->incx, sizeof(float) * n), "increment operators") ||
+      !cuda_ok(h, cudaMalloc((void**)&h->incr_exp, (size_t)2 * h->d.NZ * h->nk2), "increment operators"))
     return CHF_E_NOMEM;
   const int nmax = std::max(sl.ne_v, sl.ne_w);
   const size_t smem = sizeof(double) * (size_t)nmax * BW;
@@ -408,7 +448,9 @@ int setup_solver_mixed(Handle* h) {
     return CHF_E_CUDA;
   k_build_incr<<<dim3(h->nk2, 4), 256, smem, h->stream>>>(h->t0, h->t2, h->t4, h->k2vals, h->xinv, sl, h->d.N,
                                                           h->cfg.dt / h->cfg.re, h->incm, h->incx);
-  if (!cuda_ok(h, cudaGetLastError(), "k_build_incr") ||
+  if (!cuda_ok(h, cudaGetLastError(), "k_build_incr")) return CHF_E_CUDA;
+  k_incr_rowexp<<<dim3(h->nk2, 4), 128, 0, h->stream>>>(h->incm, sl, h->incr_exp);
+  if (!cuda_ok(h, cudaGetLastError(), "k_incr_rowexp") ||
       !cuda_ok(h, cudaStreamSynchronize(h->stream), "k_build_incr sync"))
     return CHF_E_CUDA;
   return CHF_OK;
@@ -441,7 +483,7 @@ int launch_solve_mixed(Handle* h) {
       return CHF_E_CUDA;
     prof_begin(h, K_INC_SOLVE, &ev);
     k_inc_solve<<<h->nk2, MV_THREADS, smem, st>>>(h->f[F_V], h->f[F_OY], h->f[F_RV], h->f[F_U], h->f[F_RG],
-                                                   h->f[F_W], h->incm, h->incx, h->sl, h->group_start,
+                                                   h->f[F_W], h->incm, h->incx, h->incr_exp, h->sl, h->group_start,
                                                    h->group_modes, d, (float)(1.5 * dt), (float)(0.5 * dt));
     prof_end(h, K_INC_SOLVE, ev);
     if (h->after_inc && !cuda_ok(h, cudaEventRecord(h->after_inc, st), "increment solve event")) return CHF_E_CUDA;
