@@ -112,11 +112,14 @@ struct Line6 {
   f32x2 r[3], i[3];  // r[j] = (x[2j].re, x[2j+1].re), i[j] likewise
 };
 
-// per transform sign; component-major so that a warp's 16-byte loads are
-// conflict-free
+// per transform sign, lane-contiguous (conflict-free 8- and 16-byte loads):
+// st[s][lane] = W', the twiddle of stage s (h = 16 >> s) on the upper lane
+// of a butterfly and 1 on the lower one; tw6[j][lane] = W192^(lane k1) for
+// k1 = 2j, 2j + 1 as {re, re', im, im'}.  The butterfly sign S comes from
+// the lane bits.
 struct Fft192Table {
-  float4 st[5][2][32];   // stage s (h = 16 >> s): {W'.re, W'.re, W'.im, W'.im}, {-W'.im, -W'.im, S, S}
-  float4 tw6[3][2][32];  // W192^(lane k1) for k1 = 2j, 2j + 1: {re, re', im, im'}, {-im, -im', 0, 0}
+  float2 st[5][32];
+  float4 tw6[3][32];
 };
 
 template <int SIGN>
@@ -125,19 +128,26 @@ __device__ __forceinline__ void fft192_table(Fft192Table* t, const cplx<float>* 
     const int s = e >> 5, lane = e & 31;
     if (s < 5) {
       const int h = 16 >> s;
-      const bool upper = (lane & h) != 0;
       cplx<float> w = twid<float, SIGN>(tw, (lane & (h - 1)) * (96 / h));
-      if (!upper) w = cplx<float>{1.f, 0.f};
-      const float sg = upper ? -1.f : 1.f;
-      t->st[s][0][lane] = make_float4(w.re, w.re, w.im, w.im);
-      t->st[s][1][lane] = make_float4(-w.im, -w.im, sg, sg);
+      if ((lane & h) == 0) w = cplx<float>{1.f, 0.f};
+      t->st[s][lane] = make_float2(w.re, w.im);
     } else {
       const int j = s - 5;
       const cplx<float> a = twid<float, SIGN>(tw, lane * 2 * j), b = twid<float, SIGN>(tw, lane * (2 * j + 1));
-      t->tw6[j][0][lane] = make_float4(a.re, b.re, a.im, b.im);
-      t->tw6[j][1][lane] = make_float4(-a.im, -b.im, 0.f, 0.f);
+      t->tw6[j][lane] = make_float4(a.re, b.re, a.im, b.im);
     }
   }
+}
+
+// the packed constants of cross-lane stage s for this lane
+struct StageK {
+  f32x2 wr, wi, nwi, sg;
+};
+__device__ __forceinline__ StageK stage_k(const Fft192Table& t, int s, int lane) {
+  const int h = 16 >> s;
+  const float2 w = t.st[s][lane];
+  const float sg = (lane & h) ? -1.f : 1.f;
+  return StageK{pk(w.x, w.x), pk(w.y, w.y), pk(-w.y, -w.y), pk(sg, sg)};
 }
 
 // (r, i) <- (r, i) (wr, wi) for two elements; nwi = -wi
@@ -199,19 +209,18 @@ __device__ __forceinline__ void fft192_natural_to_perm_x2(Line6& a, const Fft192
   dft6_x2<SIGN, Z1>(a);
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    const float4 p = t.tw6[j][0][lane], q = t.tw6[j][1][lane];
-    cmul_x2(a.r[j], a.i[j], pk(p.x, p.y), pk(p.z, p.w), pk(q.x, q.y));
+    const float4 p = t.tw6[j][lane];
+    cmul_x2(a.r[j], a.i[j], pk(p.x, p.y), pk(p.z, p.w), pk(-p.z, -p.w));
   }
 #pragma unroll
   for (int s = 0; s < 5; ++s) {
     const int h = 16 >> s;
-    const float4 p = t.st[s][0][lane], q = t.st[s][1][lane];
-    const f32x2 sg = pk(q.z, q.w);
+    const StageK k = stage_k(t, s, lane);
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      a.r[j] = fma2(sg, a.r[j], shfl_x2(a.r[j], h));
-      a.i[j] = fma2(sg, a.i[j], shfl_x2(a.i[j], h));
-      if (h > 1) cmul_x2(a.r[j], a.i[j], pk(p.x, p.y), pk(p.z, p.w), pk(q.x, q.y));  // W_2 = 1
+      a.r[j] = fma2(k.sg, a.r[j], shfl_x2(a.r[j], h));
+      a.i[j] = fma2(k.sg, a.i[j], shfl_x2(a.i[j], h));
+      if (h > 1) cmul_x2(a.r[j], a.i[j], k.wr, k.wi, k.nwi);  // W_2 = 1
     }
   }
 }
@@ -223,19 +232,18 @@ __device__ __forceinline__ void fft192_perm_to_natural_x2(Line6& a, const Fft192
 #pragma unroll
   for (int s = 4; s >= 0; --s) {
     const int h = 16 >> s;
-    const float4 p = t.st[s][0][lane], q = t.st[s][1][lane];
-    const f32x2 sg = pk(q.z, q.w);
+    const StageK k = stage_k(t, s, lane);
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      if (h > 1) cmul_x2(a.r[j], a.i[j], pk(p.x, p.y), pk(p.z, p.w), pk(q.x, q.y));
-      a.r[j] = fma2(sg, a.r[j], shfl_x2(a.r[j], h));
-      a.i[j] = fma2(sg, a.i[j], shfl_x2(a.i[j], h));
+      if (h > 1) cmul_x2(a.r[j], a.i[j], k.wr, k.wi, k.nwi);
+      a.r[j] = fma2(k.sg, a.r[j], shfl_x2(a.r[j], h));
+      a.i[j] = fma2(k.sg, a.i[j], shfl_x2(a.i[j], h));
     }
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    const float4 p = t.tw6[j][0][lane], q = t.tw6[j][1][lane];
-    cmul_x2(a.r[j], a.i[j], pk(p.x, p.y), pk(p.z, p.w), pk(q.x, q.y));
+    const float4 p = t.tw6[j][lane];
+    cmul_x2(a.r[j], a.i[j], pk(p.x, p.y), pk(p.z, p.w), pk(-p.z, -p.w));
   }
   dft6_x2<SIGN>(a);
 }

@@ -410,6 +410,16 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zfwd(const cd* __restrict__ wz, 
 constexpr int W_WARPS = 8;    // warps (lines) per CTA in the x kernel
 constexpr int YW_COLS = 16;   // kx columns (one warp each) per CTA in the y kernels
 
+// Element t of a pass over a [rows][YW_COLS] tile (rows a multiple of 32,
+// row stride YW_COLS + 1 floats): a warp takes the 16 columns of rows r and
+// r + 16, whose banks are disjoint (17 * 16 = 16 mod 32), and each half-warp
+// one 128-byte row segment in global memory.
+__device__ __forceinline__ void tile_rc(int t, int& row, int& col) {
+  const int lane = t & 31, wi = t >> 5;
+  col = lane & 15;
+  row = (wi >> 4) * 32 + (lane >> 4) * 16 + (wi & 15);
+}
+
 // x: c2r (three packed pairs), Lamb products, r2c; KX = 64, PX = 192.
 // grid ceil(nrows / W_WARPS), W_WARPS * 32 threads.
 __global__ void __launch_bounds__(W_WARPS * 32) k_xprod_w(cf* __restrict__ wy, long nrows, size_t fstride,
@@ -483,7 +493,7 @@ __global__ void __launch_bounds__(W_WARPS * 32) k_xprod_w(cf* __restrict__ wy, l
 // y inverse: per (field, plane, 16 kx columns); KY = 128, PY = 192.
 // grid (KX / 16, MP, 6), 512 threads.  The tile holds real and imaginary
 // parts in separate planes (the packed lines pair elements, not re / im).
-__global__ void __launch_bounds__(YW_COLS * 32) k_yinv_w(const cf* __restrict__ wz, cf* __restrict__ wy, Dims d,
+__global__ void __launch_bounds__(YW_COLS * 32, 4) k_yinv_w(const cf* __restrict__ wz, cf* __restrict__ wy, Dims d,
                                                         const cf* __restrict__ tw) {
   __shared__ Fft192Table s_t;
   __shared__ float tre[192][YW_COLS + 1], tim[192][YW_COLS + 1];
@@ -492,7 +502,8 @@ __global__ void __launch_bounds__(YW_COLS * 32) k_yinv_w(const cf* __restrict__ 
   const long modes = d.modes();
   const cf* src = wz + ((size_t)f * d.MP + p) * modes;
   for (int t = threadIdx.x; t < 128 * YW_COLS; t += blockDim.x) {
-    const int c = t % YW_COLS, ky = t / YW_COLS;
+    int ky, c;
+    tile_rc(t, ky, c);
     const cf x = src[(size_t)ky * d.KX + kx0 + c];
     tre[ky][c] = x.re;
     tim[ky][c] = x.im;
@@ -516,14 +527,15 @@ __global__ void __launch_bounds__(YW_COLS * 32) k_yinv_w(const cf* __restrict__ 
   __syncthreads();
   cf* dst = wy + ((size_t)f * d.MP + p) * (size_t)192 * d.KX;
   for (int t = threadIdx.x; t < 192 * YW_COLS; t += blockDim.x) {
-    const int cc = t % YW_COLS, q = t / YW_COLS;
+    int q, cc;
+    tile_rc(t, q, cc);
     dst[(size_t)q * d.KX + kx0 + cc] = cf{tre[q][cc], tim[q][cc]};
   }
 }
 
 // y forward: per (component, plane, 16 kx columns); keeps ky = 0..64 and
 // the negative modes, scaled by 1/(PX PY).  grid (KX / 16, MP, 3), 512 threads.
-__global__ void __launch_bounds__(YW_COLS * 32) k_yfwd_w(const cf* __restrict__ wy, cf* __restrict__ wz, Dims d,
+__global__ void __launch_bounds__(YW_COLS * 32, 4) k_yfwd_w(const cf* __restrict__ wy, cf* __restrict__ wz, Dims d,
                                                         const cf* __restrict__ tw, float scale) {
   __shared__ Fft192Table s_t;
   __shared__ float tre[192][YW_COLS + 1], tim[192][YW_COLS + 1];
@@ -532,7 +544,8 @@ __global__ void __launch_bounds__(YW_COLS * 32) k_yfwd_w(const cf* __restrict__ 
   const long modes = d.modes();
   const cf* src = wy + ((size_t)f * d.MP + p) * (size_t)192 * d.KX;
   for (int t = threadIdx.x; t < 192 * YW_COLS; t += blockDim.x) {
-    const int c = t % YW_COLS, q = t / YW_COLS;
+    int q, c;
+    tile_rc(t, q, c);
     const cf x = src[(size_t)q * d.KX + kx0 + c];
     tre[q][c] = x.re;
     tim[q][c] = x.im;
@@ -572,7 +585,8 @@ __global__ void __launch_bounds__(YW_COLS * 32) k_yfwd_w(const cf* __restrict__ 
   __syncthreads();
   cf* dst = wz + ((size_t)f * d.MP + p) * modes;
   for (int t = threadIdx.x; t < 128 * YW_COLS; t += blockDim.x) {
-    const int cc = t % YW_COLS, ky = t / YW_COLS;
+    int ky, cc;
+    tile_rc(t, ky, cc);
     dst[(size_t)ky * d.KX + kx0 + cc] = cf{tre[ky][cc], tim[ky][cc]};
   }
 }

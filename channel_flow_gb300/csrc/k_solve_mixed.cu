@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(128) k_incr_rowexp(const float2* __restrict__ 
 // delta = (S - sigma) + C with S - sigma exact: M c to about
 // 2^-40 sum_c |M_rc| max|c|, X r to FP32 rounding.
 // ---------------------------------------------------------------------------
-struct CoefHL {
+struct __align__(16) CoefHL {
   float hr, hi, lr, li;  // high and low parts of the real and imaginary parts
 };
 
@@ -192,7 +192,6 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
       ma[u] = u < n ? __ldg(Mb + (size_t)u * n) : make_float2(0.f, 0.f);
       xa[u] = u < n ? __ldg(Xb + (size_t)u * n) : 0.f;
     }
-    const f32x2* Cs2 = reinterpret_cast<const f32x2*>(Cs);  // (hr, hi), (lr, li) per entry
     const f32x2* Rs2 = reinterpret_cast<const f32x2*>(Rs);
     for (int c0 = 0; c0 < n; c0 += CB) {
       float2 mb[CB];
@@ -211,7 +210,8 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
 #pragma unroll
           for (int q = 0; q < NM; ++q) {
             const int si = q * 2 * NZ + roff + c0 + u;
-            sig_mac2(mh, ml, Cs2[2 * si], Cs2[2 * si + 1], S[q], C[q]);
+            const float4 ch = reinterpret_cast<const float4*>(Cs)[si];  // one 16-byte load
+            sig_mac2(mh, ml, pk(ch.x, ch.y), pk(ch.z, ch.w), S[q], C[q]);
             C[q] = fma2(xx, Rs2[si], C[q]);
           }
         }
