@@ -35,30 +35,32 @@ namespace chf {
 
 namespace {
 
-constexpr int CURL_THREADS = 32;  // 16 (mode, re/im) columns per CTA, two threads each
+constexpr int CURL_THREADS = 64;  // 16 (mode, re/im) columns per CTA: warp 0 h_v, warp 1 h_g
+constexpr int CURL_COLS = 16;
 
-// Two threads per (mode, re/im) column (lanes 2c and 2c + 1), grid
-// (ceil(4 modes / CURL_THREADS)).  lc: 3 fields [NZ][ncols] FP64 (H1, H2, H3
-// coefficients from the exact z transform); hs: FP32 scratch [2][NZ][ncols];
-// out: fixed-point digit images and column exponents for the GL GEMM
-// (k_tcgemm.cu layout), field 0 = h_v, field 1 = h_g (mode (0,0) carries H1,
-// H3).  FP64 up to h_v, h_g: h_v is a small remainder of k^2 H2 + D G with
-// G = i a H1 + i b H3 (the gradient part of the Lamb vector cancels), so FP32
-// derivatives would leave an error ~100x FP32 rounding in it.  Only G is
-// differentiated, by dz's backward recurrence (REF:570-599)
+// Grid ceil(ncols / CURL_COLS), CURL_THREADS threads: warp f of a CTA forms
+// field f (0 = h_v, 1 = h_g) of the CTA's 16 (mode, re/im) columns, two lanes
+// per column (lanes 2c and 2c + 1).  lc: 3 fields [NZ][ncols] FP64 (H1, H2,
+// H3 coefficients from the exact z transform); hs: FP32 scratch
+// [2][NZ][ncols]; out: fixed-point digit images and column exponents for the
+// GL GEMM (k_tcgemm.cu layout), field 0 = h_v, field 1 = h_g (mode (0,0)
+// carries H1, H3).  FP64 up to h_v, h_g: h_v is a small remainder of
+// k^2 H2 + D G with G = i a H1 + i b H3 (the gradient part of the Lamb vector
+// cancels), so FP32 derivatives would leave an error ~100x FP32 rounding in
+// it.  Only G is differentiated, by dz's backward recurrence (REF:570-599)
 //   (D G)_k = (D G)_{k+2} + 2 (k+1) G_{k+1},
-// whose even-k and odd-k chains are independent: the pair's thread p runs the
-// rows k = p (mod 2), forming the G values of the other parity it needs.
-// Multiplying by i folds into the signs of the per-thread coefficients, the
-// partner component is read directly.  Pass 1 (descending, 6 FP64 operations
-// per element, CURL_PF rows of H loaded ahead) rounds h_v, h_g to FP32 by
-// integer operations into hs; the pair combines its column maxima (their
-// powers of two).  Pass 2 (the pair splits the 8-row groups) writes the
-// digits, 8 rows per 16-byte store, and the exact level sums of the GL row N
-// (the wall z = -1), which the GL GEMM leaves out (it covers 0..N-1).
-constexpr int CURL_PF = 8;  // own rows of H loaded ahead of the recurrence
+// whose even-k and odd-k chains are independent: lane p of a pair runs the
+// rows k = p (mod 2), forming the G values of the other parity it needs;
+// h_g = i a H3 - i b H1 is pointwise.  Multiplying by i folds into the signs
+// of the per-thread coefficients, the partner component is read directly.
+// Pass 1 (descending, CURL_PF rows of H loaded ahead) rounds the field to
+// FP32 by integer operations into hs; the pair combines its column maxima
+// (their powers of two).  Pass 2 (the pair splits the 8-row groups) writes
+// the digits, 8 rows per 16-byte store, and the exact level sums of the GL
+// row N (the wall z = -1), which the GL GEMM leaves out (it covers 0..N-1).
+constexpr int CURL_PF = 6;  // own rows of H loaded ahead of the recurrence
 
-__global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict__ lc,
+__global__ void __launch_bounds__(CURL_THREADS, 14) k_curl(const double* __restrict__ lc,
                                                        const double* __restrict__ iapha,
                                                        const double* __restrict__ ibeta, Dims d,
                                                        const __grid_constant__ FxPlan plan, float* __restrict__ hs,
@@ -66,9 +68,9 @@ __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict_
                                                        const float* __restrict__ gl_tail, int gl_tail_exp,
                                                        double* __restrict__ glv_n, double* __restrict__ glg_n) {
   const long modes = d.modes(), ncols = 2 * modes;
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long col = t >> 1;
-  const int par = (int)(t & 1);
+  const int f = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long col = (long)blockIdx.x * CURL_COLS + (lane >> 1);
+  const int par = lane & 1;
   const bool live = col < ncols;  // every lane takes part in the pair's shuffles
   const long cl = live ? col : 0;
   const long m = cl >> 1;
@@ -82,103 +84,91 @@ __global__ void __launch_bounds__(CURL_THREADS) k_curl(const double* __restrict_
   const double* H1 = lc;
   const double* H2 = lc + (size_t)NZ * ncols;
   const double* H3 = lc + (size_t)2 * NZ * ncols;
-  double dg2 = 0.0;         // D G at k+2 (this parity)
-  float mv = 0.f, mg = 0.f;  // column maxima of |h_v|, |h_g| over this parity's rows
+  float* out = hs + (size_t)f * NZ * ncols;
+  double dg2 = 0.0;  // D G at k+2 (this parity)
+  float mx = 0.f;    // column maximum of |field| over this parity's rows
   const int ktop = (N - par) & ~1 | par;  // the largest k <= N with k = par (mod 2)
   for (int k0 = ktop; k0 >= 0; k0 -= 2 * CURL_PF) {
-    double h1[CURL_PF], h2[CURL_PF], h3[CURL_PF], g1[CURL_PF], g3[CURL_PF];
+    // h_v: H2 (H1 for the mean) at row k, H1 and H3 at row k + 1;
+    // h_g: H1 and H3 at row k
+    double x1[CURL_PF], x2[CURL_PF], x3[CURL_PF];
 #pragma unroll
     for (int i = 0; i < CURL_PF; ++i) {
       const int k = max(k0 - 2 * i, 0);
       const size_t base = (size_t)k * ncols, up = (size_t)min(k + 1, N) * ncols;
-      h1[i] = H1[base + pcol];
-      h2[i] = H2[base + cl];
-      h3[i] = H3[base + pcol];
-      g1[i] = H1[up + pcol];  // row k + 1 for G_{k+1}
-      g3[i] = H3[up + pcol];
+      if (f == 0) {
+        x2[i] = mean ? H1[base + cl] : H2[base + cl];
+        x1[i] = H1[up + pcol];
+        x3[i] = H3[up + pcol];
+      } else {
+        x2[i] = 0.0;
+        x1[i] = H1[base + pcol];
+        x3[i] = H3[base + pcol];
+      }
     }
 #pragma unroll
     for (int i = 0; i < CURL_PF; ++i) {
       const int k = k0 - 2 * i;
       if (k < 0) break;
-      double dg = 0.0;
-      if (k < N) {
-        const double gk1 = fma(sa, g1[i], sb * g3[i]);  // (i a H1 + i b H3) at row k + 1
-        dg = fma(bits::from_int(2u * (uint32_t)(k + 1)), gk1, dg2);
-      }
-      dg2 = dg;
-      if (k == 0) dg = bits::half(dg);  // dz halves b_0
-      float ov, og;
-      if (mean) {
-        ov = bits::narrow(h1[i]);
-        og = bits::narrow(h3[i]);
+      float o;
+      if (f == 0) {
+        double dg = 0.0;
+        if (k < N) {
+          const double gk1 = fma(sa, x1[i], sb * x3[i]);  // (i a H1 + i b H3) at row k + 1
+          dg = fma(bits::from_int(2u * (uint32_t)(k + 1)), gk1, dg2);
+        }
+        dg2 = dg;
+        if (k == 0) dg = bits::half(dg);  // dz halves b_0
+        o = bits::narrow(mean ? x2[i] : fma(k2, x2[i], dg));  // h_v = k^2 H2 + D G
       } else {
-        ov = bits::narrow(fma(k2, h2[i], dg));           // h_v = k^2 H2 + D G
-        og = bits::narrow(fma(sa, h3[i], -(sb * h1[i])));  // h_g = i a H3 - i b H1
+        o = bits::narrow(mean ? x3[i] : fma(sa, x3[i], -(sb * x1[i])));  // h_g = i a H3 - i b H1
       }
-      if (live) {
-        const size_t base = (size_t)k * ncols;
-        hs[base + col] = ov;
-        hs[(size_t)NZ * ncols + base + col] = og;
-      }
-      mv = fmaxf(mv, fabsf(ov));
-      mg = fmaxf(mg, fabsf(og));
+      if (live) out[(size_t)k * ncols + col] = o;
+      mx = fmaxf(mx, fabsf(o));
     }
   }
-  mv = fmaxf(mv, __shfl_xor_sync(0xffffffffu, mv, 1));
-  mg = fmaxf(mg, __shfl_xor_sync(0xffffffffu, mg, 1));
-  int e[2] = {0, 0};
-  if (mv > 0.f) (void)frexpf(mv, &e[0]);
-  if (mg > 0.f) (void)frexpf(mg, &e[1]);
-  if (live && par == 0) {
-    bexp[col] = e[0];
-    bexp[plan.bexp_stride() + col] = e[1];
-  }
-  __syncwarp();  // the partner's rows of hs are visible from here on
+  mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+  int e = 0;
+  if (mx > 0.f) (void)frexpf(mx, &e);
+  if (live && par == 0) bexp[(size_t)f * plan.bexp_stride() + col] = e;
+  __syncwarp();  // the partner's rows of the field are visible from here on
   // pass 2: digits, groups of 8 rows (rows >= NZ are zero), the pair taking
   // alternate groups, and the level sums of the GL row N
   const int nt = (int)(cl / FX_NT), r = (int)(cl % FX_NT);
-  float lev[2][FX_PLANES] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+  float lev[FX_PLANES] = {0.f, 0.f, 0.f, 0.f};
+  uint8_t* fimg = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes;
   for (int g = par; g < plan.kpad / 8; g += 2) {
     const int ch = (8 * g) / TC_KC, kl = 8 * g - ch * TC_KC;
     const uint32_t pbytes = (uint32_t)FX_NT * plan.kc[ch] * 2u;
     const size_t off = ((size_t)(kl / 8) * (FX_NT / 8) + r / 8) * 128 + (r % 8) * 16;
+    uint16_t hd[FX_PLANES][8];
 #pragma unroll
-    for (int f = 0; f < 2; ++f) {
-      uint16_t hd[FX_PLANES][8];
+    for (int q = 0; q < 8; ++q) {
+      const int k = 8 * g + q;
+      const float x = (live && k <= N) ? out[(size_t)k * ncols + col] : 0.f;
+      float dg[FX_PLANES];
+      tc::fx_digits_f(x, e, dg);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int k = 8 * g + q;
-        const float x = (live && k <= N) ? hs[(size_t)f * NZ * ncols + (size_t)k * ncols + col] : 0.f;
-        float dg[FX_PLANES];
-        tc::fx_digits_f(x, e[f], dg);
+      for (int i = 0; i < FX_PLANES; ++i) hd[i][q] = tc::bf16_bits(dg[i]);
+      tc::fx_tail_mac(gl_tail, plan.kpad, k, dg, lev);
+    }
+    if (live) {
+      uint8_t* base = fimg + plan.b_chunk_off[ch];
 #pragma unroll
-        for (int i = 0; i < FX_PLANES; ++i) hd[i][q] = tc::bf16_bits(dg[i]);
-        tc::fx_tail_mac(gl_tail, plan.kpad, k, dg, lev[f]);
-      }
-      if (live) {
-        uint8_t* base = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes + plan.b_chunk_off[ch];
-#pragma unroll
-        for (int pl = 0; pl < FX_PLANES; ++pl) {
-          uint4 u4;
-          u4.x = (uint32_t)hd[pl][0] | ((uint32_t)hd[pl][1] << 16);
-          u4.y = (uint32_t)hd[pl][2] | ((uint32_t)hd[pl][3] << 16);
-          u4.z = (uint32_t)hd[pl][4] | ((uint32_t)hd[pl][5] << 16);
-          u4.w = (uint32_t)hd[pl][6] | ((uint32_t)hd[pl][7] << 16);
-          *reinterpret_cast<uint4*>(base + (size_t)pl * pbytes + off) = u4;
-        }
+      for (int pl = 0; pl < FX_PLANES; ++pl) {
+        uint4 u4;
+        u4.x = (uint32_t)hd[pl][0] | ((uint32_t)hd[pl][1] << 16);
+        u4.y = (uint32_t)hd[pl][2] | ((uint32_t)hd[pl][3] << 16);
+        u4.z = (uint32_t)hd[pl][4] | ((uint32_t)hd[pl][5] << 16);
+        u4.w = (uint32_t)hd[pl][6] | ((uint32_t)hd[pl][7] << 16);
+        *reinterpret_cast<uint4*>(base + (size_t)pl * pbytes + off) = u4;
       }
     }
   }
   // the pair's partial level sums are exact integers: their sum is exact
 #pragma unroll
-  for (int f = 0; f < 2; ++f)
-#pragma unroll
-    for (int i = 0; i < FX_PLANES; ++i) lev[f][i] += __shfl_xor_sync(0xffffffffu, lev[f][i], 1);
-  if (live && par == 0) {
-    glv_n[col] = tc::fx_tail_value(lev[0], gl_tail_exp + e[0] - 35);
-    glg_n[col] = tc::fx_tail_value(lev[1], gl_tail_exp + e[1] - 35);
-  }
+  for (int i = 0; i < FX_PLANES; ++i) lev[i] += __shfl_xor_sync(0xffffffffu, lev[i], 1);
+  if (live && par == 0) (f == 0 ? glv_n : glg_n)[col] = tc::fx_tail_value(lev, gl_tail_exp + e - 35);
 }
 
 // (0,0)-mode histories: the GL GEMM left the GL values of H1(0,0), H3(0,0)
@@ -354,7 +344,7 @@ int launch_nonlinear_mixed(Handle* h, const cudaEvent_t* field_ready) {
     prof_begin(h, K_CURL32, &ev);
     // FP32 scratch for h_v, h_g: the product-grid buffer, free once the z2
     // digits are formed (2 NZ <= 6 MP rows of modes complex values)
-    k_curl<<<(unsigned)((2 * cols + CURL_THREADS - 1) / CURL_THREADS), CURL_THREADS, 0, h->stream>>>(
+    k_curl<<<(unsigned)((cols + CURL_COLS - 1) / CURL_COLS), CURL_THREADS, 0, h->stream>>>(
         h->lc64, h->iapha, h->ibeta, d, h->tgl, reinterpret_cast<float*>(h->wz32), h->bimg, h->bexp,
         h->gl_tail, h->gl_tail_exp, reinterpret_cast<double*>(h->f[F_U]) + (size_t)d.N * cols,
         reinterpret_cast<double*>(h->f[F_W]) + (size_t)d.N * cols);
