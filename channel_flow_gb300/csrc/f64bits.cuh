@@ -103,6 +103,21 @@ __host__ __device__ __forceinline__ float narrow(double x) {
   return make_f(sign, e == 0 ? 0 : er - 896, (uint32_t)(r >> 29) & 0x7fffffu);
 }
 
+// x rounded to the nearest binary32, ties to even (the hardware conversion's
+// result wherever that is a normal binary32); magnitudes below 2^-126 give
+// signed zero, 2^128 and above infinity, NaN stays NaN.
+__host__ __device__ __forceinline__ float narrow_rn(double x) {
+  const uint64_t u = d2u(x);
+  const uint32_t sign = (uint32_t)(u >> 63);
+  const int e = (int)((u >> 52) & 0x7ff);
+  if (e == 0x7ff) return u2f((sign << 31) | 0x7f800000u | ((u & 0xfffffffffffffull) ? 0x400000u : 0u));
+  // half an ulp of the 24-bit result minus one, plus the kept part's last
+  // bit: a tie carries only from an odd significand
+  const uint64_t m = u & 0x7fffffffffffffffull;
+  const uint64_t r = m + 0x0fffffffull + ((m >> 29) & 1ull);
+  return make_f(sign, e == 0 ? 0 : (int)(r >> 52) - 896, (uint32_t)(r >> 29) & 0x7fffffu);
+}
+
 // the binary64 of a binary32 (exact; binary32 subnormals give signed zero)
 __host__ __device__ __forceinline__ double widen(float f) {
   const uint32_t v = f2u(f);

@@ -405,76 +405,145 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
 // ---------------------------------------------------------------------------
 // Split a field [K rows][ncols] (rows >= kvalid are zero) into FX_PLANES digit
 // planes and write the K-major 64-column tile images plus the column
-// exponents.  One thread per column: pass 1 finds the column's largest
-// |value| (its exponent e_c: max < 2^e_c), pass 2 writes the digits of 8 rows
-// at a time as one 16-byte store per plane (consecutive threads fill
-// consecutive core-matrix rows).  grid (ntiles, 1, nfields), FX_NT threads.
+// exponents.  grid (2 ntiles, 1, nfields): a CTA takes 32 columns (half a B
+// tile) with one warp per slot q = 0 .. Q-1 (blockDim 32 Q); warp q takes
+// the 8-row groups q, q + Q, ... of the 32 columns (one coalesced row
+// segment per load).  Q = ceil(groups / SG) keeps every thread's rows in
+// registers as FP32 (SG = 2 groups for FP64 input, 3 for FP32: all loads in
+// flight at once) between the column maximum and the digits; columns longer
+// than 32 SG groups re-read the rest.  The column's largest |value|
+// (max < 2^e_c) is combined in shared memory; the digits of 8 rows go out as
+// one 16-byte store per plane, consecutive columns filling consecutive
+// core-matrix rows.
 // ---------------------------------------------------------------------------
-// max_k |(float) x_k| of a column.  For FP64 data the maximum is taken on the
-// magnitudes' bit patterns (non-negative doubles order like their bits, and
-// rounding to FP32 is monotone), so only the maximum is converted: the FP64
-// pipe, which also executes the conversions, sees one per column.
-__device__ __forceinline__ float column_absmax(const float* __restrict__ in, size_t ld, long col, int n) {
-  float mx = 0.f;
-  for (int k = 0; k < n; ++k) mx = fmaxf(mx, fabsf(in[(size_t)k * ld + col]));
-  return mx;
-}
-__device__ __forceinline__ float column_absmax(const double* __restrict__ in, size_t ld, long col, int n) {
-  unsigned long long mb = 0ull;
-  for (int k = 0; k < n; ++k)
-    mb = max(mb, (unsigned long long)__double_as_longlong(in[(size_t)k * ld + col]) & 0x7fffffffffffffffull);
-  return (float)__longlong_as_double((long long)mb);
+constexpr int SP_COLS = 32;  // columns per CTA
+template <typename InT>
+struct SplitGroups {
+  static constexpr int value = sizeof(InT) == 8 ? 2 : 3;  // 8-row groups per thread in registers
+};
+
+// FP64 inputs are rounded to FP32 (to nearest even) by integer operations:
+// the FP64 pipe, which would execute the conversions, retires about 2 per
+// clock per SM
+__device__ __forceinline__ float to_f32(float x) { return x; }
+__device__ __forceinline__ float to_f32(double x) { return bits::narrow_rn(x); }
+
+// digits of the 8 rows of group g of one column (exponent e, position r in
+// its 64-column tile): the tile image stores and, with a tail, the row's
+// level sums
+__device__ __forceinline__ void split_group(const FxPlan& plan, uint8_t* __restrict__ tile, int r, int g,
+                                            const float* v, int e, const FxTail& tail, float* lev, bool live) {
+  uint16_t h[FX_PLANES][8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    float dg[FX_PLANES];
+    fx_digits_f(v[u], e, dg);
+#pragma unroll
+    for (int i = 0; i < FX_PLANES; ++i) h[i][u] = bf16_bits(dg[i]);
+    if (tail.adig) fx_tail_mac(tail.adig, plan.kpad, 8 * g + u, dg, lev);
+  }
+  if (!live) return;
+  const int ch = (8 * g) / TC_KC;
+  const int kl = 8 * g - ch * TC_KC;
+  const uint32_t pbytes = (uint32_t)FX_NT * plan.kc[ch] * 2u;
+  uint8_t* base = tile + plan.b_chunk_off[ch];
+  // core matrix (column group r / 8, k group kl / 8) of a 64-column tile
+  const size_t off = ((size_t)(kl / 8) * (FX_NT / 8) + r / 8) * 128 + (r % 8) * 16;
+#pragma unroll
+  for (int pl = 0; pl < FX_PLANES; ++pl) {
+    uint4 w;
+    w.x = (uint32_t)h[pl][0] | ((uint32_t)h[pl][1] << 16);
+    w.y = (uint32_t)h[pl][2] | ((uint32_t)h[pl][3] << 16);
+    w.z = (uint32_t)h[pl][4] | ((uint32_t)h[pl][5] << 16);
+    w.w = (uint32_t)h[pl][6] | ((uint32_t)h[pl][7] << 16);
+    *reinterpret_cast<uint4*>(base + (size_t)pl * pbytes + off) = w;
+  }
 }
 
 // tail (optional): one more output row that the GEMM's plan leaves out,
 // computed exactly as the GEMM would (the row's digit planes tail.adig, its
-// exponent tail.aexp; levels i + j <= 3 summed exactly in FP32, combined in
-// 64 bits) from the column's digits formed in the second pass, written as
-// FP64 to tail.out.p[f][col].
+// exponent tail.aexp; levels i + j <= 3 summed exactly in FP32 -- the
+// threads' partial sums and their total are integers below 2^24, so adding
+// them in shared memory is exact in any order -- combined in 64 bits),
+// written as FP64 to tail.out.p[f][col].
 template <typename InT>
-__global__ void __launch_bounds__(FX_NT) k_tc_split_fx(const __grid_constant__ FxPlan plan,
-                                                       const __grid_constant__ Ptr8<const InT> ins, int kvalid,
-                                                       uint8_t* __restrict__ bimg, int* __restrict__ bexp,
-                                                       const __grid_constant__ FxTail tail) {
-  const int nt = blockIdx.x, f = blockIdx.z, r = threadIdx.x;
+__global__ void __launch_bounds__(1024) k_tc_split_fx(const __grid_constant__ FxPlan plan,
+                                                      const __grid_constant__ Ptr8<const InT> ins, int kvalid,
+                                                      uint8_t* __restrict__ bimg, int* __restrict__ bexp,
+                                                      const __grid_constant__ FxTail tail) {
+  constexpr int SG = SplitGroups<InT>::value;
+  __shared__ int s_max[SP_COLS];  // column maxima as float bits (non-negative floats order as integers)
+  __shared__ float s_lev[FX_PLANES][SP_COLS];
+  const int f = blockIdx.z;
+  const int lane = threadIdx.x & 31, q = threadIdx.x >> 5, Q = blockDim.x >> 5;
   const InT* in = ins.p[f];
-  const long col = (long)nt * FX_NT + r;
+  const long col = (long)blockIdx.x * SP_COLS + lane;
+  const int nt = blockIdx.x >> 1, r = (blockIdx.x & 1) * SP_COLS + lane;  // tile, column in the tile
   const bool live = col < plan.ncols;
-  const float mx = live ? column_absmax(in, (size_t)plan.ncols, col, kvalid) : 0.f;
-  float lev[FX_PLANES] = {0.f, 0.f, 0.f, 0.f};
-  int e = 0;
-  if (mx > 0.f) (void)frexpf(mx, &e);  // mx = m 2^e, m in [0.5, 1)
-  bexp[(size_t)f * plan.bexp_stride() + col] = e;
-  uint8_t* tile = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes;
-  for (int g = 0; g < plan.kpad / 8; ++g) {
-    uint16_t h[FX_PLANES][8];
+  const int ng = plan.kpad / 8;
+  if (threadIdx.x < SP_COLS) {
+    s_max[threadIdx.x] = 0;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int k = 8 * g + q;
-      const float x = (live && k < kvalid) ? (float)in[(size_t)k * plan.ncols + col] : 0.f;
-      float dg[FX_PLANES];
-      fx_digits_f(x, e, dg);
+    for (int i = 0; i < FX_PLANES; ++i) s_lev[i][threadIdx.x] = 0.f;
+  }
+  // all of a thread's loads first, then their FP32 values
+  InT raw[SG][8];
 #pragma unroll
-      for (int i = 0; i < FX_PLANES; ++i) h[i][q] = bf16_bits(dg[i]);
-      if (tail.adig) fx_tail_mac(tail.adig, plan.kpad, k, dg, lev);
-    }
-    const int ch = (8 * g) / TC_KC;
-    const int kl = 8 * g - ch * TC_KC;
-    const uint32_t pbytes = (uint32_t)FX_NT * plan.kc[ch] * 2u;
-    uint8_t* base = tile + plan.b_chunk_off[ch];
-    // core matrix (column group r / 8, k group kl / 8) of a 64-column tile
-    const size_t off = ((size_t)(kl / 8) * (FX_NT / 8) + r / 8) * 128 + (r % 8) * 16;
+  for (int j = 0; j < SG; ++j) {
+    const int g = q + Q * j;
 #pragma unroll
-    for (int pl = 0; pl < FX_PLANES; ++pl) {
-      uint4 v;
-      v.x = (uint32_t)h[pl][0] | ((uint32_t)h[pl][1] << 16);
-      v.y = (uint32_t)h[pl][2] | ((uint32_t)h[pl][3] << 16);
-      v.z = (uint32_t)h[pl][4] | ((uint32_t)h[pl][5] << 16);
-      v.w = (uint32_t)h[pl][6] | ((uint32_t)h[pl][7] << 16);
-      *reinterpret_cast<uint4*>(base + (size_t)pl * pbytes + off) = v;
+    for (int u = 0; u < 8; ++u) {
+      const int k = 8 * g + u;
+      raw[j][u] = (live && g < ng && k < kvalid) ? in[(size_t)k * plan.ncols + col] : (InT)0;
     }
   }
-  if (tail.adig && live) tail.out.p[f][col] = fx_tail_value(lev, tail.aexp + e - 35);
+  float x[SG][8];
+  float mx = 0.f;
+#pragma unroll
+  for (int j = 0; j < SG; ++j)
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      x[j][u] = to_f32(raw[j][u]);
+      mx = fmaxf(mx, fabsf(x[j][u]));
+    }
+  for (int g = q + Q * SG; g < ng; g += Q)
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int k = 8 * g + u;
+      if (live && k < kvalid) mx = fmaxf(mx, fabsf(to_f32(in[(size_t)k * plan.ncols + col])));
+    }
+  __syncthreads();
+  atomicMax(&s_max[lane], __float_as_int(mx));
+  __syncthreads();
+  int e = 0;
+  const float cm = __int_as_float(s_max[lane]);
+  if (cm > 0.f) (void)frexpf(cm, &e);  // cm = m 2^e, m in [0.5, 1)
+  if (q == 0) bexp[(size_t)f * plan.bexp_stride() + col] = e;
+  uint8_t* tile = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes;
+  float lev[FX_PLANES] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int j = 0; j < SG; ++j) {
+    const int g = q + Q * j;
+    if (g < ng) split_group(plan, tile, r, g, x[j], e, tail, lev, live);
+  }
+  for (int g = q + Q * SG; g < ng; g += Q) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int k = 8 * g + u;
+      v[u] = (live && k < kvalid) ? to_f32(in[(size_t)k * plan.ncols + col]) : 0.f;
+    }
+    split_group(plan, tile, r, g, v, e, tail, lev, live);
+  }
+  if (tail.adig) {
+#pragma unroll
+    for (int i = 0; i < FX_PLANES; ++i) atomicAdd(&s_lev[i][lane], lev[i]);
+    __syncthreads();
+    if (q == 0 && live) {
+      const float tot[FX_PLANES] = {s_lev[0][lane], s_lev[1][lane], s_lev[2][lane], s_lev[3][lane]};
+      tail.out.p[f][col] = fx_tail_value(tot, tail.aexp + e - 35);
+    }
+  }
 }
 
 FxPlan make_fx_plan(int mvalid, int kvalid, long ncols) {
@@ -577,10 +646,14 @@ int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int
 template <typename InT>
 int launch_tc_split_fx(Handle* h, const FxPlan& p, const Ptr8<const InT>& ins, int kvalid, uint8_t* bimg,
                        int* bexp, int nfields, int kid, const FxTail& tail) {
-  dim3 grid(p.ntiles, 1, nfields);
+  // warps per CTA: enough that each thread's groups fit in registers, at
+  // most 32 (longer columns re-read their remaining groups)
+  const int ng = p.kpad / 8, sg = SplitGroups<InT>::value;
+  const int nq = std::min(32, (ng + sg - 1) / sg);
+  dim3 grid(2 * p.ntiles, 1, nfields);
   cudaEvent_t ev;
   prof_begin(h, kid, &ev);
-  k_tc_split_fx<InT><<<grid, FX_NT, 0, h->stream>>>(p, ins, kvalid, bimg, bexp, tail);
+  k_tc_split_fx<InT><<<grid, 32 * nq, 0, h->stream>>>(p, ins, kvalid, bimg, bexp, tail);
   prof_end(h, kid, ev);
   return cuda_ok(h, cudaGetLastError(), "k_tc_split_fx") ? CHF_OK : CHF_E_CUDA;
 }

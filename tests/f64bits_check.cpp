@@ -24,6 +24,7 @@ int main() {
     const float n = narrow(x);
     const float nref = std::fabs(x) >= std::ldexp(1.0, -126) ? static_cast<float>(x) : 0.f;  // flush
     if (n != nref) return fail("narrow", x, n, nref);
+    if (narrow_rn(x) != nref) return fail("narrow_rn", x, narrow_rn(x), nref);
     // split: hi is x truncated to 24 bits, lo the next 23 bits
     float hi, lo;
     split(x, hi, lo);
@@ -51,6 +52,13 @@ int main() {
   // rounding carry into the exponent and the smallest normal
   const double up = std::nextafter(2.0, 0.0);  // rounds up to 2.0f
   if (narrow(up) != 2.0f) return fail("carry", up, narrow(up), 2.0);
+  if (narrow_rn(up) != static_cast<float>(up)) return fail("carry rn", up, narrow_rn(up), static_cast<float>(up));
+  // exact ties go to the even significand, as the compiler's conversion does
+  for (double t : {1.0 + std::ldexp(1.0, -24), 1.0 + 3.0 * std::ldexp(1.0, -24), -(1.0 + 3.0 * std::ldexp(1.0, -24)),
+                   std::ldexp(1.0 + std::ldexp(1.0, -24), 100), 2.0 - std::ldexp(1.0, -25)})
+    if (narrow_rn(t) != static_cast<float>(t)) return fail("tie rn", t, narrow_rn(t), static_cast<float>(t));
+  if (!std::isinf(narrow_rn(1e300)) || !std::isnan(narrow_rn(std::nan(""))) || narrow_rn(1e-300) != 0.f)
+    return fail("special rn", 0, 0, 0);
   const double tiny = std::ldexp(1.0, -126);
   if (narrow(tiny) != static_cast<float>(tiny)) return fail("min normal", tiny, narrow(tiny), tiny);
   for (double x : {1.0, -3.5, 1e-300, -7e200, 0.0, std::ldexp(1.0, -1021)})
