@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
 // FP64 operations per element; the factors 2 (k + 1) are built by integer
 // operations; RC_PF steps of v and omega_y loaded ahead.
 // ---------------------------------------------------------------------------
-constexpr int RC_THREADS = 64;
+constexpr int RC_THREADS = 32;  // one warp: 1024 CTAs at 128^3, balanced over the SMs
 constexpr int RC_PF = 8;  // steps of v, omega_y loaded ahead of the recurrences
 
 __global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict__ v, const cd* __restrict__ g,
