@@ -126,9 +126,12 @@ def kernel_work(cfg, zpad=0, precision="fp64"):
     def kp(k):
         return (k + 15) // 16 * 16
 
-    img = 4 * 2  # four bf16 planes per element
-    w["k_tc_split_z1"] = (6 * NZ * cols * 8 + 6 * kp(NZ) * cols * img, 0)
-    w["k_tc_gemm_z1"] = (6 * kp(NZ) * cols * img + 6 * MP * cols * 4, 6 * 10 * 2 * 256 * cols * kp(NZ))
+    img = 4 * 2  # four bf16 planes per element (Z2, GL: 10 digit products)
+    # Z1: three planes of 8-bit digits, 6 products, where K (padded) <= 204
+    np1 = 3 if kp(NZ) <= 204 else 4
+    img1, prod1 = np1 * 2, (6 if np1 == 3 else 10)
+    w["k_tc_split_z1"] = (6 * NZ * cols * 8 + 6 * kp(NZ) * cols * img1, 0)
+    w["k_tc_gemm_z1"] = (6 * kp(NZ) * cols * img1 + 6 * MP * cols * 4, 6 * prod1 * 2 * 256 * cols * kp(NZ))
     w["k_tc_split_z2"] = (3 * MP * cols * 4 + 3 * kp(MP) * cols * img, 0)
     # Z2 and GL run one 128-row tile (rows 0..N-1); row N is formed beside the digits
     w["k_tc_gemm_z2"] = (3 * kp(MP) * cols * img + 3 * N * cols * 8, 3 * 10 * 2 * N * cols * kp(MP))

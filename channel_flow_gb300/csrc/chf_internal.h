@@ -35,10 +35,14 @@ struct Dims {
 
 // Tensor-core GEMM plans (k_tcgemm.cu): K in chunks of at most TC_KC.
 constexpr int TC_KC = 32;
-constexpr int FX_PLANES = 4;     // digit planes per operand
+constexpr int FX_PLANES = 4;     // digit planes per operand (the most a plan uses)
 constexpr int FX_NT = 64;        // columns per B tile
 struct FxPlan {
   int mvalid, mtiles, kpad, ntiles, nchunks;
+  // digit format: 4 planes of 7-bit digits (levels 0..3, about 2^-28 of the
+  // row and column maxima), or 3 planes of 8-bit digits (levels 0..2, about
+  // 2^-24: for transforms whose output is FP32)
+  int planes;
   long ncols;
   int kc[24];  // K <= 680 (the exactness bound) in chunks of TC_KC
   size_t a_chunk_off[24], b_chunk_off[24];
@@ -208,7 +212,7 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
 // signed 7-bit integer digits below a per-row (A) / per-column (B) power of
 // two, products of digits accumulated exactly per level i + j <= 3.
 // 128-row A tiles, 64-column B tiles (two CTAs per SM fit in TMEM).
-FxPlan make_fx_plan(int mvalid, int kvalid, long ncols);
+FxPlan make_fx_plan(int mvalid, int kvalid, long ncols, int planes = FX_PLANES);
 std::vector<uint8_t> make_a_image_fx(const FxPlan& p, const std::vector<double>& a, int M, int K,
                                      std::vector<int>& row_exp);
 template <typename OutT>

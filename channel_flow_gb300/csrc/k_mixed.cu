@@ -212,7 +212,10 @@ int setup_mixed(Handle* h) {
   // last coefficient / the wall point z = -1, is formed beside the digits by
   // k_tc_split_fx and k_curl with the same exact level sums, instead of by a
   // second row tile of MMAs
-  h->tz1 = make_fx_plan(MP, NZ, cols);
+  // Z1's values go to FP32 products: 3-plane digits (about 2^-24 of the row
+  // and column maxima, as an FP32 GEMM) suffice there, where their level sums
+  // stay exact (K padded to at most 204); 4 planes beyond that
+  h->tz1 = make_fx_plan(MP, NZ, cols, (NZ + 15) / 16 * 16 <= 204 ? 3 : 4);
   h->tz2 = make_fx_plan(N, MP, cols);
   h->tgl = make_fx_plan(N, NZ, cols);
   std::vector<double> a1((size_t)MP * NZ), a2((size_t)NZ * MP), a3((size_t)NZ * NZ);

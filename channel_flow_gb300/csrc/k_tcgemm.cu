@@ -13,23 +13,27 @@
 // as with the z transforms done in FP64).
 //
 // How: every row m of A is scaled by 2^-f_m and every column c of B by
-// 2^-e_c (powers of two, so exactly) into (-1, 1), then written as
-// FX_PLANES digits of 7 bits:
-//     x = sum_i d_i 2^(-7 (i + 1)),   d_0 in [-128, 128], d_i in [-64, 64]
-// (each digit is rint of the scaled remainder, so all steps are exact).
-// Digits are integers of at most 8 bits, exact in bf16.  The products of
-// one level L = i + j (at most four planes pairs) summed over K <= 680 stay
-// integers below 2^24, so tensor-core FP32 accumulation of a level is EXACT
-// (the launcher checks K).  B data are taken as FP32 (FP64 coefficients are
-// rounded to FP32 first: a relative error per coefficient, not a flat floor).  Levels
-// 0..3 (ten products) go to four TMEM accumulators; the epilogue forms
-//     C = 2^(f_m + e_c - 14) * sum_L 2^(-7 L) acc_L
-// exactly: the four levels combine into one 64-bit integer
-//     t = acc_0 2^21 + acc_1 2^14 + acc_2 2^7 + acc_3,   |t| < 2^46,
+// 2^-e_c (powers of two, so exactly) into (-1, 1), then written as NP digit
+// planes (each digit the rint of the scaled remainder, so all steps are
+// exact; digits are integers of at most 9 bits, exact in bf16):
+//   NP = 4:  x = sum_i d_i 2^(-7 (i + 1)),  d_0 in [-128, 128], d_i in [-64, 64]
+//   NP = 3:  x = sum_i d_i 2^(-8 (i + 1)),  d_0 in [-256, 256], d_i in [-128, 128]
+// The products of one level L = i + j summed over K stay integers below 2^24
+// (K <= 680 for NP = 4, K <= 204 for NP = 3; the launcher checks), so
+// tensor-core FP32 accumulation of a level is EXACT.  B data are taken as
+// FP32 (FP64 coefficients are rounded to FP32 first: a relative error per
+// coefficient, not a flat floor).  Levels 0..NP-1 (ten or six products) go
+// to NP TMEM accumulators; the epilogue combines them exactly into one
+// 64-bit integer
+//   NP = 4:  t = acc_0 2^21 + acc_1 2^14 + acc_2 2^7 + acc_3,   |t| < 2^46
+//   NP = 3:  t = acc_0 2^16 + acc_1 2^8 + acc_2,                 |t| < 2^41
 // converted once (exactly to FP64, correctly rounded to FP32) and scaled by
-// 2^(f_m + e_c - 35).  What is dropped -- levels >= 4 and the digit
-// remainders -- is below 2^-28 of max|A row| * max|B column| per term,
-// instead of 2^-24 of each running FP32 sum.
+// 2^(f_m + e_c - 35) or 2^(f_m + e_c - 32).  What is dropped -- the higher
+// levels and the digit remainders -- is below 2^-28 (NP = 4) or 2^-24
+// (NP = 3) of max|A row| * max|B column| per term, instead of 2^-24 of each
+// running FP32 sum.  The 4-plane format serves the transforms whose output
+// is differentiated (Z2, GL); Z1, whose values go to FP32 products, uses 3
+// planes (six MMAs per K16 slice instead of ten).
 //
 // Operand images: each 128-row tile of A and each 64-column tile of B is
 // stored in HBM already in the shared-memory "core matrix" layout that
@@ -63,16 +67,15 @@ namespace {
 
 using namespace tc;
 
-constexpr int FX_LEVELS = 4;  // products d_i e_j with i + j <= 3
-constexpr uint32_t FX_TMEM_COLS = (uint32_t)FX_NT * FX_LEVELS;
-
-// FX_PLANES digits of x * 2^-e on the host (exact in double)
-void fx_digits_host(double x, int e, double* dg) {
-  double y = std::scalbn(x, 7 - e);
-  for (int i = 0; i < FX_PLANES; ++i) {
+// np digits of x * 2^-e on the host (exact in double), the format of
+// fx_digits_np: radix 2^7 for 4 planes, 2^8 for 3
+void fx_digits_host(double x, int e, double* dg, int np) {
+  const int rb = np == 4 ? 7 : 8;
+  double y = std::scalbn(x, rb - e);
+  for (int i = 0; i < np; ++i) {
     const double di = std::rint(y);
     dg[i] = di;
-    y = (y - di) * 128.0;
+    y = (y - di) * (double)(1 << rb);
   }
 }
 
@@ -92,10 +95,10 @@ void fx_digits_host(double x, int e, double* dg) {
 //   warp 0    producer: per K chunk of an item waits for a free stage, then
 //             moves the chunk's plane images with cp.async.bulk (completion
 //             counted in bytes on the stage's "full" barrier);
-//   warps 1-2 MMA issuers (levels {0, 3} and {1, 2}, 5 of the 10 products
-//             each: one thread's MMA issue rate, not the tensor pipe, bounds
-//             these 128x64x16 MMAs): wait for a free accumulator set (two sets
-//             of four 64-column level accumulators, so one item's epilogue
+//   warps 1-2 MMA issuers (4 planes: levels {0, 3} and {1, 2}, 5 of the 10
+//             products each; 3 planes: levels {0, 1} and {2}, 3 of the 6):
+//             wait for a free accumulator set (two sets of NP 64-column level
+//             accumulators, so one item's epilogue
 //             overlaps the next item's MMAs), per chunk wait for "full", issue
 //             their level MMAs per K16 slice (descriptors formed once per chunk,
 //             advanced by a constant per slice) and commit to the stage's
@@ -112,39 +115,57 @@ void fx_digits_host(double x, int e, double* dg) {
 // instruction descriptor: D = F32, A = B = BF16, both K-major, M = 128, N = 64
 constexpr uint32_t IDESC_FX = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 constexpr int WS_STAGES = 4;
-constexpr int WS_MMA_WARPS = 2;  // issuers: levels {0, 3} and {1, 2}, 5 products each
+constexpr int WS_MMA_WARPS = 2;  // issuers on disjoint level accumulators
 constexpr int WS_EPI_WARPS = 8;
 constexpr int WS_EPI0 = 1 + WS_MMA_WARPS;  // first epilogue warp
 constexpr int WS_THREADS = 32 * (WS_EPI0 + WS_EPI_WARPS);
 constexpr uint32_t WS_A_PLANE = 128u * TC_KC * 2u;
 constexpr uint32_t WS_B_PLANE = (uint32_t)FX_NT * TC_KC * 2u;
-constexpr uint32_t WS_B_STAGE = (uint32_t)FX_PLANES * WS_B_PLANE;
-constexpr uint32_t WS_AB_STAGE = (uint32_t)FX_PLANES * (WS_A_PLANE + WS_B_PLANE);
-constexpr uint32_t WS_TMEM_COLS = 2u * FX_TMEM_COLS;  // two accumulator sets
-constexpr size_t WS_SMEM_LIMIT = 225u * 1024u;        // dynamic, below the 227 KB opt-in
+// one stage of the ring: the B planes of a K chunk (A resident), or A and B
+__host__ __device__ constexpr uint32_t ws_b_stage(int np) { return (uint32_t)np * WS_B_PLANE; }
+__host__ __device__ constexpr uint32_t ws_ab_stage(int np) { return (uint32_t)np * (WS_A_PLANE + WS_B_PLANE); }
+// two accumulator sets of np 64-column level accumulators (allocation: all 512)
+constexpr uint32_t WS_TMEM_COLS = 512u;
+constexpr size_t WS_SMEM_LIMIT = 225u * 1024u;  // dynamic, below the 227 KB opt-in
 
 __host__ __device__ inline size_t ws_a_resident_bytes(const FxPlan& p) { return (p.a_tile_bytes + 1023) / 1024 * 1024; }
 __host__ __device__ inline bool ws_resident(const FxPlan& p) {
-  return ws_a_resident_bytes(p) + (size_t)WS_STAGES * WS_B_STAGE <= WS_SMEM_LIMIT;
+  return ws_a_resident_bytes(p) + (size_t)WS_STAGES * ws_b_stage(p.planes) <= WS_SMEM_LIMIT;
 }
 
-// one output from the four exact level sums: t 2^n, |t| < 2^46, with
-// t = acc_0 2^21 + acc_1 2^14 + acc_2 2^7 + acc_3 (the levels can cancel, so
-// t is formed exactly before the single rounding)
+// one output from the exact level sums: t 2^n with
+//   4 planes: t = acc_0 2^21 + acc_1 2^14 + acc_2 2^7 + acc_3,  |t| < 2^46
+//   3 planes: t = acc_0 2^16 + acc_1 2^8 + acc_2,              |t| < 2^41
+// (the levels can cancel, so t is formed exactly before the single rounding)
+template <int NP>
 __device__ __forceinline__ long long fx_level_sum(const uint32_t* acc) {
-  return ((long long)__float2int_rn(__uint_as_float(acc[0])) << 21) +
-         ((long long)__float2int_rn(__uint_as_float(acc[1])) << 14) +
-         ((long long)__float2int_rn(__uint_as_float(acc[2])) << 7) +
-         (long long)__float2int_rn(__uint_as_float(acc[3]));
+  if (NP == 4)
+    return ((long long)__float2int_rn(__uint_as_float(acc[0])) << 21) +
+           ((long long)__float2int_rn(__uint_as_float(acc[1])) << 14) +
+           ((long long)__float2int_rn(__uint_as_float(acc[2])) << 7) +
+           (long long)__float2int_rn(__uint_as_float(acc[NP - 1]));
+  return ((long long)__float2int_rn(__uint_as_float(acc[0])) << 16) +
+         ((long long)__float2int_rn(__uint_as_float(acc[1])) << 8) + (long long)__float2int_rn(__uint_as_float(acc[2]));
 }
-template <typename OutT>
+// the power of two of t: 2^(f_m + e_c - FX_SHIFT) (two digit radices for the
+// first digits, one per level)
+template <int NP>
+__host__ __device__ constexpr int fx_shift() { return NP == 4 ? 35 : 32; }
+template <typename OutT, int NP>
 __device__ __forceinline__ OutT fx_out(const uint32_t* acc, int n);
 // FP32: t = t_h 2^23 + t_l with |t_h| < 2^23 and 0 <= t_l < 2^23, both exact
 // in binary32, so one FMA rounds the exact t once (to nearest even); the
 // scaling by 2^n is two exact power-of-two multiplies
 template <>
-__device__ __forceinline__ float fx_out<float>(const uint32_t* acc, int n) {
-  const long long t = fx_level_sum(acc);
+__device__ __forceinline__ float fx_out<float, 4>(const uint32_t* acc, int n) {
+  const long long t = fx_level_sum<4>(acc);
+  const float v = __fmaf_rn(__int2float_rn((int)(t >> 23)), 8388608.0f, __int2float_rn((int)(t & 0x7fffff)));
+  const int h = n / 2;  // two factors keep each power of two in range
+  return v * __int_as_float((127 + h) << 23) * __int_as_float((127 + n - h) << 23);
+}
+template <>
+__device__ __forceinline__ float fx_out<float, 3>(const uint32_t* acc, int n) {
+  const long long t = fx_level_sum<3>(acc);
   const float v = __fmaf_rn(__int2float_rn((int)(t >> 23)), 8388608.0f, __int2float_rn((int)(t & 0x7fffff)));
   const int h = n / 2;  // two factors keep each power of two in range
   return v * __int_as_float((127 + h) << 23) * __int_as_float((127 + n - h) << 23);
@@ -152,8 +173,12 @@ __device__ __forceinline__ float fx_out<float>(const uint32_t* acc, int n) {
 // FP64: exact, built from the 64-bit integer by bit operations (off the
 // narrow FP64 pipe)
 template <>
-__device__ __forceinline__ double fx_out<double>(const uint32_t* acc, int n) {
-  return bits::scaled_i64(fx_level_sum(acc), n);
+__device__ __forceinline__ double fx_out<double, 4>(const uint32_t* acc, int n) {
+  return bits::scaled_i64(fx_level_sum<4>(acc), n);
+}
+template <>
+__device__ __forceinline__ double fx_out<double, 3>(const uint32_t* acc, int n) {
+  return bits::scaled_i64(fx_level_sum<3>(acc), n);
 }
 
 __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
@@ -170,7 +195,7 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-template <typename OutT>
+template <typename OutT, int NP>
 __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_constant__ FxPlan plan,
                                                               const uint8_t* __restrict__ aimg,
                                                               const int* __restrict__ aexp,
@@ -183,14 +208,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
   __shared__ uint32_t tmem_base;
   __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  constexpr int NP = FX_PLANES;
+  constexpr uint32_t SET_COLS = (uint32_t)FX_NT * NP;  // one accumulator set: NP levels
   const bool resident = ws_resident(plan);
   const int mt = (int)(blockIdx.x % plan.mtiles);
   const long j0 = blockIdx.x / plan.mtiles, jstep = gridDim.x / plan.mtiles;
   const long njobs = (long)nfields * plan.ntiles;  // (field, column tile) items of this row tile
   uint8_t* sAres = smem;                                            // resident A tile
   uint8_t* ring = resident ? smem + ws_a_resident_bytes(plan) : smem;  // stages
-  const uint32_t stage_bytes = resident ? WS_B_STAGE : WS_AB_STAGE;
+  const uint32_t stage_bytes = resident ? ws_b_stage(NP) : ws_ab_stage(NP);
   if (tid == 0) {
     s_fail = 0;
     for (int i = 0; i < WS_STAGES; ++i) {
@@ -255,8 +280,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
     }
   } else if (warp < WS_EPI0) {
     // ---------------- MMA issuers ----------------
-    // issuer 0 owns the level-0 and level-3 accumulators, issuer 1 levels 1
-    // and 2: disjoint accumulators, 5 products per K16 slice each
+    // the two issuers own disjoint level accumulators (see the selection
+    // below), with equal numbers of products per K16 slice
     const int mw = warp - 1;
     if (lane == 0) {
       // K-adjacent core matrices: 16 (A, 128 rows) or 8 (B, 64 columns)
@@ -274,7 +299,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t tacc = tmem + b * FX_TMEM_COLS;
+        const uint32_t tacc = tmem + b * SET_COLS;
         for (int ch = 0; ch < plan.nchunks; ++ch, ++g) {
           const uint32_t s = g % WS_STAGES, ph = (g / WS_STAGES) & 1u;
           if (!mbar_wait(smem_u32(&full[s]), ph)) {
@@ -300,10 +325,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
             // accumulator between neighbours); each level's first MMA (i = 0)
             // comes in round 0
 #pragma unroll
-            for (int i = 0; i < FX_LEVELS; ++i) {
+            for (int i = 0; i < NP; ++i) {
 #pragma unroll
-              for (int L = i; L < FX_LEVELS; ++L) {
-                if ((L == 0 || L == 3) != (mw == 0)) continue;
+              for (int L = i; L < NP; ++L) {
+                // issuer 0: levels {0, 3} (4 planes) or {0, 1} (3 planes)
+                if ((NP == 4 ? (L == 0 || L == 3) : L < 2) != (mw == 0)) continue;
                 const uint32_t accum = (first && i == 0) ? 0u : 1u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -350,10 +376,10 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
 #pragma unroll
       for (int g2 = 0; g2 < 2; ++g2) {
         const int c0 = cbase + 16 * g2;
-        uint32_t r[FX_LEVELS][16];
+        uint32_t r[NP][16];
 #pragma unroll
-        for (int L = 0; L < FX_LEVELS; ++L) {
-          const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * FX_TMEM_COLS + (uint32_t)(L * FX_NT + c0);
+        for (int L = 0; L < NP; ++L) {
+          const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * SET_COLS + (uint32_t)(L * FX_NT + c0);
           asm volatile(
               "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
               "[%16];"
@@ -376,8 +402,10 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
           OutT v[16];
 #pragma unroll
           for (int qq = 0; qq < 16; ++qq) {
-            const uint32_t acc[FX_LEVELS] = {r[0][qq], r[1][qq], r[2][qq], r[3][qq]};
-            v[qq] = fx_out<OutT>(acc, fm + ec[qq] - 35);
+            uint32_t acc[NP];
+#pragma unroll
+            for (int L = 0; L < NP; ++L) acc[L] = r[L][qq];
+            v[qq] = fx_out<OutT, NP>(acc, fm + ec[qq] - fx_shift<NP>());
           }
           // a thread's 16 outputs are consecutive in its row: 16-byte stores
           // when the group is whole and aligned, element stores otherwise
@@ -403,7 +431,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
 }
 
 // ---------------------------------------------------------------------------
-// Split a field [K rows][ncols] (rows >= kvalid are zero) into FX_PLANES digit
+// Split a field [K rows][ncols] (rows >= kvalid are zero) into NP digit
 // planes and write the K-major 64-column tile images plus the column
 // exponents.  grid (2 ntiles, 1, nfields): a CTA takes 32 columns (half a B
 // tile) with one warp per slot q = 0 .. Q-1 (blockDim 32 Q); warp q takes
@@ -431,16 +459,17 @@ __device__ __forceinline__ float to_f32(double x) { return bits::narrow_rn(x); }
 // digits of the 8 rows of group g of one column (exponent e, position r in
 // its 64-column tile): the tile image stores and, with a tail, the row's
 // level sums
+template <int NP>
 __device__ __forceinline__ void split_group(const FxPlan& plan, uint8_t* __restrict__ tile, int r, int g,
                                             const float* v, int e, const FxTail& tail, float* lev, bool live) {
-  uint16_t h[FX_PLANES][8];
+  uint16_t h[NP][8];
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
     float dg[FX_PLANES];
-    fx_digits_f(v[u], e, dg);
+    fx_digits_np<NP>(v[u], e, dg);
 #pragma unroll
-    for (int i = 0; i < FX_PLANES; ++i) h[i][u] = bf16_bits(dg[i]);
-    if (tail.adig) fx_tail_mac(tail.adig, plan.kpad, 8 * g + u, dg, lev);
+    for (int i = 0; i < NP; ++i) h[i][u] = bf16_bits(dg[i]);
+    if (NP == 4 && tail.adig) fx_tail_mac(tail.adig, plan.kpad, 8 * g + u, dg, lev);
   }
   if (!live) return;
   const int ch = (8 * g) / TC_KC;
@@ -450,7 +479,7 @@ __device__ __forceinline__ void split_group(const FxPlan& plan, uint8_t* __restr
   // core matrix (column group r / 8, k group kl / 8) of a 64-column tile
   const size_t off = ((size_t)(kl / 8) * (FX_NT / 8) + r / 8) * 128 + (r % 8) * 16;
 #pragma unroll
-  for (int pl = 0; pl < FX_PLANES; ++pl) {
+  for (int pl = 0; pl < NP; ++pl) {
     uint4 w;
     w.x = (uint32_t)h[pl][0] | ((uint32_t)h[pl][1] << 16);
     w.y = (uint32_t)h[pl][2] | ((uint32_t)h[pl][3] << 16);
@@ -465,8 +494,8 @@ __device__ __forceinline__ void split_group(const FxPlan& plan, uint8_t* __restr
 // exponent tail.aexp; levels i + j <= 3 summed exactly in FP32 -- the
 // threads' partial sums and their total are integers below 2^24, so adding
 // them in shared memory is exact in any order -- combined in 64 bits),
-// written as FP64 to tail.out.p[f][col].
-template <typename InT>
+// written as FP64 to tail.out.p[f][col].  Tails are for 4-plane plans.
+template <typename InT, int NP>
 __global__ void __launch_bounds__(1024) k_tc_split_fx(const __grid_constant__ FxPlan plan,
                                                       const __grid_constant__ Ptr8<const InT> ins, int kvalid,
                                                       uint8_t* __restrict__ bimg, int* __restrict__ bexp,
@@ -524,7 +553,7 @@ __global__ void __launch_bounds__(1024) k_tc_split_fx(const __grid_constant__ Fx
 #pragma unroll
   for (int j = 0; j < SG; ++j) {
     const int g = q + Q * j;
-    if (g < ng) split_group(plan, tile, r, g, x[j], e, tail, lev, live);
+    if (g < ng) split_group<NP>(plan, tile, r, g, x[j], e, tail, lev, live);
   }
   for (int g = q + Q * SG; g < ng; g += Q) {
     float v[8];
@@ -533,9 +562,9 @@ __global__ void __launch_bounds__(1024) k_tc_split_fx(const __grid_constant__ Fx
       const int k = 8 * g + u;
       v[u] = (live && k < kvalid) ? to_f32(in[(size_t)k * plan.ncols + col]) : 0.f;
     }
-    split_group(plan, tile, r, g, v, e, tail, lev, live);
+    split_group<NP>(plan, tile, r, g, v, e, tail, lev, live);
   }
-  if (tail.adig) {
+  if (NP == 4 && tail.adig) {
 #pragma unroll
     for (int i = 0; i < FX_PLANES; ++i) atomicAdd(&s_lev[i][lane], lev[i]);
     __syncthreads();
@@ -546,8 +575,9 @@ __global__ void __launch_bounds__(1024) k_tc_split_fx(const __grid_constant__ Fx
   }
 }
 
-FxPlan make_fx_plan(int mvalid, int kvalid, long ncols) {
+FxPlan make_fx_plan(int mvalid, int kvalid, long ncols, int planes) {
   FxPlan p{};
+  p.planes = planes;
   p.mvalid = mvalid;
   p.mtiles = (mvalid + 127) / 128;
   p.kpad = (kvalid + 15) / 16 * 16;
@@ -559,8 +589,8 @@ FxPlan make_fx_plan(int mvalid, int kvalid, long ncols) {
     p.kc[c] = std::min(TC_KC, p.kpad - c * TC_KC);
     p.a_chunk_off[c] = oa;
     p.b_chunk_off[c] = ob;
-    oa += (size_t)FX_PLANES * 128 * p.kc[c] * 2;
-    ob += (size_t)FX_PLANES * FX_NT * p.kc[c] * 2;
+    oa += (size_t)p.planes * 128 * p.kc[c] * 2;
+    ob += (size_t)p.planes * FX_NT * p.kc[c] * 2;
   }
   p.a_tile_bytes = oa;
   p.b_tile_bytes = ob;
@@ -584,13 +614,13 @@ std::vector<uint8_t> make_a_image_fx(const FxPlan& p, const std::vector<double>&
     for (int k = 0; k < p.kpad; ++k) {
       const double x = (m < M && k < K) ? a[(size_t)m * K + k] : 0.0;
       double dg[FX_PLANES];
-      fx_digits_host(x, row_exp[m], dg);
+      fx_digits_host(x, row_exp[m], dg, p.planes);
       const int mt = m / 128, r = m % 128, ch = k / TC_KC, kl = k - ch * TC_KC;
       const size_t pbytes = (size_t)128 * p.kc[ch] * 2;
       const size_t off = (size_t)mt * p.a_tile_bytes + p.a_chunk_off[ch] +
                          ((size_t)(kl / 8) * 16 + r / 8) * 128 + (r % 8) * 16 + (kl % 8) * 2;
-      for (int pl = 0; pl < FX_PLANES; ++pl) {
-        // digits are integers with |d| <= 128: their bf16 pattern is the top
+      for (int pl = 0; pl < p.planes; ++pl) {
+        // digits are integers with |d| <= 256: their bf16 pattern is the top
         // half of the float's
         const float fd = (float)dg[pl];
         uint32_t w;
@@ -612,7 +642,7 @@ std::vector<float> a_row_digits(const FxPlan& p, const std::vector<double>& a, i
   std::vector<float> dig((size_t)FX_PLANES * p.kpad, 0.f);
   for (int k = 0; k < K; ++k) {
     double dg[FX_PLANES];
-    fx_digits_host(a[(size_t)row * K + k], row_exp, dg);
+    fx_digits_host(a[(size_t)row * K + k], row_exp, dg, FX_PLANES);
     for (int i = 0; i < FX_PLANES; ++i) dig[(size_t)i * p.kpad + k] = (float)dg[i];
   }
   return dig;
@@ -621,15 +651,21 @@ std::vector<float> a_row_digits(const FxPlan& p, const std::vector<double>& a, i
 template <typename OutT>
 int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int* aexp, const uint8_t* bimg,
                       const int* bexp, const Ptr8<OutT>& outs, int nfields, size_t ldc, int kid) {
-  // exactness of a level's FP32 sum: (2 * 128 * 64 + 2 * 64 * 64) * kpad < 2^24
-  if (p.kpad > 680) {
+  // exactness of a level's FP32 sum, the largest level's products per k times
+  // kpad below 2^24: 4 planes (2 * 128 * 64 + 2 * 64 * 64) * kpad, 3 planes
+  // (2 * 256 * 128 + 128 * 128) * kpad
+  if ((p.planes == 4 && p.kpad > 680) || (p.planes == 3 && p.kpad > 204) || (p.planes != 3 && p.planes != 4)) {
     h->err = "k_tc_gemm_fx: K is too long for exact sums";
     return CHF_E_INVALID;
   }
-  const size_t smem = ws_resident(p) ? ws_a_resident_bytes(p) + (size_t)WS_STAGES * WS_B_STAGE
-                                     : (size_t)WS_STAGES * WS_AB_STAGE;
-  if (!cuda_ok(h, cudaFuncSetAttribute(k_tc_gemm_fx<OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem),
+  if (p.planes == 3 && sizeof(OutT) != 4) {
+    h->err = "k_tc_gemm_fx: 3-plane digits are for FP32 outputs";
+    return CHF_E_INVALID;
+  }
+  auto kern = p.planes == 4 ? k_tc_gemm_fx<OutT, 4> : k_tc_gemm_fx<OutT, 3>;
+  const size_t smem = ws_resident(p) ? ws_a_resident_bytes(p) + (size_t)WS_STAGES * ws_b_stage(p.planes)
+                                     : (size_t)WS_STAGES * ws_ab_stage(p.planes);
+  if (!cuda_ok(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                "k_tc_gemm_fx smem"))
     return CHF_E_CUDA;
   // whole multiples of the row tiles, each CTA on one row tile
@@ -637,8 +673,7 @@ int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int
   const int grid = (int)(std::min<long>(items, (long)std::max(h->num_sms, p.mtiles)) / p.mtiles * p.mtiles);
   cudaEvent_t ev;
   prof_begin(h, kid, &ev);
-  k_tc_gemm_fx<OutT><<<grid, WS_THREADS, smem, h->stream>>>(p, aimg, aexp, bimg, bexp, outs, ldc, nfields,
-                                                            h->dev_status);
+  kern<<<grid, WS_THREADS, smem, h->stream>>>(p, aimg, aexp, bimg, bexp, outs, ldc, nfields, h->dev_status);
   prof_end(h, kid, ev);
   return cuda_ok(h, cudaGetLastError(), "k_tc_gemm_fx") ? CHF_OK : CHF_E_CUDA;
 }
@@ -646,6 +681,10 @@ int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int
 template <typename InT>
 int launch_tc_split_fx(Handle* h, const FxPlan& p, const Ptr8<const InT>& ins, int kvalid, uint8_t* bimg,
                        int* bexp, int nfields, int kid, const FxTail& tail) {
+  if (tail.adig && p.planes != 4) {
+    h->err = "k_tc_split_fx: row tails need 4-plane digits";
+    return CHF_E_INVALID;
+  }
   // warps per CTA: enough that each thread's groups fit in registers, at
   // most 32 (longer columns re-read their remaining groups)
   const int ng = p.kpad / 8, sg = SplitGroups<InT>::value;
@@ -653,7 +692,10 @@ int launch_tc_split_fx(Handle* h, const FxPlan& p, const Ptr8<const InT>& ins, i
   dim3 grid(2 * p.ntiles, 1, nfields);
   cudaEvent_t ev;
   prof_begin(h, kid, &ev);
-  k_tc_split_fx<InT><<<grid, 32 * nq, 0, h->stream>>>(p, ins, kvalid, bimg, bexp, tail);
+  if (p.planes == 4)
+    k_tc_split_fx<InT, 4><<<grid, 32 * nq, 0, h->stream>>>(p, ins, kvalid, bimg, bexp, tail);
+  else
+    k_tc_split_fx<InT, 3><<<grid, 32 * nq, 0, h->stream>>>(p, ins, kvalid, bimg, bexp, tail);
   prof_end(h, kid, ev);
   return cuda_ok(h, cudaGetLastError(), "k_tc_split_fx") ? CHF_OK : CHF_E_CUDA;
 }

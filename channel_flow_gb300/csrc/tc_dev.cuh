@@ -53,17 +53,21 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
 
 
-// FX_PLANES digits of x * 2^-e (|x| < 2^e), each the rint of the scaled
-// remainder, exact in float (FX_PLANES from chf_internal.h)
-__device__ __forceinline__ void fx_digits_f(float x, int e, float* dg) {
-  float y = scalbnf(x, 7 - e);
+// NP digits of x * 2^-e (|x| < 2^e), each the rint of the scaled remainder,
+// exact in float: NP = 4, radix 2^7 (d_0 in [-128, 128], then [-64, 64]);
+// NP = 3, radix 2^8 (d_0 in [-256, 256], then [-128, 128])
+template <int NP>
+__device__ __forceinline__ void fx_digits_np(float x, int e, float* dg) {
+  constexpr int RB = NP == 4 ? 7 : 8;
+  float y = scalbnf(x, RB - e);
 #pragma unroll
-  for (int i = 0; i < FX_PLANES; ++i) {
+  for (int i = 0; i < NP; ++i) {
     const float di = rintf(y);
     dg[i] = di;
-    y = (y - di) * 128.0f;
+    y = (y - di) * (float)(1 << RB);
   }
 }
+__device__ __forceinline__ void fx_digits_f(float x, int e, float* dg) { fx_digits_np<4>(x, e, dg); }
 
 // one element of an extra output row: the level sums lev[L] += sum_{i+j=L}
 // a_i b_j of the row's digits a (plane-major, kpad each, at k) and the
