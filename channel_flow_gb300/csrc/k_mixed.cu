@@ -58,9 +58,9 @@ constexpr int CURL_COLS = 16;
 // (their powers of two).  Pass 2 (the pair splits the 8-row groups) writes
 // the digits, 8 rows per 16-byte store, and the exact level sums of the GL
 // row N (the wall z = -1), which the GL GEMM leaves out (it covers 0..N-1).
-constexpr int CURL_PF = 6;  // own rows of H loaded ahead of the recurrence
+constexpr int CURL_PF = 4;  // own rows of H loaded ahead of the recurrence
 
-__global__ void __launch_bounds__(CURL_THREADS, 14) k_curl(const double* __restrict__ lc,
+__global__ void __launch_bounds__(CURL_THREADS, 16) k_curl(const double* __restrict__ lc,
                                                        const double* __restrict__ iapha,
                                                        const double* __restrict__ ibeta, Dims d,
                                                        const __grid_constant__ FxPlan plan, float* __restrict__ hs,
