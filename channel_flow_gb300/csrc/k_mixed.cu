@@ -205,9 +205,8 @@ int setup_mixed(Handle* h) {
   const Dims& d = h->d;
   const long cols = 2 * d.modes();
   const int N = d.N, NZ = d.NZ, MZ = d.MZ, MP = d.MP;
-  // z transforms with exact accumulation (fixed-point digits, k_tcgemm.cu);
-  // the GL evaluation of h_v, h_g is not differentiated afterwards and keeps
-  // the floating bf16x3 split
+  // z transforms with exact accumulation (fixed-point digits, k_tcgemm.cu):
+  // Z2 and GL on four planes of 7-bit digits, Z1 on three of 8 bits (below)
   // Z2 and GL cover rows 0..N-1 (one 128-row tile for nnz = 128): row N, the
   // last coefficient / the wall point z = -1, is formed beside the digits by
   // k_tc_split_fx and k_curl with the same exact level sums, instead of by a
