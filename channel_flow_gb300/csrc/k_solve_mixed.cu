@@ -127,13 +127,14 @@ __global__ void __launch_bounds__(128) k_incr_rowexp(const float2* __restrict__ 
 // and writes x = c + delta in FP64.  M c is compensated: the products of the
 // high parts p = mh ch are summed into S, which starts at the power of two
 //   sigma = 2^(e_r + e_c + 3) >= 8 sum_c |mh ch|      (sum_c |mh| < 2^e_r),
-// so that S and every S + p stay within (3/4, 5/4) sigma: s = S + p, then
+// so that S and every S + p stay within (7/8, 9/8) sigma: s = S + p, then
 // S - s is exact (Sterbenz) and fma(mh, ch, S - s) is the product's rounding
 // error plus the part of p that S could not hold, rounded once.  That term
 // and the cross products mh cl + ml ch go to a second FP32 accumulator C,
 // with X r in plain FP32 (r is O(dt) and X r has no cancellation), and
 // delta = (S - sigma) + C with S - sigma exact: M c to about
-// 2^-40 sum_c |M_rc| max|c|, X r to FP32 rounding.
+// 2^-38 sum_c |M_rc| max|c| (sigma is at most 2^5 of that; the dropped
+// parts are 2^-43 of sigma), X r to FP32 rounding.
 // ---------------------------------------------------------------------------
 struct __align__(16) CoefHL {
   float hr, hi, lr, li;  // high and low parts of the real and imaginary parts
