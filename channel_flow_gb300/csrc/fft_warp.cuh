@@ -1,19 +1,20 @@
-// fft_warp.cuh -- register-resident length-192 DFTs, one warp per line.
+// fft_warp.cuh -- register-resident length-192 DFTs in FP32, one warp per
+// line.
 //
-// 192 = 6 x 32.  Lane l holds six values; "natural" layout means register j
-// of lane l is element 32 j + l.  With n = 32 j + l and k = k1 + 6 k2,
+// 192 = 6 x 32.  Lane l holds six values; "natural" layout means value j of
+// lane l is element 32 j + l.  With n = 32 j + l and k = k1 + 6 k2,
 //   X[k1 + 6 k2] = sum_l W32^(l k2) W192^(l k1) sum_j W6^(j k1) x[32 j + l],
 // so a 6-point DFT per lane, a twiddle W192^(l k1) and a 32-point DFT across
-// lanes (radix-2 decimation in frequency over warp shuffles) give, in
-// register k1 of lane l, element k1 + 6 bitrev5(l): the "permuted" layout.
-// fft192_perm_to_natural runs the reverse factorisation (32-point decimation
-// in time across lanes from bit-reversed input, twiddle, 6-point DFT per
-// lane) and takes permuted input to natural output.  Physical-space values
-// are consumed pointwise (products) or row by row, so they stay permuted and
-// no reordering pass exists.
+// lanes (radix-2 decimation in frequency over warp shuffles) give, as value
+// k1 of lane l, element k1 + 6 bitrev5(l): the "permuted" layout.
+// fft192_perm_to_natural_x2 runs the reverse factorisation (32-point
+// decimation in time across lanes from bit-reversed input, twiddle, 6-point
+// DFT per lane) and takes permuted input to natural output.  Physical-space
+// values are consumed pointwise (products) or row by row, so they stay
+// permuted and no reordering pass exists.
 //
-// tw[m] = exp(-2 pi i m / 192), m = 0..191 (shared memory); SIGN = -1 is the
-// forward (FFTW_FORWARD) transform, +1 the backward one.
+// tw[m] = exp(-2 pi i m / 192), m = 0..191; SIGN = -1 is the forward
+// (FFTW_FORWARD) transform, +1 the backward one.
 #pragma once
 #include "f32x2.cuh"
 #include "fft_dev.cuh"
@@ -27,85 +28,19 @@ __device__ __forceinline__ cplx<T> twid(const cplx<T>* tw, int m) {
   return w;
 }
 
-// 6-point DFT in registers: X[k] = sum_j a[j] exp(SIGN 2 pi i j k / 6)
-template <typename T, int SIGN>
-__device__ __forceinline__ void dft6(cplx<T>* a) {
-  cplx<T> e[3] = {a[0], a[2], a[4]};
-  cplx<T> o[3] = {a[1], a[3], a[5]};
-  bfly3<T, SIGN>(e);
-  bfly3<T, SIGN>(o);
-  // omega6^k = exp(SIGN i pi k / 3), k = 0, 1, 2
-  const T c = (T)0.5, s = (T)0.86602540378443864676;
-  cplx<T> w1{c, (T)SIGN * s};
-  cplx<T> w2{-c, (T)SIGN * s};
-  cplx<T> t0 = o[0], t1 = cmul(o[1], w1), t2 = cmul(o[2], w2);
-  a[0] = cadd(e[0], t0);
-  a[3] = csub(e[0], t0);
-  a[1] = cadd(e[1], t1);
-  a[4] = csub(e[1], t1);
-  a[2] = cadd(e[2], t2);
-  a[5] = csub(e[2], t2);
-}
-
-template <typename T>
-__device__ __forceinline__ cplx<T> shfl_x(cplx<T> v, int mask) {
-  return cplx<T>{__shfl_xor_sync(0xffffffffu, v.re, mask), __shfl_xor_sync(0xffffffffu, v.im, mask)};
-}
-
 template <typename T>
 __device__ __forceinline__ cplx<T> shfl_i(cplx<T> v, int src) {
   return cplx<T>{__shfl_sync(0xffffffffu, v.re, src), __shfl_sync(0xffffffffu, v.im, src)};
 }
 
-// natural -> permuted
-template <typename T, int SIGN>
-__device__ __forceinline__ void fft192_natural_to_perm(cplx<T>* v, const cplx<T>* tw) {
-  const int lane = threadIdx.x & 31;
-  dft6<T, SIGN>(v);
-#pragma unroll
-  for (int k1 = 1; k1 < 6; ++k1) v[k1] = cmul(v[k1], twid<T, SIGN>(tw, lane * k1));
-#pragma unroll
-  for (int h = 16; h >= 1; h >>= 1) {
-    const bool upper = (lane & h) != 0;
-    const cplx<T> w = twid<T, SIGN>(tw, (lane & (h - 1)) * (96 / h));  // W_{2h}^t = W192^(t * 96/h)
-#pragma unroll
-    for (int k1 = 0; k1 < 6; ++k1) {
-      cplx<T> p = shfl_x(v[k1], h);
-      v[k1] = upper ? cmul(csub(p, v[k1]), w) : cadd(v[k1], p);
-    }
-  }
-}
-
-// permuted -> natural
-template <typename T, int SIGN>
-__device__ __forceinline__ void fft192_perm_to_natural(cplx<T>* v, const cplx<T>* tw) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int h = 1; h <= 16; h <<= 1) {
-    const bool upper = (lane & h) != 0;
-    const cplx<T> w = twid<T, SIGN>(tw, (lane & (h - 1)) * (96 / h));
-#pragma unroll
-    for (int k1 = 0; k1 < 6; ++k1) {
-      cplx<T> x = upper ? cmul(v[k1], w) : v[k1];
-      cplx<T> p = shfl_x(x, h);
-      v[k1] = upper ? csub(p, x) : cadd(x, p);
-    }
-  }
-#pragma unroll
-  for (int k1 = 1; k1 < 6; ++k1) v[k1] = cmul(v[k1], twid<T, SIGN>(tw, lane * k1));
-  // 6-point DFT over k1 -> register j' holds element 32 j' + lane
-  dft6<T, SIGN>(v);
-}
-
 // ---------------------------------------------------------------------------
-// FP32 packed form.  The same factorisation and layouts, with a lane's six
-// values held as three (element 2j, element 2j + 1) pairs of real parts and
-// three of imaginary parts, so that each f32x2 instruction does one
-// operation for two elements.  A cross-lane radix-2 stage becomes, per pair,
-// four shuffles, y = p + S v (S = +1 on the lower lane of a butterfly, -1 on
-// the upper one) and y W' (W' = the stage twiddle on the upper lane, 1 on
-// the lower one): the lower lane's v + p and the upper lane's (p - v) W of
-// the scalar form.  The per-lane constants come from a shared-memory table
+// Packed form: a lane's six values are held as three (element 2j, element
+// 2j + 1) pairs of real parts and three of imaginary parts, so that each
+// f32x2 instruction does one operation for two elements.  A cross-lane
+// radix-2 stage is, per pair, four shuffles, y = p + S v (S = +1 on the lower
+// lane of a butterfly, -1 on the upper one) and y W' (W' = the stage twiddle
+// on the upper lane, 1 on the lower one): the lower lane's v + p and the
+// upper lane's (p - v) W.  The per-lane constants come from a shared-memory table
 // built once per CTA (fft192_table).
 // ---------------------------------------------------------------------------
 struct Line6 {
@@ -163,8 +98,9 @@ __device__ __forceinline__ f32x2 shfl_x2(f32x2 v, int mask) {
   return pk(__shfl_xor_sync(0xffffffffu, a, mask), __shfl_xor_sync(0xffffffffu, b, mask));
 }
 
-// 6-point DFT of a lane's values (the scalar dft6): the pairs (x[2j],
-// x[2j+1]) are (e_j, o_j), so one packed 3-point DFT over j does both halves.
+// 6-point DFT of a lane's values, X[k] = sum_j x[j] exp(SIGN 2 pi i j k / 6):
+// the pairs (x[2j], x[2j+1]) are (e_j, o_j), so one packed 3-point DFT over j
+// does both halves.
 // Z1: elements 2 and 3 are zero (zero-padded inverse transforms).
 template <int SIGN, bool Z1 = false>
 __device__ __forceinline__ void dft6_x2(Line6& a) {
@@ -201,7 +137,7 @@ __device__ __forceinline__ void dft6_x2(Line6& a) {
   a.i[2] = pk(E1i - t1i, E2i - t2i);
 }
 
-// natural -> permuted (fft192_natural_to_perm), table of the same SIGN;
+// natural -> permuted, table of the same SIGN;
 // Z1 as for dft6_x2
 template <int SIGN, bool Z1 = false>
 __device__ __forceinline__ void fft192_natural_to_perm_x2(Line6& a, const Fft192Table& t) {
@@ -225,7 +161,7 @@ __device__ __forceinline__ void fft192_natural_to_perm_x2(Line6& a, const Fft192
   }
 }
 
-// permuted -> natural (fft192_perm_to_natural), table of the same SIGN
+// permuted -> natural, table of the same SIGN
 template <int SIGN>
 __device__ __forceinline__ void fft192_perm_to_natural_x2(Line6& a, const Fft192Table& t) {
   const int lane = threadIdx.x & 31;
@@ -254,24 +190,6 @@ __device__ __forceinline__ cplx<float> line_get(const Line6& a, int k) {
   upk(a.r[k >> 1], r0, r1);
   upk(a.i[k >> 1], i0, i1);
   return (k & 1) ? cplx<float>{r1, i1} : cplx<float>{r0, i0};
-}
-
-// a line from six complex values / back
-__device__ __forceinline__ Line6 line_pack(const cplx<float>* v) {
-  Line6 a;
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    a.r[j] = pk(v[2 * j].re, v[2 * j + 1].re);
-    a.i[j] = pk(v[2 * j].im, v[2 * j + 1].im);
-  }
-  return a;
-}
-__device__ __forceinline__ void line_unpack(const Line6& a, cplx<float>* v) {
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    upk(a.r[j], v[2 * j].re, v[2 * j + 1].re);
-    upk(a.i[j], v[2 * j].im, v[2 * j + 1].im);
-  }
 }
 
 }  // namespace chf
