@@ -41,14 +41,11 @@
 // per core matrix; core (g = row/8, c = k/8) at (c * G + g) * 128 bytes with
 // G = 16 for A and 8 for B).  K is cut into chunks of TC_KC; every (tile,
 // chunk, plane) image is one contiguous block moved by one cp.async.bulk,
-// completion signalled on an mbarrier.  One thread issues the MMAs and
-// tcgen05.commit arrives on a second mbarrier; four warps read the
-// accumulators back with tcgen05.ld.  Every wait is bounded (1 s of wall
-// time); on timeout the kernel records an error code, stops issuing work,
-// waits (bounded) for the MMAs it issued and frees its tensor memory.  The
-// four accumulators take 4 x 64 TMEM columns and the operands 96 KB of
-// shared memory, so two CTAs share an SM and one's copies overlap the
-// other's MMAs and epilogue.
+// completion signalled on an mbarrier.  The GEMM kernel below is persistent
+// and warp-specialised (its section says how); every wait in it is bounded
+// (1 s of wall time), and on timeout it records an error code, stops issuing
+// work, waits (bounded) for the copies and MMAs in flight and frees its
+// tensor memory.
 #include <cuda_bf16.h>
 
 #include <algorithm>
