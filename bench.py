@@ -37,7 +37,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    p.add_argument("--precision", choices=["fp64", "mixed", "mixed_fp64solve"], default="mixed")
     p.add_argument("--config", default="c3_retau180_128")
     p.add_argument("--zpad", default="auto",
                    help="product-grid intervals in z: 0 = 2*nnz (reference), 'auto' = smallest "
@@ -73,10 +73,24 @@ def dist_env():
     return rank, world, local
 
 
-def workload_name(cfg, precision, zpad):
-    return (f"Re_tau180 channel {cfg.nnx}x{cfg.nnz + 1}x{cfg.nny} (nnx x wall-normal x nny), "
+# the arithmetic of each precision of the library
+DTYPES = {
+    "fp64": "f64",
+    "mixed": "f64 state; f32 x/y FFTs and products; exact fixed-point tcgen05 z transforms (bf16 digits, exact "
+             "f32 level sums); f64 curl and recurrences; solve as f64 update c + delta with delta from "
+             "compensated f32 (about 2^-38), A^-1 r in f32; (0,0) mode f64",
+    "mixed_fp64solve": "f64 state; f32 x/y FFTs and products; exact fixed-point tcgen05 z transforms (bf16 "
+                       "digits, exact f32 level sums); f64 curl; f64 tau solve for every mode",
+}
+
+
+def workload_name(cfg):
+    """The physical workload alone (grid, box, time step, Reynolds number):
+    both arms print the same string; the arithmetic (precision) and the
+    wall-normal product grid are separate config keys."""
+    return (f"channel {cfg.nnx}x{cfg.nnz + 1}x{cfg.nny} (nnx x wall-normal x nny), "
             f"box {2 * cfg.aphi:g}pi x 2 x {2 * cfg.beta:.4g}pi, dt={cfg.dt:g}, re={cfg.re:g}, "
-            f"re_p={cfg.re_p:g}, {precision} path, product grid {zpad or 2 * cfg.nnz} intervals")
+            f"re_p={cfg.re_p:g}, seeded laminar + 10% divergence-free perturbation")
 
 
 # --------------------------------------------------------------------------
@@ -115,7 +129,7 @@ def kernel_work(cfg, zpad=0, precision="fp64"):
     nsolve = int((k2 != 0.0).sum())
     w["k_solve"] = ((nk2 + 1) * stride * 8 + 12 * NZ * modes * c,
                     nsolve * (8 * (ne * ne + no * no) + 2 * fft_flops(2 * N)))
-    if precision != "mixed":
+    if precision == "fp64":
         return w
     # mixed path: FP32 x/y work halves the bytes; the z transforms are exact
     # GEMMs on bf16 digit planes (B images in, FP32/FP64 out: 3 planes for Z1,
@@ -241,7 +255,8 @@ def run_reference(args):
         "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 / rate,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded laminar profile + 10% divergence-free perturbation)",
-        "config": {"workload": workload_name(cfg, "fp64", 0), "grid_points": cfg.points},
+        "config": {"workload": workload_name(cfg), "grid_points": cfg.points, "precision": "fp64",
+                   "zpad": 2 * cfg.nnz, "parallelism": "host threads (rank 0 only)"},
         "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -349,26 +364,34 @@ def main():
     # mixed form, the velocity error after --accuracy-steps steps of both paths
     accuracy = None
     fp64_rate = None
-    if args.precision == "mixed":
-        ref = Channel(cfg, precision="fp64", zpad=args.zpad, device=local)
-        rs = torch.cuda.Stream(device=local)
-        ref.set_stream(rs.cuda_stream)
-        ref.upload_state(st)
-        ref.getnonlinear()
-        ref.solve()
-        ref.step(max(3, args.warmup))
-        ref.synchronize()
-        k64 = max(2, min(args.steps, 30))
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
-        f0.record(rs)
-        ref.step(k64)
-        f1.record(rs)
-        torch.cuda.synchronize()
-        fp64_rate = k64 / (f0.elapsed_time(f1) / 1e3)
-        ref.close()
+    other_rates = {}
+    if args.precision != "fp64":
+        def device_rate(prec, k):
+            ref = Channel(cfg, precision=prec, zpad=args.zpad, device=local)
+            rs = torch.cuda.Stream(device=local)
+            ref.set_stream(rs.cuda_stream)
+            ref.upload_state(st)
+            ref.getnonlinear()
+            ref.solve()
+            ref.step(max(3, args.warmup))
+            ref.synchronize()
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(rs)
+            ref.step(k)
+            f1.record(rs)
+            torch.cuda.synchronize()
+            ref.close()
+            return k / (f0.elapsed_time(f1) / 1e3)
+
+        fp64_rate = device_rate("fp64", max(2, min(args.steps, 30)))
+        # the other mixed form beside the headline one
+        for prec in ("mixed", "mixed_fp64solve"):
+            if prec != args.precision:
+                other_rates[prec] = device_rate(prec, max(2, min(args.steps, 100)))
         if args.accuracy_steps > 0:
-            accuracy = accuracy_vs_fp64(Channel, cfg, st, args.zpad, local, args.accuracy_steps)
+            accuracy = accuracy_vs_fp64(Channel, cfg, st, args.zpad, local, args.accuracy_steps,
+                                        forms=("mixed", "mixed_fp64solve"))
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -386,7 +409,7 @@ def main():
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     achieved_gbs = nbytes / (avg_ms / 1e3) / 1e9
-    traffic = read_traffic(kname + ("_f32" if args.precision == "mixed" and kname in ("k_yinv", "k_xprod", "k_yfwd") else ""))
+    traffic = read_traffic(kname + ("_f32" if args.precision != "fp64" and kname in ("k_yinv", "k_xprod", "k_yfwd") else ""))
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved_gbs, "peak": hbm_peak,
                 "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback",
@@ -409,12 +432,10 @@ def main():
         "metric": "steps/s", "value": value, "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else ("f64 state; f32 x/y FFTs and products; exact fixed-point "
-                                                         "tcgen05 z transforms (bf16 digits, exact f32 level sums); "
-                                                         "f64 curl and recurrences; compensated f32 increment solve"),
+        "dtype": DTYPES[args.precision],
         "data": "synthetic (seeded laminar profile + 10% divergence-free perturbation)",
-        "config": {"workload": workload_name(cfg, args.precision, args.zpad),
-                   "grid_points": cfg.points, "precision": args.precision,
+        "config": {"workload": workload_name(cfg),
+                   "grid_points": cfg.points, "precision": args.precision, "zpad": args.zpad,
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2: >0.9 GB touched per step vs 129 MB L2"},
         "grid_point_steps_per_s": value * cfg.points,
@@ -434,6 +455,9 @@ def main():
     if fp64_rate is not None:
         line["fp64_steps_per_s"] = fp64_rate
         line["mixed_over_fp64"] = value / world / fp64_rate
+        for prec, r in other_rates.items():
+            line[prec] = {"steps_per_s": r, "over_fp64": r / fp64_rate, "dtype": DTYPES[prec],
+                          "timing": "device events, the same start, chf_step graph replays"}
     if world == 1 and not args.no_cpu_baseline:
         rate, threads, steps, el = cpu_reference_rate(cfg, args.cpu_seconds)
         line["cpu_baseline"] = {
@@ -528,13 +552,14 @@ def ensemble_rate(n, device, precision, steps=20, warmup=4):
             "timing": "host wall clock around chf_batch_step + synchronize"}
 
 
-def accuracy_vs_fp64(Channel, cfg, st, zpad, device, nsteps):
-    """Both paths from the same start for nsteps steps (after the start-up
-    getnonlinear + solve): rel-L2 of each field of the mixed state against
-    the FP64 state, and of the velocity vector (u, v, w) as a whole."""
+def accuracy_vs_fp64(Channel, cfg, st, zpad, device, nsteps, forms=("mixed",)):
+    """The FP64 path and each mixed form from the same start for nsteps steps
+    (after the start-up getnonlinear + solve): per form, rel-L2 of each field
+    against the FP64 state, of the velocity vector (u, v, w) as a whole, of
+    the pressure, and the relative differences of wall shear and energy."""
     import numpy as np
     out, extra = {}, {}
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64",) + tuple(forms):
         ch = Channel(cfg, precision=prec, zpad=zpad, device=device)
         ch.upload_state(st)
         ch.getnonlinear()
@@ -544,28 +569,32 @@ def accuracy_vs_fp64(Channel, cfg, st, zpad, device, nsteps):
         out[prec] = ch.download_state()
         extra[prec] = (ch.pressure(), ch.statistics())
         ch.close()
-    a, b = out["fp64"], out["mixed"]
+    a = out["fp64"]
     nyq = cfg.nny // 2
-    errs, num, den = {}, 0.0, 0.0
-    for k in ("unp1", "vnp1", "wnp1", "omegaynp1"):
-        pa = np.delete(a[k], nyq, axis=1)
-        pb = np.delete(b[k], nyq, axis=1)
-        d2, r2 = float(np.sum((pb - pa) ** 2)), float(np.sum(pa ** 2))
-        errs[k] = (d2 / r2) ** 0.5
-        if k != "omegaynp1":
-            num, den = num + d2, den + r2
-    vel = (num / den) ** 0.5
-    pa = np.delete(extra["fp64"][0], nyq, axis=1)
-    pb = np.delete(extra["mixed"][0], nyq, axis=1)
-    errs["pressure"] = float(np.linalg.norm(pb - pa) / np.linalg.norm(pa))
-    sa, sb = extra["fp64"][1], extra["mixed"][1]
-    rel = lambda k: abs(sb[k] - sa[k]) / abs(sa[k])
-    errs["wall_shear_top"] = rel("u_tau_top") * 2.0     # tau_w = u_tau^2
-    errs["wall_shear_bottom"] = rel("u_tau_bottom") * 2.0
-    errs["energy"] = rel("energy")
-    return {"steps": nsteps, "rel_l2_vs_fp64": errs, "velocity_rel_l2": vel,
-            "velocity_component_max_rel_l2": max(errs[k] for k in ("unp1", "vnp1", "wnp1")),
-            "target": 1e-5, "met": vel <= 1e-5,
+    res = {}
+    for prec in forms:
+        b = out[prec]
+        errs, num, den = {}, 0.0, 0.0
+        for k in ("unp1", "vnp1", "wnp1", "omegaynp1"):
+            pa = np.delete(a[k], nyq, axis=1)
+            pb = np.delete(b[k], nyq, axis=1)
+            d2, r2 = float(np.sum((pb - pa) ** 2)), float(np.sum(pa ** 2))
+            errs[k] = (d2 / r2) ** 0.5
+            if k != "omegaynp1":
+                num, den = num + d2, den + r2
+        vel = (num / den) ** 0.5
+        pa = np.delete(extra["fp64"][0], nyq, axis=1)
+        pb = np.delete(extra[prec][0], nyq, axis=1)
+        errs["pressure"] = float(np.linalg.norm(pb - pa) / np.linalg.norm(pa))
+        sa, sb = extra["fp64"][1], extra[prec][1]
+        rel = lambda k: abs(sb[k] - sa[k]) / abs(sa[k])
+        errs["wall_shear_top"] = rel("u_tau_top") * 2.0     # tau_w = u_tau^2
+        errs["wall_shear_bottom"] = rel("u_tau_bottom") * 2.0
+        errs["energy"] = rel("energy")
+        res[prec] = {"rel_l2_vs_fp64": errs, "velocity_rel_l2": vel,
+                     "velocity_component_max_rel_l2": max(errs[k] for k in ("unp1", "vnp1", "wnp1")),
+                     "met": vel <= 1e-5}
+    return {"steps": nsteps, "target": 1e-5, "forms": res,
             "note": "spectral coefficients without the spanwise Nyquist slot; velocity = (u, v, w) as one "
                     "vector; pressure = total head (chf_pressure); wall shear and energy from chf_statistics "
                     "(relative differences)"}

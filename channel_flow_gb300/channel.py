@@ -14,7 +14,7 @@ from .fields import FIELD_NAMES, MEAN_NAMES
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libchflow.so")
 
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "mixed_fp64solve": 2}
 STATUS = {0: "CHF_OK", -1: "CHF_E_INVALID", -2: "CHF_E_CUDA", -3: "CHF_E_NOMEM",
           -4: "CHF_E_STATE", -5: "CHF_E_NUMERIC"}
 

@@ -109,7 +109,8 @@ static std::string validate(const chf_config* c) {
   if (!(c->aphi > 0) || !(c->beta > 0)) return "aphi and beta must be positive";
   if (!(c->dt > 0) || !(c->re > 0)) return "dt and re must be positive";
   if (!std::isfinite(c->re_p)) return "re_p must be finite";
-  if (c->precision != CHF_FP64 && c->precision != CHF_MIXED) return "precision must be CHF_FP64 or CHF_MIXED";
+  if (c->precision != CHF_FP64 && c->precision != CHF_MIXED && c->precision != CHF_MIXED_F64SOLVE)
+    return "precision must be CHF_FP64, CHF_MIXED or CHF_MIXED_F64SOLVE";
   int mz = c->zpad == 0 ? 2 * c->nnz : c->zpad;
   if (2 * mz <= 3 * c->nnz) return "zpad must satisfy 2*zpad > 3*nnz (exact dealiasing)";
   if (!factors_235(3 * c->nnx / 2) || !factors_235(3 * c->nny / 2) || !factors_235(2 * mz) ||
@@ -147,11 +148,19 @@ static void release(chf_handle* h) {
 }
 
 namespace chf {
+bool mixed_front(const Handle* h) { return h->cfg.precision != CHF_FP64; }
+bool increment_solve(const Handle* h) { return h->cfg.precision == CHF_MIXED; }
+
+int launch_nonlinear(Handle* h, const cudaEvent_t* field_ready) {
+  return mixed_front(h) ? launch_nonlinear_mixed(h, field_ready) : launch_nonlinear_fp64(h);
+}
+
+int launch_solve(Handle* h) { return increment_solve(h) ? launch_solve_mixed(h) : launch_solve_fp64(h); }
+
 int step_once(Handle* h) {
-  const bool mixed = h->cfg.precision == CHF_MIXED;
-  int rc = mixed ? launch_nonlinear_mixed(h) : launch_nonlinear_fp64(h);
+  int rc = launch_nonlinear(h, nullptr);
   if (rc != CHF_OK) return rc;
-  return mixed ? launch_solve_mixed(h) : launch_solve_fp64(h);
+  return launch_solve(h);
 }
 }  // namespace chf
 
@@ -292,9 +301,9 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
   }
   int rc = setup_solver(h);
   if (rc != CHF_OK) return fail(rc);
-  if (cfg->precision == CHF_MIXED) {
+  if (mixed_front(h)) {
     rc = setup_mixed(h);
-    if (rc == CHF_OK) rc = setup_solver_mixed(h);
+    if (rc == CHF_OK && increment_solve(h)) rc = setup_solver_mixed(h);
     if (rc != CHF_OK) return fail(rc);
     if (!cuda_ok(h, cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming), "cudaEventCreate") ||
@@ -308,7 +317,10 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
     if (!cuda_ok(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate")) return fail(CHF_E_CUDA);
   for (cudaEvent_t& e : h->ev_field)
     if (!cuda_ok(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate")) return fail(CHF_E_CUDA);
-  h->kernels_per_step = cfg->precision == CHF_MIXED ? 13 : 6;
+  // FP64: k_zc2v, k_yinv, k_xprod, k_yfwd, k_zcurl, k_solve; mixed front:
+  // two splits, three GEMMs, k_yinv_w, k_xprod_w, k_yfwd_w, k_curl,
+  // k_meanfix; then k_solve, or k_inc_solve + k_inc_recover + the (0,0) mode
+  h->kernels_per_step = !mixed_front(h) ? 6 : increment_solve(h) ? 13 : 11;
   if (!cuda_ok(h, cudaStreamSynchronize(h->stream), "create sync")) return fail(CHF_E_CUDA);
   *out = h;
   return CHF_OK;
@@ -377,7 +389,7 @@ int chf_getnonlinear(chf_handle* h) {
     return CHF_E_STATE;
   }
   if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
-  return h->cfg.precision == CHF_MIXED ? launch_nonlinear_mixed(h) : launch_nonlinear_fp64(h);
+  return launch_nonlinear(h, nullptr);
 }
 
 int chf_solve(chf_handle* h) {
@@ -387,7 +399,7 @@ int chf_solve(chf_handle* h) {
     return CHF_E_STATE;
   }
   if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
-  return h->cfg.precision == CHF_MIXED ? launch_solve_mixed(h) : launch_solve_fp64(h);
+  return launch_solve(h);
 }
 
 int chf_step(chf_handle* h, int nsteps) {
@@ -460,7 +472,9 @@ int chf_step_host(chf_handle* h, int nsteps, double* vnp1, double* omegaynp1, do
     return CHF_E_INVALID;
   }
   if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
-  const bool mixed = h->cfg.precision == CHF_MIXED;
+  // mixed: the nonlinear front follows the fields as they land; inc: the
+  // increment solve finishes v and omega_y before the recovery
+  const bool mixed = mixed_front(h), inc = increment_solve(h);
   const size_t fb = sizeof(cd) * h->d.field_elems(), mb = sizeof(double) * 2 * h->d.NZ;
   cudaStream_t S = h->stream, ci = h->copy_in, co = h->copy_out;
   auto up = [&](void* dst, const void* src, size_t n) {
@@ -489,7 +503,7 @@ int chf_step_host(chf_handle* h, int nsteps, double* vnp1, double* omegaynp1, do
   }
   for (int s = 0; s < nsteps; ++s) {
     const bool last = s == nsteps - 1;
-    int rc = mixed ? launch_nonlinear_mixed(h, s == 0 ? h->ev_field : nullptr) : launch_nonlinear_fp64(h);
+    int rc = launch_nonlinear(h, (mixed && s == 0) ? h->ev_field : nullptr);
     if (rc != CHF_OK) return rc;
     if (s == 0 && !ev_wait(h, S, h->ev_hist_in)) return CHF_E_CUDA;
     if (last) {  // the new histories are final; the host buffers were read by the upload
@@ -497,18 +511,18 @@ int chf_step_host(chf_handle* h, int nsteps, double* vnp1, double* omegaynp1, do
           !down(fh[F_RV], h->f[F_RV], fb) || !down(fh[F_RG], h->f[F_RG], fb))
         return CHF_E_CUDA;
     }
-    h->after_inc = (last && mixed) ? h->ev_vg : nullptr;
-    rc = mixed ? launch_solve_mixed(h) : launch_solve_fp64(h);
+    h->after_inc = (last && inc) ? h->ev_vg : nullptr;
+    rc = launch_solve(h);
     h->after_inc = nullptr;
     if (rc != CHF_OK) return rc;
-    if (last && mixed &&
+    if (last && inc &&
         (!ev_wait(h, co, h->ev_vg) || !down(fh[F_V], h->f[F_V], fb) || !down(fh[F_OY], h->f[F_OY], fb)))
       return CHF_E_CUDA;
   }
   if (!ev_rec(h, h->ev_done, S) || !ev_wait(h, co, h->ev_done)) return CHF_E_CUDA;
   for (int i : {F_U, F_W, F_OX, F_OZ})
     if (!down(fh[i], h->f[i], fb)) return CHF_E_CUDA;
-  if (!mixed)
+  if (!inc)
     for (int i : {F_V, F_OY})
       if (!down(fh[i], h->f[i], fb)) return CHF_E_CUDA;
   for (int i = 0; i < M_COUNT; ++i)

@@ -235,6 +235,14 @@ int setup_mixed(Handle* h);
 // u, v, w, omega_x, omega_y, omega_z; when given, each field's share of the
 // first stages waits for its own event only (chf_step_host's upload)
 int launch_nonlinear_mixed(Handle* h, const cudaEvent_t* field_ready = nullptr);
+// precision of the handle's stages (chf_api.cu): the mixed nonlinear front
+// (CHF_MIXED, CHF_MIXED_F64SOLVE) and the increment solve (CHF_MIXED only;
+// CHF_FP64 and CHF_MIXED_F64SOLVE run the FP64 k_solve)
+bool mixed_front(const Handle* h);
+bool increment_solve(const Handle* h);
+// getnonlinear / the solve of the handle's precision, on h->stream
+int launch_nonlinear(Handle* h, const cudaEvent_t* field_ready);
+int launch_solve(Handle* h);
 // one time step (getnonlinear + solve) on h->stream (chf_api.cu)
 int step_once(Handle* h);
 // launchers (k_solve.cu)

@@ -11,7 +11,10 @@
 // kernel reads -- lives in a file-scope __device__ array of fixed size.
 //
 // Limits and sharing: at most CHF_STATIC_MAX_PLANES wall-normal planes
-// (nnz + 1 <= 1025); larger grids are rejected with CHF_E_INVALID.  Every
+// (nnz + 1 <= 1025); larger grids, and grids that chf_create would reject
+// (nnx or nny not a multiple of 4, nnz odd or below 4), are rejected with
+// CHF_E_INVALID before any CUDA call.  The call waits for its stream and
+// returns its results in host memory.  Every
 // device that loads the library holds the array (about 33 KB) until the
 // process exits.  All calls share it: every slot is written before it is
 // read within one call, so nothing has to be cleared between calls, and the
@@ -111,8 +114,10 @@ extern "C" int chf_diagnostics_static(int nnx, int nny, int nnz, const double* d
                                       const double* d_omegaxnp1, const double* d_omegaynp1,
                                       const double* d_omegaznp1, double* energy_profile,
                                       chf_diag* out, void* stream) {
-  if (nnx <= 0 || nny <= 0 || nnz <= 0 || !d_unp1 || !d_vnp1 || !d_wnp1 || !d_omegaxnp1 ||
-      !d_omegaynp1 || !d_omegaznp1 || !out)
+  // the grid rules of chf_create: (re, im) pairs along x and a spanwise
+  // Nyquist slot at nny / 2 need nnx and nny to be multiples of 4
+  if (nnx < 4 || nnx % 4 || nny < 4 || nny % 4 || nnz < 4 || nnz % 2 || !d_unp1 || !d_vnp1 || !d_wnp1 ||
+      !d_omegaxnp1 || !d_omegaynp1 || !d_omegaznp1 || !out)
     return CHF_E_INVALID;
   if (nnz + 1 > MAX_PLANES) return CHF_E_INVALID;  // the fixed scratch holds 1025 planes
   int dev = 0;

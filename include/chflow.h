@@ -42,7 +42,14 @@ extern "C" {
 #define CHF_E_NUMERIC (-5)   /* non-finite values detected */
 
 #define CHF_FP64 0           /* all arithmetic in FP64 */
-#define CHF_MIXED 1          /* FP32 transforms/products, FP64 solves */
+#define CHF_MIXED 1          /* FP32 x/y transforms and products, exact tensor-core
+                                z transforms, FP64 state; the per-mode solve as an
+                                FP64 update c + delta whose increment delta is
+                                formed by compensated FP32 arithmetic (about
+                                2^-38 of its terms), A^-1 r in FP32; the (0,0)
+                                mode and the operator factorisations in FP64 */
+#define CHF_MIXED_F64SOLVE 2 /* the nonlinear term of CHF_MIXED with the FP64
+                                tau solve of CHF_FP64 for every mode */
 
 /* Runtime counterpart of the compile-time parameters of paraandcons.f90:4-25. */
 typedef struct chf_config {
@@ -54,7 +61,7 @@ typedef struct chf_config {
   double dt;      /* time step, paraandcons.f90:23 */
   double re;      /* Reynolds number (viscosity 1/re), paraandcons.f90:24 */
   double re_p;    /* mean pressure gradient, paraandcons.f90:25 */
-  int precision;  /* CHF_FP64 or CHF_MIXED */
+  int precision;  /* CHF_FP64, CHF_MIXED or CHF_MIXED_F64SOLVE */
   int zpad;       /* wall-normal intervals of the product grid; 0 = 2*nnz as
                      in getlamb (poiseuilleflow.f90:1647-1648); any value with
                      2*zpad > 3*nnz gives the same (exact) products */
@@ -256,11 +263,14 @@ int chf_batch_synchronize(chf_batch* b);
  * field layout above, plus the energy of every wall-normal plane k in
  * energy_profile[k] (k = 0..nnz, may be NULL), with no handle and no
  * allocation: its scratch is a fixed __device__ array inside the library.
- * nnz + 1 must not exceed CHF_STATIC_MAX_PLANES (else CHF_E_INVALID).  The
- * first call on a device looks up the array's address with that device
- * current (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  All calls share the array, so calls that overlap on the GPU race
- * and must be serialised by the caller.  stream: a cudaStream_t or NULL. */
+ * nnz + 1 must not exceed CHF_STATIC_MAX_PLANES, and the grid must satisfy
+ * chf_create's rules (nnx, nny multiples of 4; nnz even, >= 4), else
+ * CHF_E_INVALID before any CUDA call.  The call waits for its stream and
+ * returns its results in host memory.  The first call on a device looks up
+ * the array's address with that device current (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU race and must be serialised by the
+ * caller.  stream: a cudaStream_t or NULL. */
 #define CHF_STATIC_MAX_PLANES 1025
 int chf_diagnostics_static(int nnx, int nny, int nnz,
                            const double* d_unp1, const double* d_vnp1, const double* d_wnp1,

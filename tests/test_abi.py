@@ -72,13 +72,16 @@ def test_python_layer_raises_channel_error(chflow_lib):
         Channel(config.small(nnx=16, nny=8, nnz=16))
 
 
-def test_static_diagnostics_rejects_oversized_grid(chflow_lib):
+@pytest.mark.parametrize("nnx,nny,nnz", [(16, 8, 1025), (18, 8, 16), (16, 10, 16), (15, 8, 16),
+                                          (16, 8, 15), (16, 8, 2), (0, 8, 16)])
+def test_static_diagnostics_rejects_bad_grids(chflow_lib, nnx, nny, nnz):
     """The allocation-free entry point checks the plane count against its
-    fixed scratch before touching the GPU."""
+    fixed scratch, and the grid against chf_create's rules (its layout needs
+    nnx, nny multiples of 4), before touching the GPU."""
     from channel_flow_gb300.channel import CDiag
     d = CDiag()
-    one = ctypes.c_void_p(16)  # never dereferenced: the size check comes first
-    rc = chflow_lib.chf_diagnostics_static(16, 8, 1025, one, one, one, one, one, one, None,
+    one = ctypes.c_void_p(16)  # never dereferenced: the size checks come first
+    rc = chflow_lib.chf_diagnostics_static(nnx, nny, nnz, one, one, one, one, one, one, None,
                                            ctypes.byref(d), None)
     assert rc == -1
 

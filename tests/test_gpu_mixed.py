@@ -59,15 +59,36 @@ def test_mixed_nonlinear_term(chflow_lib, name):
         assert e < 1e-4, (k, e)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fp64solve"])
 @pytest.mark.parametrize("name,nsteps", [("small16", 50), ("c1_32", 50), ("c2_os", 50), ("mixed_radix", 30),
                                           ("warp192", 30), ("long_xz", 10), ("long_y", 20)])
-def test_mixed_steps_vs_fp64(chflow_lib, name, nsteps):
+def test_mixed_steps_vs_fp64(chflow_lib, name, nsteps, precision):
     cfg = CASES[name]
     st = fields.turbulent_start_state(cfg, seed=4)
     a = run(cfg, st, "fp64", nsteps)
-    b = run(cfg, st, "mixed", nsteps)
+    b = run(cfg, st, precision, nsteps)
     errs = vel_err(b, a)
     assert max(errs.values()) < 1e-5, errs
+
+
+def test_fp64solve_form_runs_the_fp64_solve(chflow_lib):
+    """CHF_MIXED_F64SOLVE shares the nonlinear term of CHF_MIXED and the
+    solve of CHF_FP64: one solve from the same post-nonlinear state is
+    bit-identical to the FP64 path's."""
+    cfg = CASES["mixed_radix"]
+    st = fields.turbulent_start_state(cfg, seed=8)
+    with Channel(cfg, precision="mixed_fp64solve") as g:
+        g.upload_state(st)
+        g.getnonlinear()
+        mid = g.download_state()
+        g.solve()
+        got = g.download_state()
+    with Channel(cfg, precision="fp64") as f:
+        f.upload_state(mid)
+        f.solve()
+        want = f.download_state()
+    for k in ("vnp1", "omegaynp1", "unp1", "wnp1", "omegaxnp1", "omegaznp1", "au0", "w0"):
+        assert np.array_equal(got[k], want[k]), k
 
 
 def test_mixed_steps_vs_oracle(chflow_lib, oracle_mod):
@@ -112,14 +133,20 @@ def test_mixed_retau550_full_size(chflow_lib):
     assert max(errs.values()) < 1e-5, errs
 
 
-def test_mixed_accuracy_after_1000_steps(chflow_lib):
-    """The mixed form's accuracy target at Re_tau 180, 128 x 129 x 128: the
-    velocity (u, v, w) rel-L2 against the FP64 path after 1000 steps from the
-    same start is at most 1e-5."""
+@pytest.fixture(scope="module")
+def fp64_after_1000():
     cfg = config.CONFIGS["c3_retau180_128"]
     st = fields.turbulent_start_state(cfg, seed=0)
-    a = run(cfg, st, "fp64", 1000, zpad=200)
-    b = run(cfg, st, "mixed", 1000, zpad=200)
+    return cfg, st, run(cfg, st, "fp64", 1000, zpad=200)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fp64solve"])
+def test_mixed_accuracy_after_1000_steps(chflow_lib, fp64_after_1000, precision):
+    """The mixed forms' accuracy target at Re_tau 180, 128 x 129 x 128: the
+    velocity (u, v, w) rel-L2 against the FP64 path after 1000 steps from the
+    same start is at most 1e-5."""
+    cfg, st, a = fp64_after_1000
+    b = run(cfg, st, precision, 1000, zpad=200)
     num = den = 0.0
     for k in VEL:
         pa, pb = split(a[k], k)[k], split(b[k], k)[k]

@@ -291,7 +291,7 @@ def test_mean_lamb_accuracy(chflow_lib, oracle_mod, name):
     assert err_g <= max(2.0 * err_o, 1e-13), (err_g, err_o)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_fp64solve"])
 def test_step_graph_matches_direct_launches(chflow_lib, precision):
     """chf_step replays a captured graph for pairs of steps; the state after
     7 steps (3 replays and one direct step) is bit-identical to 7 direct

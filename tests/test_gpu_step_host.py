@@ -27,7 +27,7 @@ def copy(st):
     return {k: np.ascontiguousarray(st[k], dtype=np.float64).copy() for k in FIELD_NAMES + MEAN_NAMES}
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_fp64solve"])
 @pytest.mark.parametrize("nsteps", [1, 3])
 def test_step_host_matches_upload_step_download(chflow_lib, precision, nsteps):
     st = start()
