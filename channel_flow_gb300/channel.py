@@ -26,7 +26,8 @@ EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
            "chf_diagnostics_static", "chf_write_restart", "chf_read_restart",
            "chf_batch_create", "chf_batch_destroy", "chf_batch_last_error", "chf_batch_size",
            "chf_batch_handle", "chf_batch_step", "chf_batch_synchronize",
-           "chf_set_flow_rate", "chf_get_flow_rate", "chf_statistics", "chf_pressure")
+           "chf_set_flow_rate", "chf_get_flow_rate", "chf_statistics", "chf_pressure",
+           "chf_transform", "chf_cfl", "chf_physical_velocity", "chf_write_velocity")
 
 
 class ChannelError(RuntimeError):
@@ -99,6 +100,10 @@ def load_library(path: str = None):
     L.chf_get_flow_rate.argtypes = [vp, dp, dp, dp]
     L.chf_statistics.argtypes = [vp, dp, ctypes.POINTER(CStats)]
     L.chf_pressure.argtypes = [vp, dp]
+    L.chf_transform.argtypes = [vp, ctypes.c_int, dp]
+    L.chf_cfl.argtypes = [vp, dp, dp, dp]
+    L.chf_physical_velocity.argtypes = [vp, dp, dp]
+    L.chf_write_velocity.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, dp]
     for name in EXPORTS:
         getattr(L, name).restype = getattr(L, name).restype or ctypes.c_int
     L.chf_last_error.restype = ctypes.c_char_p
@@ -247,6 +252,36 @@ class Channel:
         out = np.zeros(self.shape)
         self._check(self.L.chf_pressure(self.h, _dptr(out)))
         return out
+
+    def transform(self, isign: int, u: np.ndarray) -> np.ndarray:
+        """transform (poiseuilleflow.f90:919-1005) of one array in the field
+        layout on the device: isign = 1 spectral -> physical grid, -1 back.
+        Returns a new array."""
+        a = np.ascontiguousarray(u, dtype=np.float64).copy()
+        if a.shape != self.shape:
+            raise ChannelError(-1, f"shape {a.shape} != {self.shape}")
+        self._check(self.L.chf_transform(self.h, int(isign), _dptr(a)))
+        return a
+
+    def cfl(self) -> dict:
+        """CFL_X (streamwise), CFL_Y (wall-normal), CFL_Z (spanwise) of the
+        current state, as statistics prints them."""
+        x, y, z = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.L.chf_cfl(self.h, ctypes.byref(x), ctypes.byref(y), ctypes.byref(z)))
+        return {"cfl_x": x.value, "cfl_y": y.value, "cfl_z": z.value}
+
+    def physical_velocity(self, u0=None) -> np.ndarray:
+        """(u + u0, w, v) on the physical grid, shape (3, nz+1, nny, nnx):
+        the reference's ftmp(i, j, k, m) of the 3Ddata dump."""
+        out = np.empty((3,) + self.shape)
+        p0 = None if u0 is None else np.ascontiguousarray(u0, dtype=np.float64)
+        self._check(self.L.chf_physical_velocity(self.h, _dptr(p0), _dptr(out)))
+        return out
+
+    def write_velocity(self, directory: str, nproc: int = 1, istep: int = 0, u0=None):
+        """The 3Ddata dump files velocity<istep>.<rank>.dat in directory."""
+        p0 = None if u0 is None else np.ascontiguousarray(u0, dtype=np.float64)
+        self._check(self.L.chf_write_velocity(self.h, os.fsencode(directory), int(nproc), int(istep), _dptr(p0)))
 
     def set_flow_rate(self, bulk_velocity: float):
         """Hold the bulk velocity at bulk_velocity (> 0) by adjusting the mean

@@ -127,6 +127,11 @@ struct Handle {
   void* scratch = nullptr;  // reduction scratch (diagnostics)
   void* stats_buf = nullptr;  // chf_statistics: GL values of u, v, w + plane sums (first call)
   void* pres_buf = nullptr;   // chf_pressure: Lamb coefficients, right-hand sides, P (first call)
+  // physical space (chf_phys.cu, first call): three field-sized FP64
+  // buffers, plane maxima, and the unpadded x / y transform plans
+  void* phys_buf = nullptr;
+  FftPlan pxu{}, pyu{};       // nnx, nny
+  cd *tw_pxu = nullptr, *tw_pyu = nullptr;
   size_t scratch_bytes = 0;
 
   // mixed-precision path (k_mixed.cu): FP32 transforms, tcgen05 GEMMs
@@ -258,4 +263,6 @@ int launch_diagnostics(Handle* h, chf_diag* out);
 
 // FFT plan helper (host)
 FftPlan make_plan(int L);
+// tw[k] = exp(-2 pi i k / L), k = 0..L-1 (host, libm)
+std::vector<cd> twiddles(int L);
 }  // namespace chf

@@ -4,7 +4,8 @@
 // (0,0) mode, written as an FP64 state plus an increment:
 //   x = c + delta,   delta = A^-1 (B - A) c + A^-1 r,
 //   r = dt (3/2 N^n - 1/2 N^{n-1})
-// on the collocation rows and 0 on the wall rows, with B - A =
+// on the collocation rows and minus the wall residual of c on the wall rows
+// (0 for coefficients that satisfy the walls), with B - A =
 // (dt/re) (D^2 - k^2)^2 for v and (dt/re) (D^2 - k^2) for omega_y (the CN
 // operators of get_coef_v / get_coef_omegay and of get_coef_rhs /
 // get_rhs_omegay, REF:3348-3489) and A^-1 the even/odd inverses of
@@ -307,6 +308,45 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
       const float mx = __int_as_float(s_cexp[threadIdx.x]);
       if (mx > 0.f) (void)frexpf(mx, &e);
       s_cexp[threadIdx.x] = max(-60, e);
+    }
+    // Wall rows of the staged right-hand side: minus the wall residual of c,
+    // in FP64, one warp per (mode, block).  M = A^-1 (B - A) has zero wall
+    // rows, so without this term x would keep the wall values of c; with it,
+    // A x = B' c + r with B' zero on the wall rows, the equations the
+    // reference solves (its wall rows hold the boundary values, 0), also
+    // for coefficients that do not satisfy the walls (an uploaded initial
+    // field).  Folded wall rows of the operators (k_invert): row 0 sums c_j
+    // (value at the wall), row 1 of v sums j^2 c_j (slope at the wall).  For
+    // coefficients that satisfy the walls the residual is rounding.
+    {
+      const int lane = threadIdx.x & 31;
+      for (int task = threadIdx.x >> 5; task < nm * 4; task += blockDim.x >> 5) {
+        const int q = task >> 2, b = task & 3;
+        const int n = b == 0 ? sl.ne_v : b == 1 ? sl.no_v : b == 2 ? sl.ne_w : sl.no_w;
+        const int roff = b == 0 ? 0 : b == 1 ? sl.ne_v : b == 2 ? NZ : NZ + sl.ne_w;
+        const cd* cb = Cd + q * 2 * NZ + roff;
+        double s0r = 0.0, s0i = 0.0, s1r = 0.0, s1i = 0.0;
+        for (int c = lane; c < n; c += 32) {
+          const cd x = cb[c];
+          const int j = (b == 0 || b == 2) ? 2 * c : 2 * c + 1;
+          const double jj = (double)(j * j);
+          s0r += x.re;
+          s0i += x.im;
+          s1r = fma(jj, x.re, s1r);
+          s1i = fma(jj, x.im, s1i);
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+          s0r += __shfl_xor_sync(0xffffffffu, s0r, off);
+          s0i += __shfl_xor_sync(0xffffffffu, s0i, off);
+          s1r += __shfl_xor_sync(0xffffffffu, s1r, off);
+          s1i += __shfl_xor_sync(0xffffffffu, s1i, off);
+        }
+        if (lane == 0) {
+          float2* rs = Rs + q * 2 * NZ + roff;
+          rs[0] = make_float2((float)-s0r, (float)-s0i);
+          if (b < 2) rs[1] = make_float2((float)-s1r, (float)-s1i);
+        }
+      }
     }
     __syncthreads();
     const signed char* rexp = rowexp + (size_t)grp * 2 * NZ;

@@ -100,3 +100,45 @@ def read_restart(cfg: ChannelConfig, directory: str, nproc: int = 1, tag: int = 
         for i, k in enumerate(REC2):
             st[k][:, :, r * w:(r + 1) * w] = d[i]
     return st
+
+
+# ---------------------------------------------------------------------------
+# The 3Ddata velocity dump of statistics (poiseuilleflow.f90:2745-2764):
+# one file per rank, one record ftmp(0:nx, 0:ny, 0:nz, 1:3) of the rank's
+# streamwise slab of nnx / nproc physical points (u + u0, w, v), read and
+# joined by post-processing/post_poiseuilleflow.f90:63-70.
+# ---------------------------------------------------------------------------
+def velocity_file_name(istep: int, rank: int) -> str:
+    """Format 212 of statistics: 'velocity', i8.8, '.', i3.3, '.dat'."""
+    return f"velocity{istep:08d}.{rank:03d}.dat"
+
+
+def write_velocity_dump(cfg: ChannelConfig, vel: np.ndarray, directory: str, istep: int = 0,
+                        nproc: int = 1) -> list:
+    """Write vel (3, nz+1, nny, nnx) = (u + u0, w, v) on the physical grid as
+    nproc rank files; returns their paths."""
+    w = check_nproc(cfg, nproc)
+    paths = []
+    for r in range(nproc):
+        p = os.path.join(directory, velocity_file_name(istep, r))
+        with open(p, "wb") as f:
+            _write_record(f, [vel[:, :, :, r * w:(r + 1) * w]])
+        paths.append(p)
+    return paths
+
+
+def read_velocity_dump(cfg: ChannelConfig, directory: str, istep: int = 0, nproc: int = 1) -> np.ndarray:
+    """Join nproc rank files of the velocity dump into (3, nz+1, nny, nnx),
+    the array ftmp2 that post_poiseuilleflow.f90:63-70 assembles."""
+    w = check_nproc(cfg, nproc)
+    nz1 = cfg.nnz + 1
+    out = np.zeros((3, nz1, cfg.nny, cfg.nnx))
+    n = 3 * w * cfg.nny * nz1 * 8
+    for r in range(nproc):
+        p = os.path.join(directory, velocity_file_name(istep, r))
+        with open(p, "rb") as f:
+            d = _read_record(f, n, p).reshape(3, nz1, cfg.nny, w)
+            if f.read(1):
+                raise ValueError(f"{p}: data after the record")
+        out[:, :, :, r * w:(r + 1) * w] = d
+    return out

@@ -192,6 +192,46 @@ typedef struct chf_stats {
 } chf_stats;
 int chf_statistics(chf_handle* h, double* profiles, chf_stats* out);
 
+/* Physical space (FP64 for either precision; the first of these calls
+ * allocates three field-sized work buffers, kept until chf_destroy; all are
+ * synchronous).  The physical grid is the unpadded one of transform:
+ * x_i = 2 pi aphi i / nnx, y_j = 2 pi beta j / nny, z_k = cos(pi k / nz),
+ * stored as a field array (0:nx,0:ny,0:nz) with x the physical point index.
+ *
+ * chf_transform: transform (poiseuilleflow.f90:919-1005, with fourtrx_zcomp
+ * :774-913) of one host array in place.  isign = 1: spectral (Chebyshev
+ * coefficients in z, interleaved (re, im) streamwise modes, spanwise modes)
+ * to physical values, spanwise and streamwise Nyquist modes dropped;
+ * isign = -1: physical values to the spectral layout (all nny spanwise
+ * slots, streamwise modes 0..nnx/2-1, normalised by 1/(nnx nny)). */
+int chf_transform(chf_handle* h, int isign, double* u);
+
+/* The CFL numbers printed by statistics (poiseuilleflow.f90:2866-2934), of
+ * the current state (call after a solve, where statistics is called):
+ * cfl_x = max|u| dt / dx (streamwise), cfl_z = max|w| dt / dz (spanwise,
+ * dz = 2 pi beta / nny), cfl_y = max over the interior planes k = 1..nz-1 of
+ * max|v| dt / dy(k) (wall-normal; dy(k) the Gauss-Lobatto spacing of
+ * statistics, mirrored about the centre).  Maxima over the physical grid;
+ * u includes the mean mode au0.  Any pointer may be NULL. */
+int chf_cfl(chf_handle* h, double* cfl_x, double* cfl_y, double* cfl_z);
+
+/* The instantaneous physical velocity of the 3Ddata dump of statistics
+ * (poiseuilleflow.f90:2745-2764): out (0:nnx-1, 0:nny-1, 0:nz, 3) real*8,
+ * Fortran order, component 1 = u + u0(k) (streamwise), 2 = w (spanwise),
+ * 3 = v (wall-normal).  u0: base-flow profile (nz + 1 doubles) added to u
+ * as the reference adds its u0, or NULL for none. */
+int chf_physical_velocity(chf_handle* h, const double* u0, double* out);
+
+/* That dump as statistics writes it: one Fortran unformatted sequential file
+ * per rank, <dir>/velocity<istep:8>.<rank:3>.dat (format 212 of
+ * poiseuilleflow.f90:2749-2750), one record holding ftmp(0:nx,0:ny,0:nz,1:3)
+ * of the rank's streamwise slab of nnx / nproc physical points, framed by
+ * 4-byte byte counts; post-processing/post_poiseuilleflow.f90:63-70 reads
+ * and joins the slabs.  nproc follows the reference's constraints (nnx a
+ * multiple of 2 nproc, nny / 2 a multiple of nproc) and a record must stay
+ * below 2 GiB, else CHF_E_INVALID. */
+int chf_write_velocity(chf_handle* h, const char* dir, int nproc, int istep, const double* u0);
+
 /* Pressure of the current state (after a solve: velocities and vorticities
  * in the module arrays), as Chebyshev coefficients in the field layout
  * (p_out: (0:nx,0:ny,0:nz) real*8, host).  The reference's pressure routine

@@ -154,3 +154,18 @@ def test_mixed_accuracy_after_1000_steps(chflow_lib, fp64_after_1000, precision)
         den += float(np.sum(pa ** 2))
     vel = (num / den) ** 0.5
     assert vel <= 1e-5, (vel, vel_err(b, a))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_fp64solve"])
+@pytest.mark.parametrize("name", ["small16", "c1_32", "mixed_radix"])
+def test_mixed_from_reference_initial_field(chflow_lib, name, precision):
+    """The analytic-plus-point-noise start of the reference's input
+    (poiseuilleflow.f90:2086-2339): white noise in every mode, and a wall
+    slope of v that the first solve has to remove (the reference's wall rows
+    hold the boundary values).  Both mixed forms follow the FP64 path."""
+    cfg = CASES[name]
+    st = fields.reference_like_state(cfg, seed=3, epsilon=0.3, noise=0.02, gamma=5.0)
+    a = run(cfg, st, "fp64", 5)
+    b = run(cfg, st, precision, 5)
+    errs = vel_err(b, a)
+    assert max(errs.values()) < 1e-5, errs

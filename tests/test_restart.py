@@ -81,3 +81,25 @@ def test_rejects_bad_layouts(tmp_path):
     open(p, "wb").write(raw[:-100])
     with pytest.raises(ValueError):
         restart.read_restart(CFG, str(tmp_path), nproc=2)        # truncated
+
+
+@pytest.mark.parametrize("nproc", [1, 2, 4])
+def test_velocity_dump_round_trip(tmp_path, nproc):
+    """The 3Ddata dump: one record of ftmp(0:nx,0:ny,0:nz,1:3) per rank
+    (Fortran order, i fastest), framed by 4-byte byte counts; the reader
+    joins the streamwise slabs as post_poiseuilleflow.f90:63-70 does."""
+    rng = np.random.default_rng(nproc)
+    vel = rng.standard_normal((3, CFG.nnz + 1, CFG.nny, CFG.nnx))
+    paths = restart.write_velocity_dump(CFG, vel, str(tmp_path), istep=1000, nproc=nproc)
+    assert [os.path.basename(p) for p in paths] == [f"velocity00001000.{r:03d}.dat" for r in range(nproc)]
+    w = CFG.nnx // nproc
+    raw = np.fromfile(paths[-1], dtype=np.uint8)
+    n = 3 * w * CFG.nny * (CFG.nnz + 1) * 8
+    assert raw.size == n + 8
+    assert int(raw[:4].view("<u4")[0]) == n and int(raw[-4:].view("<u4")[0]) == n
+    # element (i, j, k, m) of the last rank's slab, Fortran order
+    body = raw[4:-4].view("<f8").reshape(3, CFG.nnz + 1, CFG.nny, w)
+    i, j, k, m = 1, 3, 5, 2
+    assert body[m, k, j, i] == vel[m, k, j, (nproc - 1) * w + i]
+    back = restart.read_velocity_dump(CFG, str(tmp_path), istep=1000, nproc=nproc)
+    assert np.array_equal(back, vel)
