@@ -451,7 +451,7 @@ def main():
     if accuracy is not None:
         line["accuracy"] = accuracy
     if args.ensemble > 0:
-        line["ensemble"] = ensemble_rate(args.ensemble, local, args.precision)
+        line["ensemble"] = ensemble_rate(args.ensemble, local)
     if fp64_rate is not None:
         line["fp64_steps_per_s"] = fp64_rate
         line["mixed_over_fp64"] = value / world / fp64_rate
@@ -506,18 +506,21 @@ def ensemble_configs(n, seed=5):
     return out
 
 
-def ensemble_rate(n, device, precision, steps=20, warmup=4):
-    """Channel-steps/s of n uneven channels advanced by one chf_batch (one
-    graph launch per pair of steps, channels side by side), and of the same
-    channels stepped one after another on one stream (chf_step each)."""
+def ensemble_rate(n, device, precision="mixed_fp64solve", steps=20, warmup=4):
+    """Channel-steps/s of n uneven channels advanced by one chf_batch (channels
+    of one grid stacked into one set of buffers, one graph launch per pair of
+    steps), of the same channels stepped one after another on one stream
+    (chf_step each, same precision), and of the plain FP64 path one channel
+    after another.  Host wall clock around the calls and a synchronize."""
     import torch
-    from channel_flow_gb300 import Batch, fields
+    from channel_flow_gb300 import Batch, Channel, fields
     cfgs = ensemble_configs(n)
+    starts = [fields.turbulent_start_state(c, seed=100 + i) for i, c in enumerate(cfgs)]
     t0 = time.perf_counter()
     b = Batch(cfgs, precision=precision, device=device)
     t_create = time.perf_counter() - t0
-    for i, (ch, c) in enumerate(zip(b, cfgs)):
-        ch.upload_state(fields.turbulent_start_state(c, seed=100 + i))
+    for ch, st in zip(b, starts):
+        ch.upload_state(st)
         ch.getnonlinear()
         ch.solve()
     b.step(warmup)
@@ -542,14 +545,36 @@ def ensemble_rate(n, device, precision, steps=20, warmup=4):
         ch.set_stream(None)
     finite = all(ch.diagnostics()["finite"] for ch in b)
     b.close()
+    # the plain FP64 path, one channel after another
+    f64 = []
+    for c, st in zip(cfgs, starts):
+        ch = Channel(c, precision="fp64", device=device)
+        ch.set_stream(s.cuda_stream)
+        ch.upload_state(st)
+        ch.getnonlinear()
+        ch.solve()
+        ch.step(2)
+        f64.append(ch)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for ch in f64:
+        ch.step(steps)
+    torch.cuda.synchronize(device)
+    t_f64 = time.perf_counter() - t0
+    for ch in f64:
+        ch.close()
     points = sum(c.points for c in cfgs)
     return {"channels": n, "precision": precision, "steps": steps,
             "workload": "nnz in {32,64,96}, nnx = nny in {32,64}, Re_tau U[100,300], 2pi x 2 x pi, dt 2e-4",
             "channel_steps_per_s": n * steps / t_batch,
             "grid_point_steps_per_s": points * steps / t_batch,
             "sequential_channel_steps_per_s": n * steps / t_seq,
-            "batch_over_sequential": t_seq / t_batch, "create_s": t_create, "finite": finite,
-            "timing": "host wall clock around chf_batch_step + synchronize"}
+            "batch_over_sequential": t_seq / t_batch,
+            "fp64_sequential_grid_point_steps_per_s": points * steps / t_f64,
+            "batch_over_fp64_sequential": t_f64 / t_batch,
+            "create_s": t_create, "finite": finite,
+            "timing": "host wall clock around chf_batch_step + synchronize (the batch call gathers the channels "
+                      "into their classes and scatters them back once per call)"}
 
 
 def accuracy_vs_fp64(Channel, cfg, st, zpad, device, nsteps, forms=("mixed",)):

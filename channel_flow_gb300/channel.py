@@ -27,7 +27,8 @@ EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
            "chf_batch_create", "chf_batch_destroy", "chf_batch_last_error", "chf_batch_size",
            "chf_batch_handle", "chf_batch_step", "chf_batch_synchronize",
            "chf_set_flow_rate", "chf_get_flow_rate", "chf_statistics", "chf_pressure",
-           "chf_transform", "chf_cfl", "chf_physical_velocity", "chf_write_velocity")
+           "chf_transform", "chf_cfl", "chf_physical_velocity", "chf_write_velocity",
+           "chf_autotune", "chf_tuning")
 
 
 class ChannelError(RuntimeError):
@@ -101,6 +102,8 @@ def load_library(path: str = None):
     L.chf_statistics.argtypes = [vp, dp, ctypes.POINTER(CStats)]
     L.chf_pressure.argtypes = [vp, dp]
     L.chf_transform.argtypes = [vp, ctypes.c_int, dp]
+    L.chf_autotune.argtypes = [vp, ctypes.c_int]
+    L.chf_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
     L.chf_cfl.argtypes = [vp, dp, dp, dp]
     L.chf_physical_velocity.argtypes = [vp, dp, dp]
     L.chf_write_velocity.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, dp]
@@ -252,6 +255,17 @@ class Channel:
         out = np.zeros(self.shape)
         self._check(self.L.chf_pressure(self.h, _dptr(out)))
         return out
+
+    def autotune(self, reps: int = 3) -> str:
+        """Pick launch shapes and FFT radix orders by timing steps of the
+        current state (chf_autotune); returns the choice as text."""
+        self._check(self.L.chf_autotune(self.h, int(reps)))
+        return self.tuning()
+
+    def tuning(self) -> str:
+        buf = ctypes.create_string_buffer(1024)
+        self._check(self.L.chf_tuning(self.h, buf, len(buf)))
+        return buf.value.decode()
 
     def transform(self, isign: int, u: np.ndarray) -> np.ndarray:
         """transform (poiseuilleflow.f90:919-1005) of one array in the field

@@ -126,7 +126,7 @@ static void release(chf_handle* h) {
   for (auto& p : h->mean) cudaFree(p);
   void* ptrs[] = {h->iapha, h->ibeta, h->t0, h->t2, h->t4, h->k2vals, h->xinv, h->xmean,
                   h->group_start, h->group_modes, h->tw_py, h->tw_px, h->tw_z2, h->tw_zm,
-                  h->twf_py, h->twf_px, h->incm, h->incx, h->incr_exp, h->phi, h->flow, h->stats_buf, h->pres_buf, h->phys_buf, h->tw_pxu, h->tw_pyu, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
+                  h->twf_py, h->twf_px, h->incm, h->incx, h->incr_exp, h->phi, h->flow, h->stats_buf, h->pres_buf, h->phys_buf, h->tw_pxu, h->tw_pyu, h->group_re, h->ubphi_dev, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
                   h->agl, h->bimg, h->wz32, h->wy32, h->lc64, h->aexp1, h->aexp2, h->aexp3, h->bexp, h->z2_tail, h->gl_tail};
   for (void* p : ptrs) cudaFree(p);
   for (auto& p : h->pending) {
@@ -240,6 +240,8 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
   d.PY = 3 * cfg->nny / 2;
   d.MZ = cfg->zpad == 0 ? 2 * cfg->nnz : cfg->zpad;
   d.MP = d.MZ + 1;
+  d.nch = 1;
+  d.chm = d.modes();
   auto fail = [&](int code) {
     g_create_error = h->err.empty() ? "chf_create failed" : h->err;
     release(h);
@@ -299,6 +301,7 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
                  "twiddle upload"))
       return fail(CHF_E_CUDA);
   }
+  apply_cached_tuning(h);  // a measured choice for this grid earlier in the process
   int rc = setup_solver(h);
   if (rc != CHF_OK) return fail(rc);
   if (mixed_front(h)) {
@@ -414,7 +417,7 @@ int chf_step(chf_handle* h, int nsteps) {
   }
   if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice")) return CHF_E_CUDA;
   int s = 0;
-  if (nsteps >= 2) {
+  if (nsteps - s >= 2) {
     cudaGraphExec_t g = nullptr;
     int rc = pair_graph(h, &g);
     if (rc != CHF_OK) return rc;

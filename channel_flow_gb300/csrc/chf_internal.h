@@ -29,9 +29,27 @@ struct Dims {
   int PY;   // padded spanwise points = 3 nny / 2
   int MZ;   // product-grid intervals in z (2 nnz in the reference)
   int MP;   // product-grid points = MZ + 1
+  // Channels stacked in one set of buffers (an ensemble class of identical
+  // grids, chf_batch.cu): KY = nch * nny spanwise slots, channel c in slots
+  // c nny .. c nny + nny - 1, so a plane is [channel][ky][kx] and the z
+  // passes, GEMMs and solves see nch times the modes; NYQ and the FFT passes
+  // stay per channel.  chm = modes of one channel.  nch = 1: one channel.
+  int nch;
+  long chm;
   __host__ __device__ long modes() const { return (long)KX * KY; }
   __host__ __device__ size_t field_elems() const { return (size_t)NZ * KY * KX; }  // complex elements
 };
+
+// The Dims the x/y FFT passes see: one channel's spanwise modes, and the
+// product-grid planes of every stacked channel as separate planes (a plane
+// p of channel c is plane p nch + c).  The identity for one channel.
+__host__ __device__ inline Dims fft_view(Dims d) {
+  d.KY /= d.nch;
+  d.MP *= d.nch;
+  d.nch = 1;
+  d.chm = (long)d.KX * d.KY;
+  return d;
+}
 
 // Tensor-core GEMM plans (k_tcgemm.cu): K in chunks of at most TC_KC.
 constexpr int TC_KC = 32;
@@ -78,8 +96,21 @@ __host__ __device__ inline BlockOffsets block_offsets(const SolveLayout& s) {
   return b;
 }
 
+// Launch shapes chosen by measurement (chf_tune.cu).  0 = the rule of the
+// launcher (the largest shape that fits).
+struct Tuning {
+  int kxb = 0;      // streamwise modes per CTA of the shared-memory y transforms
+  int xr = 0;       // (plane, y) rows per CTA of the shared-memory x transform
+  int zl_c2v = 0;   // modes per CTA of the FP64 z transform to the product grid
+  int zl_curl = 0;  // modes per CTA of the FP64 z transform + curl
+  int inc_mch = 4;  // modes per pass of the increment solve (2 or 4)
+  int inc_cb = 3;   // matrix columns per load batch of the increment solve (2..4)
+  bool tuned = false;
+};
+
 struct Handle {
   chf_config cfg;
+  Tuning tune;
   Dims d;
   int device = 0;
   int num_sms = 1;  // multiprocessors of the device (persistent-kernel grids)
@@ -115,6 +146,11 @@ struct Handle {
   double* phi = nullptr;
   double ubphi = 0.0;
   double* flow = nullptr;
+  // stacked channels (d.nch > 1): per-group Reynolds number (group_re[g],
+  // the (0,0) groups nk2 .. nk2 + nch - 1 last), per-channel phi [nch][NZ],
+  // flow words [nch][4] and bulk velocities of phi (ubphi_dev[nch])
+  double* group_re = nullptr;
+  double* ubphi_dev = nullptr;
 
   // FFT plans and twiddles
   FftPlan py, px, pz2, pzm;   // PY, PX, 2N, 2MZ
@@ -263,6 +299,11 @@ int launch_diagnostics(Handle* h, chf_diag* out);
 
 // FFT plan helper (host)
 FftPlan make_plan(int L);
+// autotuner (chf_tune.cu): launch shapes the rules accept for a knob (0 kxb,
+// 1 xr, 2 zl_c2v, 3 zl_curl; k_nonlinear.cu), and the process's cached
+// choice for a new handle's key
+std::vector<int> shape_candidates(const Handle* h, int knob);
+void apply_cached_tuning(Handle* h);
 // tw[k] = exp(-2 pi i k / L), k = 0..L-1 (host, libm)
 std::vector<cd> twiddles(int L);
 }  // namespace chf

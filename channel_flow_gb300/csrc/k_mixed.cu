@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(CURL_THREADS, 16) k_curl(const double* __restr
   const double a = iapha[m % d.KX], b = ibeta[m / d.KX], k2 = a * a + b * b;
   const double s = (cl & 1) ? 1.0 : -1.0;  // (i z)_re = -z_im, (i z)_im = z_re
   const double sa = s * a, sb = s * b;
-  const bool mean = (m == 0);
+  const bool mean = (m % d.chm == 0);  // a channel's (0,0) mode
   // the mean column reads its own H1, H3 and passes them through
   const long pcol = mean ? cl : (cl ^ 1);
   const double* H1 = lc;
@@ -173,9 +173,17 @@ __global__ void __launch_bounds__(CURL_THREADS, 16) k_curl(const double* __restr
 
 // (0,0)-mode histories: the GL GEMM left the GL values of H1(0,0), H3(0,0)
 // in mode 0 of the h_v / h_g buffers.  clamb*nm1 <- clamb*n (REF:1560-1569),
-// clamb*n <- those values, mode 0 of h_v / h_g <- 0 (k^2 = 0 there).
+// clamb*n <- those values, mode 0 of h_v / h_g <- 0 (k^2 = 0 there).  One
+// CTA per stacked channel c: its mode c chm, its mean arrays at c * 2 NZ.
 __global__ void k_meanfix(cd* __restrict__ hv, cd* __restrict__ hg, double* cl1n, double* cl1nm1,
-                          double* cl3n, double* cl3nm1, int NZ, long modes) {
+                          double* cl3n, double* cl3nm1, int NZ, long modes, long chm) {
+  const long c = blockIdx.x;
+  hv += c * chm;
+  hg += c * chm;
+  cl1n += c * 2 * NZ;
+  cl1nm1 += c * 2 * NZ;
+  cl3n += c * 2 * NZ;
+  cl3nm1 += c * 2 * NZ;
   for (int p = threadIdx.x; p < NZ; p += blockDim.x) {
     cd a = hv[(size_t)p * modes], b = hg[(size_t)p * modes];
     cl1nm1[2 * p] = cl1n[2 * p];
@@ -262,7 +270,7 @@ int setup_mixed(Handle* h) {
   if (!cuda_ok(h, cudaMalloc((void**)&h->bimg, h->bimg_bytes), "B images") ||
       !cuda_ok(h, cudaMemsetAsync(h->bimg, 0, h->bimg_bytes, h->stream), "B images") ||
       !cuda_ok(h, cudaMalloc((void**)&h->wz32, sizeof(cf) * 6 * (size_t)MP * d.modes()), "wz32") ||
-      !cuda_ok(h, cudaMalloc((void**)&h->wy32, sizeof(cf) * 6 * (size_t)MP * d.PY * d.KX), "wy32") ||
+      !cuda_ok(h, cudaMalloc((void**)&h->wy32, sizeof(cf) * 6 * (size_t)fft_view(d).MP * d.PY * d.KX), "wy32") ||
       !cuda_ok(h, cudaMalloc((void**)&h->lc64, sizeof(double) * 3 * (size_t)NZ * cols), "lc64"))
     return CHF_E_NOMEM;
   // FP32 twiddles
@@ -363,8 +371,8 @@ int launch_nonlinear_mixed(Handle* h, const cudaEvent_t* field_ready) {
   {
     cudaEvent_t ev;
     prof_begin(h, K_MEANFIX, &ev);
-    k_meanfix<<<1, 256, 0, h->stream>>>(h->f[F_U], h->f[F_W], h->mean[M_CL1N], h->mean[M_CL1NM1],
-                                        h->mean[M_CL3N], h->mean[M_CL3NM1], d.NZ, modes);
+    k_meanfix<<<d.nch, 256, 0, h->stream>>>(h->f[F_U], h->f[F_W], h->mean[M_CL1N], h->mean[M_CL1NM1],
+                                            h->mean[M_CL3N], h->mean[M_CL3NM1], d.NZ, modes, d.chm);
     prof_end(h, K_MEANFIX, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_meanfix")) return CHF_E_CUDA;
   }

@@ -646,7 +646,7 @@ int pick_zl_curl(const Dims& d) {
 
 template <typename T, int XR>
 int run_xprod(Handle* h, cplx<T>* wy, const cplx<T>* tw_px) {
-  const Dims& d = h->d;
+  const Dims d = fft_view(h->d);
   const size_t smem = xprod_smem<T>(d, XR);
   if (!set_smem(h, k_xprod<T, 5, XR>, smem)) return CHF_E_CUDA;
   const long nrows = (long)d.MP * d.PY;
@@ -692,13 +692,42 @@ int run_zcurl(Handle* h) {
 
 }  // namespace
 
+// Launch shapes the autotuner may try (chf_tune.cu): every shape the rules
+// above accept, largest first.  y / x candidates for the handle's FFT-pass
+// dimensions and arithmetic (fp32: the mixed path's FP32 transforms).
+std::vector<int> shape_candidates(const Handle* h, int knob) {
+  const Dims d = fft_view(h->d);
+  const bool f32 = h->cfg.precision != CHF_FP64;
+  std::vector<int> out;
+  if (knob == 0) {  // kxb
+    for (int b = 16; b >= 1; b /= 2) {
+      const size_t bytes = (f32 ? sizeof(cf) : sizeof(cd)) * b * (d.PY + 1);
+      if (d.KX % b == 0 && fft_fits(b, d.PY, Y_THREADS, 6) && bytes <= kMaxSmem) out.push_back(b);
+    }
+  } else if (knob == 1) {  // xr
+    for (int r = 8; r >= 1; r /= 2) {
+      const size_t bytes = f32 ? xprod_smem<float>(d, r) : xprod_smem<double>(d, r);
+      if (fft_fits(r * 3, d.PX, X_THREADS, 5) && bytes <= kMaxSmem) out.push_back(r);
+    }
+  } else if (knob == 2) {  // zl_c2v
+    for (int l = 8; l >= 2; l /= 2)
+      if (fft_fits(l, 2 * d.MZ, ZC_THREADS, 4) && zc2v_smem(d, l) <= kMaxSmem) out.push_back(l);
+  } else if (knob == 3) {  // zl_curl
+    for (int l = 8; l >= 2; l /= 2)
+      if (fft_fits(l, 2 * d.MZ, ZC_THREADS, 4) && fft_fits(2 * l, 2 * d.N, ZC_THREADS, 4) &&
+          zcurl_smem(d, l) <= kMaxSmem)
+        out.push_back(l);
+  }
+  return out;
+}
+
 // The FP32 register-FFT path of the x/y transforms, in two parts so that a
 // caller can run the inverse y transform field by field (fields f0 ..
 // f0 + nf - 1 of the six) and the products and forward transforms once.
 bool xy_register_path(const Dims& d) { return d.PX == 192 && d.PY == 192 && d.KX % YW_COLS == 0; }
 
 int launch_yinv_fields(Handle* h, cf* wz, cf* wy, const cf* tw_py, int f0, int nf) {
-  const Dims& d = h->d;
+  const Dims d = fft_view(h->d);
   constexpr int YC = YW_COLS;
   cudaEvent_t ev;
   prof_begin(h, K_YINV, &ev);
@@ -709,7 +738,7 @@ int launch_yinv_fields(Handle* h, cf* wz, cf* wy, const cf* tw_py, int f0, int n
 }
 
 int launch_xprod_yfwd(Handle* h, cf* wz, cf* wy, const cf* tw_py, const cf* tw_px) {
-  const Dims& d = h->d;
+  const Dims d = fft_view(h->d);
   constexpr int YC = YW_COLS;
   cudaStream_t st = h->stream;
   cudaEvent_t ev;
@@ -728,7 +757,7 @@ int launch_xprod_yfwd(Handle* h, cf* wz, cf* wy, const cf* tw_py, const cf* tw_p
 
 template <typename T>
 int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const cplx<T>* tw_px) {
-  const Dims& d = h->d;
+  const Dims d = fft_view(h->d);
   cudaStream_t st = h->stream;
   if (sizeof(T) == 4 && xy_register_path(d)) {
     // register-FFT specialisation of the 128-point directions, FP32 only: in
@@ -741,8 +770,8 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     const int rc = launch_yinv_fields(h, wzf, wyf, twy, 0, 6);
     return rc == CHF_OK ? launch_xprod_yfwd(h, wzf, wyf, twy, twx) : rc;
   }
-  const int kxb = pick_kxb<T>(d);
-  const int xr = pick_xr<T>(d);
+  const int kxb = h->tune.kxb ? h->tune.kxb : pick_kxb<T>(d);
+  const int xr = h->tune.xr ? h->tune.xr : pick_xr<T>(d);
   if (!kxb || !xr) {
     h->err = "x/y transforms: FFT length too large for the launch shapes";
     return CHF_E_INVALID;
@@ -784,8 +813,8 @@ template int launch_xy<float>(Handle*, cf*, cf*, const cf*, const cf*);
 int launch_nonlinear_fp64(Handle* h) {
   const Dims& d = h->d;
   // z inverse of the six fields u, v, w, ox, oy, oz
-  const int zl = pick_zl_c2v(d);
-  const int zc = pick_zl_curl(d);
+  const int zl = h->tune.zl_c2v ? h->tune.zl_c2v : pick_zl_c2v(d);
+  const int zc = h->tune.zl_curl ? h->tune.zl_curl : pick_zl_curl(d);
   if (!zl || !zc) {
     h->err = "z transforms: FFT length too large for the launch shapes";
     return CHF_E_INVALID;
@@ -806,7 +835,7 @@ int launch_nonlinear_fp64(Handle* h) {
 // work buffers wz / wy must exist.  For the pressure (chf_pressure).
 int launch_lamb_fp64(Handle* h, cd* hc) {
   const Dims& d = h->d;
-  const int zl = pick_zl_c2v(d);
+  const int zl = h->tune.zl_c2v ? h->tune.zl_c2v : pick_zl_c2v(d);
   if (!zl) {
     h->err = "z transforms: FFT length too large for the launch shapes";
     return CHF_E_INVALID;

@@ -179,6 +179,12 @@ struct SolveArgs {
   const double* phi;
   double ubphi;
   double* flow;
+  // stacked channels (d.nch > 1): groups nk2 .. nk2 + nch - 1 are the
+  // channels' (0,0) modes; per group Reynolds number, per channel phi
+  // ([nch][NZ]), flow word ([nch][4]), mean arrays ([nch][2 NZ]) and bulk
+  // velocity of phi; group_re NULL: re and ubphi above for every group
+  const double* group_re;
+  const double* ubphi_dev;
 };
 
 
@@ -264,8 +270,16 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
   for (int j = threadIdx.x; j < NZ; j += blockDim.x) s.tj[j] = 2.0 * (double)j;
   __syncthreads();
   const int g = blockIdx.x + a.g0;
-  const bool mean = (g == a.nk2);
-  const double dt = a.dt, re = a.re;
+  const bool mean = (g >= a.nk2);
+  const int mch = mean ? g - a.nk2 : 0;      // the channel of a (0,0) group
+  const long mean_mode = (long)mch * d.chm;  // its (0,0) mode
+  const double dt = a.dt, re = a.group_re ? a.group_re[g] : a.re;
+  double* const au0 = a.au0 + (size_t)mch * 2 * NZ;
+  double* const w0 = a.w0 + (size_t)mch * 2 * NZ;
+  const double* const cl1n = a.cl1n + (size_t)mch * 2 * NZ;
+  const double* const cl1nm1 = a.cl1nm1 + (size_t)mch * 2 * NZ;
+  const double* const cl3n = a.cl3n + (size_t)mch * 2 * NZ;
+  const double* const cl3nm1 = a.cl3nm1 + (size_t)mch * 2 * NZ;
   const double k2 = mean ? 0.0 : a.k2vals[g];
   const double* X = a.xinv + (size_t)g * a.sl.stride;
   const SolveLayout& sl = a.sl;
@@ -280,9 +294,9 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
       cd v{0.0, 0.0}, oy{0.0, 0.0}, rv{0.0, 0.0}, rg{0.0, 0.0};
       if (m < nm) {
         if (mean) {
-          const double* am = m == 0 ? a.au0 : a.w0;
-          const double* cln = m == 0 ? a.cl1n : a.cl3n;
-          const double* clm = m == 0 ? a.cl1nm1 : a.cl3nm1;
+          const double* am = m == 0 ? au0 : w0;
+          const double* cln = m == 0 ? cl1n : cl3n;
+          const double* clm = m == 0 ? cl1nm1 : cl3nm1;
           oy = cd{am[2 * n], am[2 * n + 1]};
           rg = cd{-1.0 * dt / 2.0 * (3.0 * cln[2 * n] - clm[2 * n]),
                   -1.0 * dt / 2.0 * (3.0 * cln[2 * n + 1] - clm[2 * n + 1])};
@@ -427,29 +441,32 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
       // pressure gradient re_p fixed): add the multiple of phi that restores
       // the target bulk velocity U_b = sum_{n even} Re(au0_n) / (1 - n^2);
       // the multiple is this step's extra mean pressure gradient
-      const double target = a.flow[0];
+      double* const flow = a.flow + 4 * mch;
+      const double* const phi = a.phi + (size_t)mch * NZ;
+      const double ubphi = a.ubphi_dev ? a.ubphi_dev[mch] : a.ubphi;
+      const double target = flow[0];
       if (target > 0.0 && warp == 0) {
         const int lane = tid & 31;
         double ub = 0.0;
         for (int n = lane; n < NZ; n += 32)
           if (!(n & 1)) ub += s.co[n].re / (1.0 - (double)n * (double)n);
         for (int off = 16; off > 0; off >>= 1) ub += __shfl_xor_sync(0xffffffffu, ub, off);
-        const double alpha = (target - ub) / a.ubphi;
-        for (int n = lane; n < NZ; n += 32) s.co[n].re += alpha * a.phi[n];
+        const double alpha = (target - ub) / ubphi;
+        for (int n = lane; n < NZ; n += 32) s.co[n].re += alpha * phi[n];
         if (lane == 0) {
-          a.flow[1] = alpha;
-          a.flow[2] = ub;
-          a.flow[3] = ub + alpha * a.ubphi;
+          flow[1] = alpha;
+          flow[2] = ub;
+          flow[3] = ub + alpha * ubphi;
         }
       }
       __syncthreads();
       for (int t = tid; t < nm * NZ; t += blockDim.x) {
         int m = t / NZ, n = t % NZ;
         cd x = s.co[t];
-        double* am = m == 0 ? a.au0 : a.w0;
+        double* am = m == 0 ? au0 : w0;
         am[2 * n] = x.re;
         am[2 * n + 1] = x.im;
-        (m == 0 ? a.u : a.w)[(size_t)n * modes] = x;
+        (m == 0 ? a.u : a.w)[(size_t)n * modes + mean_mode] = x;
       }
       for (int task = warp; task < nm * 2; task += S_WARPS) {
         int m = task / 2, comp = task % 2;
@@ -459,7 +476,7 @@ __global__ void __launch_bounds__(S_THREADS, 3) k_solve(const __grid_constant__ 
       for (int t = tid; t < nm * NZ; t += blockDim.x) {
         int m = t / NZ, n = t % NZ;
         const double sg = m == 0 ? -1.0 : 1.0;  // omega_z = -D au0, omega_x = D w0
-        (m == 0 ? a.oz : a.ox)[(size_t)n * modes] =
+        (m == 0 ? a.oz : a.ox)[(size_t)n * modes + mean_mode] =
             cd{sg * dslot(s, m, 0, NZ)[n], sg * dslot(s, m, 1, NZ)[n]};
       }
       __syncthreads();
@@ -746,6 +763,8 @@ static int launch_solve_from(Handle* h, int g0, cudaStream_t st) {
   a.ubphi = h->ubphi;
   a.flow = h->flow;
   a.nk2 = h->nk2;
+  a.group_re = h->group_re;
+  a.ubphi_dev = h->ubphi_dev;
   const int mb2 = fft_fits(2 * CH, 2 * d.N, S_THREADS, 2) ? 2 : 4;
   if (d.N + 1 > 32 * WD_EMAX || !fft_fits(2 * CH, 2 * d.N, S_THREADS, mb2)) {
     h->err = "k_solve: nnz too large for the launch shape";
@@ -760,7 +779,8 @@ static int launch_solve_from(Handle* h, int g0, cudaStream_t st) {
     return CHF_E_CUDA;
   cudaEvent_t ev;
   prof_begin(h, g0 == 0 ? K_SOLVE : K_SOLVE_MEAN, &ev);
-  kern<<<h->nk2 + 1 - g0, S_THREADS, smem, st>>>(a);
+  // groups g0 .. nk2 - 1 and the nch (0,0)-mode groups after them
+  kern<<<h->nk2 + h->d.nch - g0, S_THREADS, smem, st>>>(a);
   prof_end(h, g0 == 0 ? K_SOLVE : K_SOLVE_MEAN, ev);
   if (!cuda_ok(h, cudaGetLastError(), "k_solve")) return CHF_E_CUDA;
   return CHF_OK;

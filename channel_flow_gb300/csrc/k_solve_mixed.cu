@@ -4,16 +4,20 @@
 // (0,0) mode, written as an FP64 state plus an increment:
 //   x = c + delta,   delta = A^-1 (B - A) c + A^-1 r,
 //   r = dt (3/2 N^n - 1/2 N^{n-1})
-// on the collocation rows and minus the wall residual of c on the wall rows
-// (0 for coefficients that satisfy the walls), with B - A =
-// (dt/re) (D^2 - k^2)^2 for v and (dt/re) (D^2 - k^2) for omega_y (the CN
-// operators of get_coef_v / get_coef_omegay and of get_coef_rhs /
-// get_rhs_omegay, REF:3348-3489) and A^-1 the even/odd inverses of
-// k_solve.cu.  Forming (B - A) c at the collocation points cancels heavily
-// (fourth derivatives of the coefficients against an O(c) result), so the
-// set-up multiplies it into the inverse once per k^2 in FP64:
-// M = A^-1 (B - A) maps coefficients to coefficients and has no such
-// cancellation (its rows sum to within ~10x of the result).  A step is then
+// on the collocation rows and 0 on the wall rows, with B - A =
+// (dt/re) (D^2 - k^2)^2 for v and (dt/re) (D^2 - k^2) for omega_y on the
+// collocation rows (the CN operators of get_coef_v / get_coef_omegay and of
+// get_coef_rhs / get_rhs_omegay, REF:3348-3489) and minus the wall rows of A
+// on the wall rows (the reference's right-hand side holds the boundary
+// values, 0, there), and A^-1 the even/odd inverses of k_solve.cu.  Then
+// A x = B c + r with B's wall rows 0: the equations the reference solves,
+// for any c (also one that does not satisfy the walls, e.g. an uploaded
+// initial field).  Forming (B - A) c at the collocation points cancels
+// heavily (fourth derivatives of the coefficients against an O(c) result),
+// so the set-up multiplies it into the inverse once per k^2 in FP64:
+// M = A^-1 (B - A) = A^-1 B - I maps coefficients to coefficients and has no
+// such cancellation (its rows sum to within ~10x of the result; at 128^3
+// the largest row sum is ~150, the median ~2).  A step is then
 //   k_inc_solve    one CTA per k^2 group: delta = M c (compensated FP32 on
 //                  (hi, lo) splits of M and c, summed against a power-of-two
 //                  offset) + A^-1 r (FP32), x = c + delta in FP64
@@ -35,7 +39,9 @@ namespace chf {
 namespace {
 
 constexpr int MV_THREADS = 288;  // threads over the 2 NZ rows of one group's four blocks
-constexpr int MCH = 4;           // modes per pass in k_inc_solve
+// modes per pass (MCH) and matrix columns per load batch (CB) of
+// k_inc_solve are template parameters: the defaults 4 and 3, others picked
+// by the autotuner (chf_tune.cu)
 
 // Chebyshev derivative recurrence (dz, REF:570-599), descending in k:
 //   b_k = b_{k+2} + 2 (k+1) a_{k+1}   (b_0 halved on output)
@@ -45,7 +51,9 @@ constexpr int MCH = 4;           // modes per pass in k_inc_solve
 // block's inverse (k_solve.cu, FP64) and W the folded rows of B - A,
 //   W[q][c] = (dt/re) (T4 - 2 k^2 T2 + k^4 T0)(z_q, T_j)   (v)
 //   W[q][c] = (dt/re) (T2 - k^2 T0)(z_q, T_j)               (omega_y)
-// for q >= r0 (0 on the wall rows), j = 2c or 2c + 1, the kernel forms
+// for q >= r0 and minus the folded wall rows of A (k_invert: -1 for the
+// value rows, -j^2 for the slope row of v) for q < r0, j = 2c or 2c + 1, the
+// kernel forms
 // M = X W in FP64 (W staged BW columns at a time, X read through L1) and
 // stores it as (hi, lo) float pairs, and X as floats; both column-major,
 // M[c * n + r], at the inverses' block offsets.
@@ -79,6 +87,8 @@ __global__ void __launch_bounds__(256) k_build_incr(const double* __restrict__ t
       if (q >= r0 && cc < nc) {
         const size_t p = (size_t)q + (size_t)NZ * j;
         w = isv ? dt_re * (t4[p] - 2.0 * k2 * t2[p] + k2 * k2 * t0[p]) : dt_re * (t2[p] - k2 * t0[p]);
+      } else if (cc < nc) {
+        w = (isv && q == 1) ? -(double)j * (double)j : -1.0;
       }
       W[t] = w;
     }
@@ -86,7 +96,7 @@ __global__ void __launch_bounds__(256) k_build_incr(const double* __restrict__ t
     for (int t = threadIdx.x; t < n * nc; t += blockDim.x) {
       const int cc = t / n, r = t % n;
       double acc = 0.0;
-      for (int q = r0; q < n; ++q) acc = fma(X[(size_t)q * n + r], W[q * BW + cc], acc);
+      for (int q = 0; q < n; ++q) acc = fma(X[(size_t)q * n + r], W[q * BW + cc], acc);
       const float hi = (float)acc;
       incm[off + (size_t)(c0 + cc) * n + r] = make_float2(hi, (float)(acc - (double)hi));
     }
@@ -141,7 +151,7 @@ struct __align__(16) CoefHL {
   float hr, hi, lr, li;  // high and low parts of the real and imaginary parts
 };
 
-constexpr int CB = 3;  // matrix columns per load batch (two batches in flight)
+// CB matrix columns per load batch (two batches in flight)
 
 // Packed FP32 pairs (f32x2.cuh): the real and imaginary parts of a
 // coefficient travel together.
@@ -158,7 +168,7 @@ __device__ __forceinline__ void sig_mac2(f32x2 mh, f32x2 ml, f32x2 ch, f32x2 cl,
 
 // Rows of one pass of k_inc_solve for NM staged modes: thread t owns row t of
 // the four blocks (v even, v odd, omega even, omega odd).
-template <int NM>
+template <int NM, int CB>
 __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g, const float2* __restrict__ Mg,
                                          const float* __restrict__ Xg, const SolveLayout& sl,
                                          const BlockOffsets& bo, int NZ, long modes, const cd* Cd,
@@ -247,6 +257,7 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
   }
 }
 
+template <int MCH, int CB>
 __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v, cd* __restrict__ g,
                                                              const cd* __restrict__ rv, const cd* __restrict__ uh,
                                                              const cd* __restrict__ rg, const cd* __restrict__ wh,
@@ -309,52 +320,17 @@ __global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v,
       if (mx > 0.f) (void)frexpf(mx, &e);
       s_cexp[threadIdx.x] = max(-60, e);
     }
-    // Wall rows of the staged right-hand side: minus the wall residual of c,
-    // in FP64, one warp per (mode, block).  M = A^-1 (B - A) has zero wall
-    // rows, so without this term x would keep the wall values of c; with it,
-    // A x = B' c + r with B' zero on the wall rows, the equations the
-    // reference solves (its wall rows hold the boundary values, 0), also
-    // for coefficients that do not satisfy the walls (an uploaded initial
-    // field).  Folded wall rows of the operators (k_invert): row 0 sums c_j
-    // (value at the wall), row 1 of v sums j^2 c_j (slope at the wall).  For
-    // coefficients that satisfy the walls the residual is rounding.
-    {
-      const int lane = threadIdx.x & 31;
-      for (int task = threadIdx.x >> 5; task < nm * 4; task += blockDim.x >> 5) {
-        const int q = task >> 2, b = task & 3;
-        const int n = b == 0 ? sl.ne_v : b == 1 ? sl.no_v : b == 2 ? sl.ne_w : sl.no_w;
-        const int roff = b == 0 ? 0 : b == 1 ? sl.ne_v : b == 2 ? NZ : NZ + sl.ne_w;
-        const cd* cb = Cd + q * 2 * NZ + roff;
-        double s0r = 0.0, s0i = 0.0, s1r = 0.0, s1i = 0.0;
-        for (int c = lane; c < n; c += 32) {
-          const cd x = cb[c];
-          const int j = (b == 0 || b == 2) ? 2 * c : 2 * c + 1;
-          const double jj = (double)(j * j);
-          s0r += x.re;
-          s0i += x.im;
-          s1r = fma(jj, x.re, s1r);
-          s1i = fma(jj, x.im, s1i);
-        }
-        for (int off = 16; off > 0; off >>= 1) {
-          s0r += __shfl_xor_sync(0xffffffffu, s0r, off);
-          s0i += __shfl_xor_sync(0xffffffffu, s0i, off);
-          s1r += __shfl_xor_sync(0xffffffffu, s1r, off);
-          s1i += __shfl_xor_sync(0xffffffffu, s1i, off);
-        }
-        if (lane == 0) {
-          float2* rs = Rs + q * 2 * NZ + roff;
-          rs[0] = make_float2((float)-s0r, (float)-s0i);
-          if (b < 2) rs[1] = make_float2((float)-s1r, (float)-s1i);
-        }
-      }
-    }
     __syncthreads();
     const signed char* rexp = rowexp + (size_t)grp * 2 * NZ;
     switch (nm) {
-      case 1: inc_rows<1>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
-      case 2: inc_rows<2>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
-      case 3: inc_rows<3>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
-      default: inc_rows<4>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      case 1: inc_rows<1, CB>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      case 2: inc_rows<2, CB>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      default:
+        if constexpr (MCH >= 4) {
+          if (nm == 3) inc_rows<3, CB>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
+          else inc_rows<4, CB>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
+        }
+        break;
     }
     __syncthreads();
   }
@@ -394,7 +370,8 @@ __global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict
   const bool in = mt < modes;  // every lane takes part in the shuffles
   const long m = in ? mt : 0;
   const long col = 2 * m + comp;
-  const bool live = in && m > 0 && (m / d.KX) != d.NYQ;
+  // not a channel's (0,0) mode nor its spanwise Nyquist slot
+  const bool live = in && (m % d.chm) > 0 && ((m % d.chm) / d.KX) != d.NYQ;
   double sak = 0.0, sbk = 0.0, sa = 0.0, sb = 0.0;
   if (live) {
     // (i z)_re = -z_im, (i z)_im = z_re: the sign s of the partner term
@@ -517,13 +494,16 @@ int launch_solve_mixed(Handle* h) {
     if (!cuda_ok(h, cudaEventRecord(h->ev_join, h->side_stream), "solve join")) return CHF_E_CUDA;
   }
   if (h->nk2 > 0) {
-    const size_t smem = (sizeof(cd) + sizeof(CoefHL) + sizeof(float2)) * MCH * 2 * (size_t)NZ;
+    const int mch = h->tune.inc_mch == 2 ? 2 : 4, cb = h->tune.inc_cb;
+    auto kern = mch == 2 ? (cb == 2 ? k_inc_solve<2, 2> : cb == 4 ? k_inc_solve<2, 4> : k_inc_solve<2, 3>)
+                         : (cb == 2 ? k_inc_solve<4, 2> : cb == 4 ? k_inc_solve<4, 4> : k_inc_solve<4, 3>);
+    const size_t smem = (sizeof(cd) + sizeof(CoefHL) + sizeof(float2)) * mch * 2 * (size_t)NZ;
     if (smem > 48 * 1024 &&
-        !cuda_ok(h, cudaFuncSetAttribute(k_inc_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+        !cuda_ok(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                  "k_inc_solve smem"))
       return CHF_E_CUDA;
     prof_begin(h, K_INC_SOLVE, &ev);
-    k_inc_solve<<<h->nk2, MV_THREADS, smem, st>>>(h->f[F_V], h->f[F_OY], h->f[F_RV], h->f[F_U], h->f[F_RG],
+    kern<<<h->nk2, MV_THREADS, smem, st>>>(h->f[F_V], h->f[F_OY], h->f[F_RV], h->f[F_U], h->f[F_RG],
                                                    h->f[F_W], h->incm, h->incx, h->incr_exp, h->sl, h->group_start,
                                                    h->group_modes, d, (float)(1.5 * dt), (float)(0.5 * dt));
     prof_end(h, K_INC_SOLVE, ev);

@@ -165,6 +165,20 @@ int chf_device_field(chf_handle* h, int which, void** dptr);
  * library's own stream.  The caller keeps the stream alive while h uses it. */
 int chf_set_stream(chf_handle* h, void* stream);
 
+/* Autotuner, the counterpart of the reference's FFTW_MEASURE planning
+ * (poiseuilleflow.f90:100-112): times whole steps of the handle's state
+ * (saved first and put back) for the candidate radix orders of the
+ * shared-memory FFTs, lines per CTA of the FFT kernels and, for CHF_MIXED,
+ * the increment solve's modes per pass and columns per load batch, and keeps
+ * the fastest (each knob in turn; a candidate must be 1% faster).  reps:
+ * timed runs per candidate (0: 3).  The choice is cached for the process:
+ * later chf_create calls for the same device, grid, product grid and
+ * precision start from it.  Synchronous; needs an uploaded state. */
+int chf_autotune(chf_handle* h, int reps);
+/* The handle's launch shapes and radix orders as text (the measured step
+ * times when tuned), NUL-terminated in buf[0..len-1]. */
+int chf_tuning(const chf_handle* h, char* buf, int len);
+
 /* Per-kernel timing with CUDA events recorded around every launch on the
  * handle's stream (off by default; the reference's only instrumentation is
  * the mpi_wtime prints at poiseuilleflow.f90:216-229, 481-486). */
