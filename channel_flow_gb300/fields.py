@@ -247,10 +247,22 @@ def _cheb_values_matrix(n: int) -> np.ndarray:
     return np.cos(np.pi * np.outer(k, k) / n)  # [point, coefficient]
 
 
+def loglaw_profile(z: np.ndarray, re_tau: float, u_tau: float = 1.0) -> np.ndarray:
+    """Turbulent mean velocity at the points z: Reichardt's wall law
+    u+ = ln(1 + k y+) / k + 7.8 (1 - exp(-y+/11) - (y+/11) exp(-y+/3)),
+    k = 0.41, y+ = (1 - |z|) Re_tau (the viscous sublayer, buffer layer and
+    log layer in one smooth formula), times u_tau."""
+    yp = (1.0 - np.abs(z)) * re_tau
+    k = 0.41
+    return u_tau * (np.log1p(k * yp) / k + 7.8 * (1.0 - np.exp(-yp / 11.0) - (yp / 11.0) * np.exp(-yp / 3.0)))
+
+
 def turbulent_start_state(cfg: ChannelConfig, seed: int = 0, u_centre: float = None,
-                          frac: float = 0.1, mode_frac: float = 0.25, deg_frac: float = 0.25) -> dict:
-    """Laminar profile u_centre (1 - z^2) plus a seeded divergence-free
-    perturbation whose rms velocity is ``frac * u_centre``.
+                          frac: float = 0.1, mode_frac: float = 0.25, deg_frac: float = 0.25,
+                          loglaw: bool = False) -> dict:
+    """Laminar profile u_centre (1 - z^2) (or, with ``loglaw``, the wall-law
+    mean profile of loglaw_profile at Re_tau = re sqrt(re_p)) plus a seeded
+    divergence-free perturbation whose rms velocity is ``frac * u_centre``.
 
     The perturbation lives in the lowest ``mode_frac`` of the streamwise and
     spanwise modes; its wall-normal profiles are (1 - z^2)^2 P(z) for v and
@@ -263,6 +275,10 @@ def turbulent_start_state(cfg: ChannelConfig, seed: int = 0, u_centre: float = N
     rng = np.random.Generator(np.random.Philox(seed))
     n = cfg.nnz
     z = zpoints(n)
+    mean_vals = None
+    if loglaw:
+        mean_vals = loglaw_profile(z, cfg.re * np.sqrt(cfg.re_p), np.sqrt(cfg.re_p))
+        u_centre = float(mean_vals[n // 2])
     if u_centre is None:
         lam = cfg.re * cfg.re_p / 2.0
         if lam <= 2.0:
@@ -307,9 +323,14 @@ def turbulent_start_state(cfg: ChannelConfig, seed: int = 0, u_centre: float = N
         st[name] *= scale
     st["unp1"][:, 0, :2] = 0.0
     st["omegaznp1"][:, 0, :2] = 0.0
-    st["unp1"][0, 0, 0] = 0.5 * u_centre
-    st["unp1"][2, 0, 0] = -0.5 * u_centre
-    st["omegaznp1"][1, 0, 0] = 2.0 * u_centre
+    if mean_vals is None:
+        st["unp1"][0, 0, 0] = 0.5 * u_centre
+        st["unp1"][2, 0, 0] = -0.5 * u_centre
+        st["omegaznp1"][1, 0, 0] = 2.0 * u_centre
+    else:  # Chebyshev coefficients of the wall-law profile; omega_z = -dU/dz
+        cu = M @ mean_vals
+        st["unp1"][:, 0, 0] = cu
+        st["omegaznp1"][:, 0, 0] = -(cheb_derivative_matrix(n) @ cu)
     _set_mean(cfg, st)
     return st
 
