@@ -27,6 +27,7 @@ FftPlan make_plan(int L) {
     Ns *= r;
     m /= r;
   }
+  fft_plan_divisors(p);
   return p;
 }
 

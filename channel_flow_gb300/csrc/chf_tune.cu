@@ -65,6 +65,7 @@ FftPlan plan_from(int L, const std::vector<int>& radices) {
     ++p.nst;
     Ns *= r;
   }
+  fft_plan_divisors(p);
   return p;
 }
 

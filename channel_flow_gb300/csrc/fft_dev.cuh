@@ -24,7 +24,33 @@ struct FftPlan {
   int nst;
   int R[16];
   int Ns[16];
+  // per stage, division by L / R[st] and by Ns[st] as a multiply-high and a
+  // shift (fft_plan_divisors): q = (umulhi(n, m) + n) >> s for 0 <= n < 2^31
+  unsigned int nr_m[16], ns_m[16];
+  int nr_s[16], ns_s[16];
 };
+
+// m, s of the division by d (d >= 1) used in FftPlan: l = ceil(log2 d),
+// m = floor(2^32 (2^l - d) / d) + 1 (the round-up method of Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994)
+inline void fft_divisor(unsigned int d, unsigned int* m, int* s) {
+  int l = 0;
+  while ((1ull << l) < d) ++l;
+  *m = (unsigned int)((((1ull << 32) * ((1ull << l) - d)) / d + 1) & 0xffffffffull);
+  *s = l;
+}
+
+// fill the divisors of every stage of p (after R, Ns, nst, L are set)
+inline void fft_plan_divisors(FftPlan& p) {
+  for (int st = 0; st < p.nst; ++st) {
+    fft_divisor((unsigned int)(p.L / p.R[st]), &p.nr_m[st], &p.nr_s[st]);
+    fft_divisor((unsigned int)p.Ns[st], &p.ns_m[st], &p.ns_s[st]);
+  }
+}
+
+__device__ __forceinline__ int fft_div(int n, unsigned int m, int s) {
+  return (int)((__umulhi((unsigned int)n, m) + (unsigned int)n) >> s);
+}
 
 template <typename T>
 __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
@@ -122,19 +148,26 @@ __device__ __forceinline__ void stage_load(const cplx<T>* __restrict__ base, int
 // butterflies (b = tid + k * blockDim.x).  Reads all inputs, synchronises,
 // writes all outputs, synchronises.
 template <typename T, int SIGN, int R, int MB>
-__device__ __forceinline__ void fft_stage(cplx<T>* s, int nlines, int lstride, int L, int Ns,
+__device__ __forceinline__ void fft_stage(cplx<T>* s, int nlines, int lstride, const FftPlan& p, int st,
                                           const cplx<T>* __restrict__ tw) {
   const int nt = blockDim.x, tid = threadIdx.x;
+  const int L = p.L, Ns = p.Ns[st];
   const int nr = L / R;
   const int total = nlines * nr;
   const int twstep = L / (Ns * R);
+  const unsigned int nrm = p.nr_m[st], nsm = p.ns_m[st];
+  const int nrs = p.nr_s[st], nss = p.ns_s[st];
   cplx<T> v[MB][R];
+  int off[MB];  // output position of butterfly b: line start + block start + jm
 #pragma unroll
   for (int b = 0; b < MB; ++b) {
     int t = tid + b * nt;
+    off[b] = 0;
     if (t < total) {
-      int line = t / nr, j = t - line * nr;
-      stage_load<T, SIGN, R>(s + line * lstride, j, nr, j % Ns, twstep, tw, v[b]);
+      const int line = fft_div(t, nrm, nrs), j = t - line * nr;
+      const int q = fft_div(j, nsm, nss), jm = j - q * Ns;
+      stage_load<T, SIGN, R>(s + line * lstride, j, nr, jm, twstep, tw, v[b]);
+      off[b] = line * lstride + q * Ns * R + jm;
     }
   }
   __syncthreads();
@@ -142,9 +175,7 @@ __device__ __forceinline__ void fft_stage(cplx<T>* s, int nlines, int lstride, i
   for (int b = 0; b < MB; ++b) {
     int t = tid + b * nt;
     if (t < total) {
-      int line = t / nr, j = t - line * nr;
-      int jm = j % Ns;
-      cplx<T>* base = s + line * lstride + (j / Ns) * Ns * R + jm;
+      cplx<T>* base = s + off[b];
 #pragma unroll
       for (int r = 0; r < R; ++r) base[r * Ns] = v[b][r];
     }
@@ -163,12 +194,57 @@ __device__ void smem_fft(cplx<T>* s, int nlines, int lstride, const FftPlan& p,
   constexpr int MB3 = (2 * MB2 + 2) / 3;
   constexpr int MB5 = (2 * MB2 + 4) / 5;
   for (int st = 0; st < p.nst; ++st) {
-    const int R = p.R[st], Ns = p.Ns[st];
-    if (R == 4) fft_stage<T, SIGN, 4, MB4>(s, nlines, lstride, p.L, Ns, tw);
-    else if (R == 2) fft_stage<T, SIGN, 2, MB2>(s, nlines, lstride, p.L, Ns, tw);
-    else if (R == 3) fft_stage<T, SIGN, 3, MB3>(s, nlines, lstride, p.L, Ns, tw);
-    else fft_stage<T, SIGN, 5, MB5>(s, nlines, lstride, p.L, Ns, tw);
+    const int R = p.R[st];
+    if (R == 4) fft_stage<T, SIGN, 4, MB4>(s, nlines, lstride, p, st, tw);
+    else if (R == 2) fft_stage<T, SIGN, 2, MB2>(s, nlines, lstride, p, st, tw);
+    else if (R == 3) fft_stage<T, SIGN, 3, MB3>(s, nlines, lstride, p, st, tw);
+    else fft_stage<T, SIGN, 5, MB5>(s, nlines, lstride, p, st, tw);
   }
+}
+
+// Out-of-place Stockham stages between two shared-memory buffers: each
+// butterfly is read from one buffer, computed and written to the other at
+// once, with one barrier per stage, so a thread holds a single butterfly's R
+// values (few registers, no per-thread butterfly bound).  Line l of either
+// buffer at l * lstride.  Call after a barrier that makes the input in `a`
+// visible; returns the buffer holding the result (a or b), visible to every
+// thread of the CTA.
+template <typename T, int SIGN, int R>
+__device__ __forceinline__ void fft_stage_pp(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
+                                             int nlines, int lstride, const FftPlan& p, int st,
+                                             const cplx<T>* __restrict__ tw) {
+  const int L = p.L, Ns = p.Ns[st];
+  const int nr = L / R;
+  const int total = nlines * nr;
+  const int twstep = L / (Ns * R);
+  const unsigned int nrm = p.nr_m[st], nsm = p.ns_m[st];
+  const int nrs = p.nr_s[st], nss = p.ns_s[st];
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int line = fft_div(t, nrm, nrs), j = t - line * nr;
+    const int q = fft_div(j, nsm, nss), jm = j - q * Ns;
+    cplx<T> v[R];
+    stage_load<T, SIGN, R>(src + line * lstride, j, nr, jm, twstep, tw, v);
+    cplx<T>* base = dst + line * lstride + q * Ns * R + jm;
+#pragma unroll
+    for (int r = 0; r < R; ++r) base[r * Ns] = v[r];
+  }
+}
+
+template <typename T, int SIGN>
+__device__ cplx<T>* smem_fft_pp(cplx<T>* a, cplx<T>* b, int nlines, int lstride, const FftPlan& p,
+                                const cplx<T>* __restrict__ tw) {
+  for (int st = 0; st < p.nst; ++st) {
+    const int R = p.R[st];
+    if (R == 4) fft_stage_pp<T, SIGN, 4>(a, b, nlines, lstride, p, st, tw);
+    else if (R == 2) fft_stage_pp<T, SIGN, 2>(a, b, nlines, lstride, p, st, tw);
+    else if (R == 3) fft_stage_pp<T, SIGN, 3>(a, b, nlines, lstride, p, st, tw);
+    else fft_stage_pp<T, SIGN, 5>(a, b, nlines, lstride, p, st, tw);
+    __syncthreads();
+    cplx<T>* t = a;
+    a = b;
+    b = t;
+  }
+  return a;
 }
 
 // Host-side check of the MB2 bound for a launch.

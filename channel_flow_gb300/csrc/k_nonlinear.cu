@@ -44,7 +44,11 @@ namespace {
 // lines (600-point z lines, 576-point x rows) run with fewer lines per CTA.
 constexpr int ZC_THREADS = 512;
 constexpr int Y_THREADS = 256;
-constexpr int X_THREADS = 512;
+constexpr int X_THREADS = 256;
+// the shared-memory y / x kernels hold two buffers (out-of-place FFT stages,
+// smem_fft_pp); the rules take the most lines per CTA whose buffers fit this
+// much, so that four CTAs share an SM
+constexpr size_t kXYSmemTarget = 56 * 1024;
 
 struct SixPtr {
   const cd* p[6];
@@ -97,12 +101,13 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zc2v(SixPtr in, cd* __restrict__
 // y inverse: per (field, plane p, group of kxb streamwise modes).
 // grid (KX / kxb, MP, 6)
 // ---------------------------------------------------------------------------
-template <typename T, int MB2>
-__global__ void __launch_bounds__(Y_THREADS) k_yinv(const cplx<T>* __restrict__ wz, cplx<T>* __restrict__ wy,
-                                                    Dims d, int kxb, const __grid_constant__ FftPlan py,
-                                                    const cplx<T>* __restrict__ tw) {
+template <typename T>
+__global__ void __launch_bounds__(Y_THREADS, 4) k_yinv(const cplx<T>* __restrict__ wz, cplx<T>* __restrict__ wy,
+                                                       Dims d, int kxb, const __grid_constant__ FftPlan py,
+                                                       const cplx<T>* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* s2 = s + kxb * (d.PY + 1);
   const int ls = d.PY + 1;
   const int f = blockIdx.z, p = blockIdx.y, kx0 = blockIdx.x * kxb;
   const long modes = d.modes();
@@ -116,11 +121,11 @@ __global__ void __launch_bounds__(Y_THREADS) k_yinv(const cplx<T>* __restrict__ 
     s[l * ls + slot] = src[(size_t)ky * d.KX + kx0 + l];
   }
   __syncthreads();
-  smem_fft<T, +1, MB2>(s, kxb, ls, py, tw);
+  const cplx<T>* r = smem_fft_pp<T, +1>(s, s2, kxb, ls, py, tw);
   cplx<T>* __restrict__ dst = wy + ((size_t)f * d.MP + p) * (size_t)d.PY * d.KX;
   for (int t = threadIdx.x; t < kxb * d.PY; t += blockDim.x) {
     int l = t % kxb, yp = t / kxb;
-    dst[(size_t)yp * d.KX + kx0 + l] = s[l * ls + yp];
+    dst[(size_t)yp * d.KX + kx0 + l] = r[l * ls + yp];
   }
 }
 
@@ -129,13 +134,14 @@ __global__ void __launch_bounds__(Y_THREADS) k_yinv(const cplx<T>* __restrict__ 
 // of six fields (u, v, w, ox, oy, oz), written back in place as H1, H2, H3
 // into field slots 0, 1, 2.  XR rows per CTA, grid (ceil(MP * PY / XR))
 // ---------------------------------------------------------------------------
-template <typename T, int MB2, int XR>
-__global__ void __launch_bounds__(X_THREADS) k_xprod(cplx<T>* __restrict__ wy, Dims d, T re_p,
-                                                     const __grid_constant__ FftPlan px, const cplx<T>* __restrict__ tw) {
+template <typename T, int XR>
+__global__ void __launch_bounds__(X_THREADS, 4) k_xprod(cplx<T>* __restrict__ wy, Dims d, T re_p,
+                                                        const __grid_constant__ FftPlan px, const cplx<T>* __restrict__ tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using C = cplx<T>;
   C* s = reinterpret_cast<C*>(smem_raw);
   const int PX = d.PX, KX = d.KX, ls = PX + 1;
+  C* s2 = s + XR * 3 * ls;  // second buffer of the out-of-place FFT stages
   const long nrows = (long)d.MP * d.PY;
   const long r0 = (long)blockIdx.x * XR;
   const size_t fstride = (size_t)d.MP * d.PY * KX;
@@ -157,7 +163,8 @@ __global__ void __launch_bounds__(X_THREADS) k_xprod(cplx<T>* __restrict__ wy, D
     }
   }
   __syncthreads();
-  smem_fft<T, +1, MB2>(s, XR * 3, ls, px, tw);
+  s = smem_fft_pp<T, +1>(s, s2, XR * 3, ls, px, tw);  // s: the physical lines
+  s2 = (s == reinterpret_cast<C*>(smem_raw)) ? s + XR * 3 * ls : reinterpret_cast<C*>(smem_raw);
   // products at every physical point; write (H1 + i H2) to pair 0, (H3 + 0i) to pair 1
   for (int t = threadIdx.x; t < XR * PX; t += blockDim.x) {
     int x = t % PX, q = t / PX;
@@ -173,7 +180,7 @@ __global__ void __launch_bounds__(X_THREADS) k_xprod(cplx<T>* __restrict__ wy, D
   }
   __syncthreads();
   // forward DFT of the 2 * XR lines holding (H1 + i H2) and H3
-  smem_fft<T, -1, MB2>(s, XR * 2, ls, px, tw);
+  s = smem_fft_pp<T, -1>(s, s2, XR * 2, ls, px, tw);
   for (int t = threadIdx.x; t < XR * KX; t += blockDim.x) {
     int k = t % KX, q = t / KX;
     long r = r0 + q;
@@ -196,12 +203,13 @@ __global__ void __launch_bounds__(X_THREADS) k_xprod(cplx<T>* __restrict__ wy, D
 // slot receives padded mode +NYQ as in expand(-1), REF:751-761) and the
 // negative modes, scaled by 1/(PX PY).  grid (KX / kxb, MP, 3)
 // ---------------------------------------------------------------------------
-template <typename T, int MB2>
-__global__ void __launch_bounds__(Y_THREADS) k_yfwd(const cplx<T>* __restrict__ wy, cplx<T>* __restrict__ wz,
-                                                    Dims d, int kxb, const __grid_constant__ FftPlan py,
-                                                    const cplx<T>* __restrict__ tw, T scale) {
+template <typename T>
+__global__ void __launch_bounds__(Y_THREADS, 4) k_yfwd(const cplx<T>* __restrict__ wy, cplx<T>* __restrict__ wz,
+                                                       Dims d, int kxb, const __grid_constant__ FftPlan py,
+                                                       const cplx<T>* __restrict__ tw, T scale) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* s2 = s + kxb * (d.PY + 1);
   const int ls = d.PY + 1;
   const int f = blockIdx.z, p = blockIdx.y, kx0 = blockIdx.x * kxb;
   const long modes = d.modes();
@@ -211,12 +219,12 @@ __global__ void __launch_bounds__(Y_THREADS) k_yfwd(const cplx<T>* __restrict__ 
     s[l * ls + yp] = src[(size_t)yp * d.KX + kx0 + l];
   }
   __syncthreads();
-  smem_fft<T, -1, MB2>(s, kxb, ls, py, tw);
+  const cplx<T>* r = smem_fft_pp<T, -1>(s, s2, kxb, ls, py, tw);
   cplx<T>* __restrict__ dst = wz + ((size_t)f * d.MP + p) * modes;
   for (int t = threadIdx.x; t < kxb * d.KY; t += blockDim.x) {
     int l = t % kxb, ky = t / kxb;
     int slot = ky <= d.NYQ ? ky : d.PY - d.KY + ky;
-    cplx<T> v = s[l * ls + slot];
+    cplx<T> v = r[l * ls + slot];
     dst[(size_t)ky * d.KX + kx0 + l] = cplx<T>{v.re * scale, v.im * scale};
   }
 }
@@ -593,6 +601,12 @@ __global__ void __launch_bounds__(YW_COLS * 32, 4) k_yfwd_w(const cf* __restrict
 
 template <typename K>
 bool set_smem(Handle* h, K kernel, size_t bytes) {
+  // the shared-memory FFT kernels want several CTAs per SM: the largest
+  // shared-memory carveout (the default heuristic can pick 32 KB, one CTA)
+  if (!cuda_ok(h, cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared),
+               "cudaFuncSetAttribute"))
+    return false;
   if (bytes > 48 * 1024)
     return cuda_ok(h, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)bytes),
@@ -603,24 +617,26 @@ bool set_smem(Handle* h, K kernel, size_t bytes) {
 constexpr size_t kMaxSmem = 227 * 1024;  // dynamic shared memory per CTA
 
 // streamwise modes per CTA in the generic y kernels: the largest power of two
-// up to 16 that divides KX and whose lines fit the butterfly bound and smem
+// up to 16 that divides KX and whose two line buffers fit kXYSmemTarget (1
+// if none does); any b whose buffers fit the SM is valid (autotuner)
+template <typename T>
+size_t y_smem(const Dims& d, int b) { return 2 * sizeof(cplx<T>) * b * (d.PY + 1); }
+
 template <typename T>
 int pick_kxb(const Dims& d) {
-  for (int b = 16; b >= 1; b /= 2)
-    if (d.KX % b == 0 && fft_fits(b, d.PY, Y_THREADS, 6) &&
-        sizeof(cplx<T>) * b * (d.PY + 1) <= kMaxSmem)
-      return b;
-  return 0;
+  for (int b = 16; b > 1; b /= 2)
+    if (d.KX % b == 0 && y_smem<T>(d, b) <= kXYSmemTarget) return b;
+  return y_smem<T>(d, 1) <= kMaxSmem ? 1 : 0;
 }
 
 template <typename T>
-size_t xprod_smem(const Dims& d, int xr) { return sizeof(cplx<T>) * xr * 3 * (d.PX + 1); }
+size_t xprod_smem(const Dims& d, int xr) { return 2 * sizeof(cplx<T>) * xr * 3 * (d.PX + 1); }
 
 template <typename T>
 int pick_xr(const Dims& d) {
-  for (int r = 8; r >= 1; r /= 2)
-    if (fft_fits(r * 3, d.PX, X_THREADS, 5) && xprod_smem<T>(d, r) <= kMaxSmem) return r;
-  return 0;
+  for (int r = 8; r > 1; r /= 2)
+    if (xprod_smem<T>(d, r) <= kXYSmemTarget) return r;
+  return xprod_smem<T>(d, 1) <= kMaxSmem ? 1 : 0;
 }
 
 size_t zc2v_smem(const Dims& d, int zl) { return sizeof(cd) * zl * 2 * d.MZ; }
@@ -648,12 +664,12 @@ template <typename T, int XR>
 int run_xprod(Handle* h, cplx<T>* wy, const cplx<T>* tw_px) {
   const Dims d = fft_view(h->d);
   const size_t smem = xprod_smem<T>(d, XR);
-  if (!set_smem(h, k_xprod<T, 5, XR>, smem)) return CHF_E_CUDA;
+  if (!set_smem(h, k_xprod<T, XR>, smem)) return CHF_E_CUDA;
   const long nrows = (long)d.MP * d.PY;
   dim3 grid((unsigned)((nrows + XR - 1) / XR));
   cudaEvent_t ev;
   prof_begin(h, K_XPROD, &ev);
-  k_xprod<T, 5, XR><<<grid, X_THREADS, smem, h->stream>>>(wy, d, (T)h->cfg.re_p, h->px, tw_px);
+  k_xprod<T, XR><<<grid, X_THREADS, smem, h->stream>>>(wy, d, (T)h->cfg.re_p, h->px, tw_px);
   prof_end(h, K_XPROD, ev);
   return cuda_ok(h, cudaGetLastError(), "k_xprod") ? CHF_OK : CHF_E_CUDA;
 }
@@ -701,13 +717,13 @@ std::vector<int> shape_candidates(const Handle* h, int knob) {
   std::vector<int> out;
   if (knob == 0) {  // kxb
     for (int b = 16; b >= 1; b /= 2) {
-      const size_t bytes = (f32 ? sizeof(cf) : sizeof(cd)) * b * (d.PY + 1);
-      if (d.KX % b == 0 && fft_fits(b, d.PY, Y_THREADS, 6) && bytes <= kMaxSmem) out.push_back(b);
+      const size_t bytes = f32 ? y_smem<float>(d, b) : y_smem<double>(d, b);
+      if (d.KX % b == 0 && bytes <= kMaxSmem) out.push_back(b);
     }
   } else if (knob == 1) {  // xr
     for (int r = 8; r >= 1; r /= 2) {
       const size_t bytes = f32 ? xprod_smem<float>(d, r) : xprod_smem<double>(d, r);
-      if (fft_fits(r * 3, d.PX, X_THREADS, 5) && bytes <= kMaxSmem) out.push_back(r);
+      if (bytes <= kMaxSmem) out.push_back(r);
     }
   } else if (knob == 2) {  // zl_c2v
     for (int l = 8; l >= 2; l /= 2)
@@ -777,12 +793,12 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     return CHF_E_INVALID;
   }
   {
-    size_t smem = sizeof(cplx<T>) * kxb * (d.PY + 1);
-    if (!set_smem(h, k_yinv<T, 6>, smem)) return CHF_E_CUDA;
+    const size_t smem = y_smem<T>(d, kxb);
+    if (!set_smem(h, k_yinv<T>, smem)) return CHF_E_CUDA;
     dim3 grid(d.KX / kxb, d.MP, 6);
     cudaEvent_t ev;
     prof_begin(h, K_YINV, &ev);
-    k_yinv<T, 6><<<grid, Y_THREADS, smem, st>>>(wz, wy, d, kxb, h->py, tw_py);
+    k_yinv<T><<<grid, Y_THREADS, smem, st>>>(wz, wy, d, kxb, h->py, tw_py);
     prof_end(h, K_YINV, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_yinv")) return CHF_E_CUDA;
   }
@@ -794,13 +810,13 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     if (rc != CHF_OK) return rc;
   }
   {
-    size_t smem = sizeof(cplx<T>) * kxb * (d.PY + 1);
-    if (!set_smem(h, k_yfwd<T, 6>, smem)) return CHF_E_CUDA;
+    const size_t smem = y_smem<T>(d, kxb);
+    if (!set_smem(h, k_yfwd<T>, smem)) return CHF_E_CUDA;
     dim3 grid(d.KX / kxb, d.MP, 3);
     T scale = (T)(1.0 / ((double)d.PX * (double)d.PY));
     cudaEvent_t ev;
     prof_begin(h, K_YFWD, &ev);
-    k_yfwd<T, 6><<<grid, Y_THREADS, smem, st>>>(wy, wz, d, kxb, h->py, tw_py, scale);
+    k_yfwd<T><<<grid, Y_THREADS, smem, st>>>(wy, wz, d, kxb, h->py, tw_py, scale);
     prof_end(h, K_YFWD, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_yfwd")) return CHF_E_CUDA;
   }
