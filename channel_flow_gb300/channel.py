@@ -28,7 +28,7 @@ EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
            "chf_batch_handle", "chf_batch_step", "chf_batch_synchronize",
            "chf_set_flow_rate", "chf_get_flow_rate", "chf_statistics", "chf_pressure",
            "chf_transform", "chf_cfl", "chf_physical_velocity", "chf_write_velocity",
-           "chf_autotune", "chf_tuning")
+           "chf_autotune", "chf_tuning", "chf_test_wait_timeout")
 
 
 class ChannelError(RuntimeError):
@@ -103,6 +103,7 @@ def load_library(path: str = None):
     L.chf_pressure.argtypes = [vp, dp]
     L.chf_transform.argtypes = [vp, ctypes.c_int, dp]
     L.chf_autotune.argtypes = [vp, ctypes.c_int]
+    L.chf_test_wait_timeout.argtypes = [vp, ctypes.c_int]
     L.chf_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
     L.chf_cfl.argtypes = [vp, dp, dp, dp]
     L.chf_physical_velocity.argtypes = [vp, dp, dp]
@@ -255,6 +256,12 @@ class Channel:
         out = np.zeros(self.shape)
         self._check(self.L.chf_pressure(self.h, _dptr(out)))
         return out
+
+    def test_wait_timeout(self, wait_us: int):
+        """Arm the test of the tensor-core pipeline's bounded waits: the next
+        GEMM launch leaves its first stage empty, its waits run out after
+        wait_us and the next synchronize reports CHF_E_CUDA."""
+        self._check(self.L.chf_test_wait_timeout(self.h, int(wait_us)))
 
     def autotune(self, reps: int = 3) -> str:
         """Pick launch shapes and FFT radix orders by timing steps of the

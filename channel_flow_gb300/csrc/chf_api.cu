@@ -547,8 +547,27 @@ static int check_status(chf_handle* h) {
     return CHF_E_CUDA;
   if (st != 0) {
     h->err = "tensor-core pipeline wait timed out (code " + std::to_string(st) + ")";
+    // reported once: the word is cleared so the handle stays usable (the
+    // state of the failed step is not; upload or read a restart file)
+    cudaMemsetAsync(h->dev_status, 0, sizeof(int), h->stream);
+    cudaStreamSynchronize(h->stream);
     return CHF_E_CUDA;
   }
+  return CHF_OK;
+}
+
+int chf_test_wait_timeout(chf_handle* h, int wait_us) {
+  if (!h) return CHF_E_INVALID;
+  if (!mixed_front(h)) {
+    h->err = "chf_test_wait_timeout: only the mixed precisions run the tensor-core pipeline";
+    return CHF_E_INVALID;
+  }
+  if (wait_us < 1 || wait_us > 1000000) {
+    h->err = "chf_test_wait_timeout: wait_us must be 1 .. 1000000";
+    return CHF_E_INVALID;
+  }
+  h->test_skip = 1;
+  h->test_wait_ns = 1000L * wait_us;
   return CHF_OK;
 }
 

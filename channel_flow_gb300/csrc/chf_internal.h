@@ -172,6 +172,10 @@ struct Handle {
 
   // mixed-precision path (k_mixed.cu): FP32 transforms, tcgen05 GEMMs
   int* dev_status = nullptr;  // device error word (tensor-core pipeline timeouts)
+  // chf_test_wait_timeout: the next exact-GEMM launch leaves its first stage
+  // empty and bounds its waits at test_wait_ns
+  int test_skip = 0;
+  long test_wait_ns = 0;
   FxPlan tz1{}, tz2{}, tgl{};
   uint8_t *az1 = nullptr, *az2 = nullptr, *agl = nullptr;  // constant A images
   uint8_t* bimg = nullptr;    // per-step B images

@@ -199,7 +199,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
                                                               const uint8_t* __restrict__ bimg,
                                                               const int* __restrict__ bexp,
                                                               const __grid_constant__ Ptr8<OutT> outs,
-                                                              size_t ldc, int nfields, int* status) {
+                                                              size_t ldc, int nfields, int* status,
+                                                              long wait_ns, int skip_first) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[WS_STAGES], empty[WS_STAGES], tfull[2], tempty[2], drain[WS_MMA_WARPS], abar;
   __shared__ uint32_t tmem_base;
@@ -252,10 +253,14 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
         const uint8_t* btile = bimg + (size_t)f * plan.b_field_bytes() + (size_t)nt * plan.b_tile_bytes;
         for (int ch = 0; ch < plan.nchunks; ++ch, ++g) {
           const uint32_t s = g % WS_STAGES, ph = (g / WS_STAGES) & 1u;
-          if (!mbar_wait(smem_u32(&empty[s]), ph ^ 1u)) {
+          if (!mbar_wait(smem_u32(&empty[s]), ph ^ 1u, wait_ns)) {
             *fail = 1;
             break;
           }
+          // test of the bounded waits (chf_test_wait_timeout): the first
+          // chunk's copies are not issued, so its stage never fills and the
+          // waits on it run out
+          if (skip_first && g == 0) continue;
           const int kc = plan.kc[ch];
           const uint32_t apb = 128u * kc * 2u, bpb = (uint32_t)FX_NT * kc * 2u;
           uint8_t* st = ring + (size_t)s * stage_bytes;
@@ -272,8 +277,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
       // issued into each stage (and the resident A tile) has arrived (a no-op
       // after a normal run, where the MMA issuer consumed everything)
       for (uint32_t k = g > (uint32_t)WS_STAGES ? g - WS_STAGES : 0; k < g; ++k)
-        if (!mbar_wait(smem_u32(&full[k % WS_STAGES]), (k / WS_STAGES) & 1u)) *fail = 6;
-      if (resident && !mbar_wait(smem_u32(&abar), 0)) *fail = 7;
+        if (!mbar_wait(smem_u32(&full[k % WS_STAGES]), (k / WS_STAGES) & 1u, wait_ns)) *fail = 6;
+      if (resident && !mbar_wait(smem_u32(&abar), 0, wait_ns)) *fail = 7;
     }
   } else if (warp < WS_EPI0) {
     // ---------------- MMA issuers ----------------
@@ -286,12 +291,12 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
       // One K16 slice advances the start address by 2 core matrices: 256 / 128
       // in the descriptor's 16-byte units.
       const uint32_t lbo_a = 16u * 128u, lbo_b = 8u * 128u, sbo = 128u;
-      bool ok = !resident || mbar_wait(smem_u32(&abar), 0);
+      bool ok = !resident || mbar_wait(smem_u32(&abar), 0, wait_ns);
       if (!ok) *fail = 3;
       uint32_t g = 0, tc = 0;
       for (long j = j0; ok && j < njobs && !*fail; j += jstep, ++tc) {
         const uint32_t b = tc & 1u, tph = (tc >> 1) & 1u;
-        if (!mbar_wait(smem_u32(&tempty[b]), tph ^ 1u)) {
+        if (!mbar_wait(smem_u32(&tempty[b]), tph ^ 1u, wait_ns)) {
           *fail = 2;
           break;
         }
@@ -299,7 +304,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
         const uint32_t tacc = tmem + b * SET_COLS;
         for (int ch = 0; ch < plan.nchunks; ++ch, ++g) {
           const uint32_t s = g % WS_STAGES, ph = (g / WS_STAGES) & 1u;
-          if (!mbar_wait(smem_u32(&full[s]), ph)) {
+          if (!mbar_wait(smem_u32(&full[s]), ph, wait_ns)) {
             ok = false;
             break;
           }
@@ -346,7 +351,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
       }
       // every MMA this thread issued has completed once "drain" arrives
       mma_commit(smem_u32(&drain[mw]));
-      if (!mbar_wait(smem_u32(&drain[mw]), 0)) *fail = 4;
+      if (!mbar_wait(smem_u32(&drain[mw]), 0, wait_ns)) *fail = 4;
     }
   } else {
     // ---------------- epilogue ----------------
@@ -361,7 +366,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
       // decisions stay warp-uniform: tcgen05.ld needs the whole warp
       if (__shfl_sync(0xffffffffu, *fail, 0)) break;
       const uint32_t b = tc & 1u, tph = (tc >> 1) & 1u;
-      if (!__all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull[b]), tph))) {
+      if (!__all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull[b]), tph, wait_ns))) {
         if (lane == 0) *fail = 5;
         break;
       }
@@ -670,7 +675,12 @@ int launch_tc_gemm_fx(Handle* h, const FxPlan& p, const uint8_t* aimg, const int
   const int grid = (int)(std::min<long>(items, (long)std::max(h->num_sms, p.mtiles)) / p.mtiles * p.mtiles);
   cudaEvent_t ev;
   prof_begin(h, kid, &ev);
-  kern<<<grid, WS_THREADS, smem, h->stream>>>(p, aimg, aexp, bimg, bexp, outs, ldc, nfields, h->dev_status);
+  // the bounded-wait test (chf_test_wait_timeout) applies to one launch
+  const long wait_ns = h->test_skip ? h->test_wait_ns : tc::WAIT_NS;
+  const int skip = h->test_skip;
+  h->test_skip = 0;
+  kern<<<grid, WS_THREADS, smem, h->stream>>>(p, aimg, aexp, bimg, bexp, outs, ldc, nfields, h->dev_status,
+                                              wait_ns, skip);
   prof_end(h, kid, ev);
   return cuda_ok(h, cudaGetLastError(), "k_tc_gemm_fx") ? CHF_OK : CHF_E_CUDA;
 }

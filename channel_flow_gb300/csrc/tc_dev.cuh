@@ -24,7 +24,9 @@ __device__ __forceinline__ uint64_t gtimer() {
   return t;
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+// wait for the phase with parity `phase` to complete, at most limit_ns of
+// wall time (false on timeout)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, long limit_ns = WAIT_NS) {
   const uint64_t t0 = gtimer();
   for (;;) {
     uint32_t ok;
@@ -35,7 +37,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
         : "r"(bar), "r"(phase)
         : "memory");
     if (ok) return true;
-    if ((long)(gtimer() - t0) > WAIT_NS) return false;
+    if ((long)(gtimer() - t0) > limit_ns) return false;
   }
 }
 

@@ -165,6 +165,19 @@ int chf_device_field(chf_handle* h, int which, void** dptr);
  * library's own stream.  The caller keeps the stream alive while h uses it. */
 int chf_set_stream(chf_handle* h, void* stream);
 
+/* Test of failure detection, no counterpart in the reference.  The
+ * tensor-core GEMMs of the mixed precisions bound every wait of their
+ * pipeline (1 s of wall time); on a timeout each role records a code in the
+ * handle's device status word, waits (bounded) for its copies and MMAs in
+ * flight, frees the tensor memory and returns, and the next
+ * chf_synchronize / chf_diagnostics / chf_step_host reports CHF_E_CUDA with
+ * the code in chf_last_error, once (the word is cleared; the state of that
+ * step is not valid).  This call arms one occurrence: the next GEMM launch
+ * on h issues no copies for its first stage, so the waits on that stage run
+ * out after wait_us microseconds (1 .. 1000000).  No fault, trap or unbounded
+ * wait is involved.  CHF_E_INVALID for CHF_FP64 handles. */
+int chf_test_wait_timeout(chf_handle* h, int wait_us);
+
 /* Autotuner, the counterpart of the reference's FFTW_MEASURE planning
  * (poiseuilleflow.f90:100-112): times whole steps of the handle's state
  * (saved first and put back) for the candidate radix orders of the
