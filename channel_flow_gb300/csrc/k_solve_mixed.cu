@@ -258,7 +258,7 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
 }
 
 template <int MCH, int CB>
-__global__ void __launch_bounds__(MV_THREADS, 3) k_inc_solve(cd* __restrict__ v, cd* __restrict__ g,
+__global__ void __launch_bounds__(MV_THREADS, MCH == 2 ? 4 : 3) k_inc_solve(cd* __restrict__ v, cd* __restrict__ g,
                                                              const cd* __restrict__ rv, const cd* __restrict__ uh,
                                                              const cd* __restrict__ rg, const cd* __restrict__ wh,
                                                              const float2* __restrict__ incm,
