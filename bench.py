@@ -39,6 +39,9 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--precision", choices=["fp64", "mixed", "mixed_fp64solve"], default="mixed")
     p.add_argument("--config", default="c3_retau180_128")
+    p.add_argument("--grid", default=None,
+                   help="nnx,nny,nnz in place of the config's grid (same box, Reynolds number and time "
+                        "step): smaller cases of a workload's kernels, for profiling")
     p.add_argument("--zpad", default="auto",
                    help="product-grid intervals in z: 0 = 2*nnz (reference), 'auto' = smallest "
                         "exact 2,3,5-smooth grid (2*zpad > 3*nnz)")
@@ -85,6 +88,15 @@ DTYPES = {
     "mixed_fp64solve": "f64 state; f32 x/y FFTs and products; exact fixed-point tcgen05 z transforms (bf16 "
                        "digits, exact f32 level sums); f64 curl; f64 tau solve for every mode",
 }
+
+
+def workload_config(args):
+    from channel_flow_gb300 import config
+    cfg = config.CONFIGS[args.config]
+    if args.grid:
+        nx, ny, nz = (int(v) for v in args.grid.split(","))
+        cfg = config.ChannelConfig(nx, ny, nz, cfg.aphi, cfg.beta, cfg.dt, cfg.re, cfg.re_p)
+    return cfg
 
 
 def start_state(cfg, seed):
@@ -258,7 +270,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     from channel_flow_gb300 import config
-    cfg = config.CONFIGS[args.config]
+    cfg = workload_config(args)
     rate, threads, steps, el = cpu_reference_rate(cfg, 0, warmup=args.warmup, steps=args.steps)
     sample = (f"{steps} full time steps of the {cfg.nnx}x{cfg.nnz + 1}x{cfg.nny} workload "
               f"(CPU restatement of the reference algorithm, 12+6 padded transforms, explicit inverses)")
@@ -298,7 +310,7 @@ def main():
         cbuild.build()
     if dist:
         dist.barrier()
-    cfg = config.CONFIGS[args.config]
+    cfg = workload_config(args)
     args.zpad = resolve_zpad(args.zpad, cfg.nnz)
     if args.accuracy_steps is None:
         args.accuracy_steps = 200 if args.config.startswith("c4") else 1000

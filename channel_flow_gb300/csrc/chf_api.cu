@@ -31,6 +31,31 @@ FftPlan make_plan(int L) {
   return p;
 }
 
+// Plans of the two-buffer FFT stages (the x / y transforms, smem_fft_pp):
+// the largest radices first (16 when allowed, then 8, 9, 4, 3, 5, 2), so
+// that a line passes through shared memory as few times as possible; maxr
+// bounds the radix (FP64 lines hold 8 complex values per thread at most)
+FftPlan make_plan_pp(int L, int maxr) {
+  FftPlan p{};
+  p.L = L;
+  int m = L, Ns = 1;
+  while (m > 1) {
+    int r = 2;
+    for (int c : {16, 8, 9, 4, 3, 5, 2})
+      if (c <= maxr && m % c == 0) {
+        r = c;
+        break;
+      }
+    p.R[p.nst] = r;
+    p.Ns[p.nst] = Ns;
+    ++p.nst;
+    Ns *= r;
+    m /= r;
+  }
+  fft_plan_divisors(p);
+  return p;
+}
+
 static bool factors_235(int n) {
   if (n <= 0) return false;
   for (int p : {2, 3, 5})
@@ -287,8 +312,11 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
     return fail(CHF_E_NOMEM);
   h->scratch_bytes = 4096;
   if (!cuda_ok(h, cudaMalloc(&h->scratch, h->scratch_bytes), "scratch alloc")) return fail(CHF_E_NOMEM);
-  h->py = make_plan(d.PY);
-  h->px = make_plan(d.PX);
+  // radix 16 is built for FP32 lines only
+  h->py64 = make_plan_pp(d.PY, 8);
+  h->px64 = make_plan_pp(d.PX, 8);
+  h->py = cfg->precision == CHF_FP64 ? h->py64 : make_plan_pp(d.PY, 16);
+  h->px = cfg->precision == CHF_FP64 ? h->px64 : make_plan_pp(d.PX, 16);
   h->pz2 = make_plan(2 * d.N);
   h->pzm = make_plan(2 * d.MZ);
   struct {

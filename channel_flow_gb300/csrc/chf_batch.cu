@@ -209,6 +209,8 @@ int build_stack(chf_batch* b, Stack& S) {
   // FFT plans and twiddles of the members' lengths
   h->py = c0.py;
   h->px = c0.px;
+  h->py64 = c0.py64;
+  h->px64 = c0.px64;
   h->pz2 = c0.pz2;
   h->pzm = c0.pzm;
   if (!dup(b, &h->tw_py, c0.tw_py, c0.d.PY, "class twiddles") || !dup(b, &h->tw_px, c0.tw_px, c0.d.PX, "class twiddles") ||

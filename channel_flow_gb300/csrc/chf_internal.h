@@ -154,6 +154,10 @@ struct Handle {
 
   // FFT plans and twiddles
   FftPlan py, px, pz2, pzm;   // PY, PX, 2N, 2MZ
+  // PY, PX for FP64 lines when the nonlinear front is FP32 (the Lamb vector of
+  // chf_pressure/chf_lamb on a mixed handle): the radix-8 rule and the launch
+  // rules, never the FP32 tuning, so those results equal an FP64 handle's
+  FftPlan py64, px64;
   cd *tw_py = nullptr, *tw_px = nullptr, *tw_z2 = nullptr, *tw_zm = nullptr;
   cf *twf_py = nullptr, *twf_px = nullptr;
 
@@ -301,8 +305,10 @@ int launch_solve_mean(Handle* h, cudaStream_t st);  // the (0,0) mode alone, on 
 int launch_solve_mixed(Handle* h);  // k_solve_mixed.cu
 int launch_diagnostics(Handle* h, chf_diag* out);
 
-// FFT plan helper (host)
+// FFT plan helpers (host): radices 4, 2, 3, 5 for the in-place stages;
+// the largest radices up to maxr for the two-buffer stages
 FftPlan make_plan(int L);
+FftPlan make_plan_pp(int L, int maxr);
 // autotuner (chf_tune.cu): launch shapes the rules accept for a knob (0 kxb,
 // 1 xr, 2 zl_c2v, 3 zl_curl; k_nonlinear.cu), and the process's cached
 // choice for a new handle's key

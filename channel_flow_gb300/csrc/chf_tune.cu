@@ -7,7 +7,9 @@
 // the same for this library's choices:
 //   * the radix order of every shared-memory FFT plan (spanwise and
 //     streamwise lengths, the 2 nnz and 2 zpad wall-normal lengths): the
-//     rule's order (4s, then 2, 3, 5), its reverse, and the odd radices first;
+//     rule's order, its reverse and the odd radices first, where the rule is
+//     the largest radices (16, 8, 9, ...) for the x / y lines and 4s, then
+//     2, 3, 5 for the wall-normal ones; the x / y lines also try radices up to 4;
 //   * the lines per CTA of the shared-memory FFT kernels (y: streamwise
 //     modes per CTA; x: rows per CTA; FP64 z: modes per CTA), every shape the
 //     launch rules accept;
@@ -75,9 +77,9 @@ std::string radix_string(const FftPlan& p) {
   return s.empty() ? "1" : s;
 }
 
-// radix orders of one length: the rule's (make_plan), reversed, odd first
-std::vector<FftPlan> plan_candidates(int L) {
-  const FftPlan rule = make_plan(L);
+// radix orders of one length: the rule's, reversed, odd radices first
+std::vector<FftPlan> plan_candidates(const FftPlan& rule) {
+  const int L = rule.L;
   std::vector<int> r(rule.R, rule.R + rule.nst);
   std::vector<std::vector<int>> orders{r, std::vector<int>(r.rbegin(), r.rend())};
   std::vector<int> odd;
@@ -203,19 +205,26 @@ int chf_autotune(chf_handle* h, int reps) {
   };
   const bool reg_xy = mixed_front(h) && xy_register_path(d);
   if (!reg_xy) {
-    try_knob([&](const FftPlan& p) { h->py = p; }, with_current(h->py, plan_candidates(d.PY)));
-    try_knob([&](const FftPlan& p) { h->px = p; }, with_current(h->px, plan_candidates(d.PX)));
+    // two-buffer stages: the large-radix rule's orders, and radices up to 4
+    const int maxr = h->cfg.precision == CHF_FP64 ? 8 : 16;
+    auto xy_cands = [&](int L) {
+      auto c = plan_candidates(make_plan_pp(L, maxr));
+      for (auto& q : plan_candidates(make_plan(L))) c.push_back(q);
+      return c;
+    };
+    try_knob([&](const FftPlan& p) { h->py = p; }, with_current(h->py, xy_cands(d.PY)));
+    try_knob([&](const FftPlan& p) { h->px = p; }, with_current(h->px, xy_cands(d.PX)));
     try_knob([&](int v) { h->tune.kxb = v; }, with_current(h->tune.kxb, shape_candidates(h, 0)));
     try_knob([&](int v) { h->tune.xr = v; }, with_current(h->tune.xr, shape_candidates(h, 1)));
   }
   if (!mixed_front(h)) {
-    try_knob([&](const FftPlan& p) { h->pzm = p; }, with_current(h->pzm, plan_candidates(2 * d.MZ)));
+    try_knob([&](const FftPlan& p) { h->pzm = p; }, with_current(h->pzm, plan_candidates(make_plan(2 * d.MZ))));
     try_knob([&](int v) { h->tune.zl_c2v = v; }, with_current(h->tune.zl_c2v, shape_candidates(h, 2)));
     try_knob([&](int v) { h->tune.zl_curl = v; }, with_current(h->tune.zl_curl, shape_candidates(h, 3)));
   }
   // the 2 nnz DFTs of the FP64 solve (every mode in CHF_FP64 and
   // CHF_MIXED_F64SOLVE, the (0,0) mode in CHF_MIXED)
-  try_knob([&](const FftPlan& p) { h->pz2 = p; }, with_current(h->pz2, plan_candidates(2 * d.N)));
+  try_knob([&](const FftPlan& p) { h->pz2 = p; }, with_current(h->pz2, plan_candidates(make_plan(2 * d.N))));
   if (increment_solve(h)) {
     std::vector<std::pair<int, int>> maps{{h->tune.inc_mch, h->tune.inc_cb}};
     for (int mch : {4, 2})

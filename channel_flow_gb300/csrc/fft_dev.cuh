@@ -123,6 +123,92 @@ __device__ __forceinline__ void bfly5(cplx<T>* v) {
   v[3] = csub(r2, i2);
 }
 
+// Larger radices for the two-buffer stages (smem_fft_pp): fewer passes
+// through shared memory.  Each is a two-level factorisation in registers,
+// X[k1 + R1 k2] = sum_p W_R^(p k1) W_R2^(p k2) sum_m x[R2 m + p] W_R1^(m k1)
+// (n = R2 m + p, R = R1 R2), with the exact roots cos / sin(2 pi q / R).
+template <typename T, int SIGN>
+__device__ __forceinline__ cplx<T> rot(cplx<T> a, T c, T s) {  // a * (c + SIGN i s)
+  return cplx<T>{a.re * c - (T)SIGN * a.im * s, a.im * c + (T)SIGN * a.re * s};
+}
+
+// radix 8 = 4 x 2
+template <typename T, int SIGN>
+__device__ __forceinline__ void bfly8(cplx<T>* v) {
+  const T h = (T)0.70710678118654752440;  // cos(pi / 4) = sin(pi / 4)
+  cplx<T> e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+  bfly4<T, SIGN>(e);
+  bfly4<T, SIGN>(o);
+  o[1] = rot<T, SIGN>(o[1], h, h);
+  o[2] = cplx<T>{(T)(-SIGN) * o[2].im, (T)(SIGN)*o[2].re};  // * SIGN i
+  o[3] = rot<T, SIGN>(o[3], -h, h);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = cadd(e[k], o[k]);
+    v[k + 4] = csub(e[k], o[k]);
+  }
+}
+
+// radix 9 = 3 x 3
+template <typename T, int SIGN>
+__device__ __forceinline__ void bfly9(cplx<T>* v) {
+  const T c1 = (T)0.76604444311897803520, s1 = (T)0.64278760968653932632;  // 2 pi / 9
+  const T c2 = (T)0.17364817766693034885, s2 = (T)0.98480775301220805936;  // 4 pi / 9
+  const T c4 = (T)-0.93969262078590838405, s4 = (T)0.34202014332566873304;  // 8 pi / 9
+  cplx<T> a[3][3];
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    a[p][0] = v[p];
+    a[p][1] = v[3 + p];
+    a[p][2] = v[6 + p];
+    bfly3<T, SIGN>(a[p]);
+  }
+  a[1][1] = rot<T, SIGN>(a[1][1], c1, s1);
+  a[1][2] = rot<T, SIGN>(a[1][2], c2, s2);
+  a[2][1] = rot<T, SIGN>(a[2][1], c2, s2);
+  a[2][2] = rot<T, SIGN>(a[2][2], c4, s4);
+#pragma unroll
+  for (int k1 = 0; k1 < 3; ++k1) {
+    cplx<T> b[3] = {a[0][k1], a[1][k1], a[2][k1]};
+    bfly3<T, SIGN>(b);
+    v[k1] = b[0];
+    v[k1 + 3] = b[1];
+    v[k1 + 6] = b[2];
+  }
+}
+
+// radix 16 = 4 x 4
+template <typename T, int SIGN>
+__device__ __forceinline__ void bfly16(cplx<T>* v) {
+  const T ca = (T)0.92387953251128675613, sa = (T)0.38268343236508977173;  // pi / 8
+  const T h = (T)0.70710678118654752440;                                    // pi / 4
+  cplx<T> a[4][4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) a[p][m] = v[4 * m + p];
+    bfly4<T, SIGN>(a[p]);
+  }
+  // W16^(p k1): p = 1: k1 = 1, 2, 3 -> pi/8, pi/4, 3pi/8; p = 2: pi/4, pi/2, 3pi/4;
+  // p = 3: 3pi/8, 3pi/4, 9pi/8
+  a[1][1] = rot<T, SIGN>(a[1][1], ca, sa);
+  a[1][2] = rot<T, SIGN>(a[1][2], h, h);
+  a[1][3] = rot<T, SIGN>(a[1][3], sa, ca);
+  a[2][1] = rot<T, SIGN>(a[2][1], h, h);
+  a[2][2] = cplx<T>{(T)(-SIGN) * a[2][2].im, (T)(SIGN)*a[2][2].re};
+  a[2][3] = rot<T, SIGN>(a[2][3], -h, h);
+  a[3][1] = rot<T, SIGN>(a[3][1], sa, ca);
+  a[3][2] = rot<T, SIGN>(a[3][2], -h, h);
+  a[3][3] = rot<T, SIGN>(a[3][3], -ca, -sa);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    cplx<T> b[4] = {a[0][k1], a[1][k1], a[2][k1], a[3][k1]};
+    bfly4<T, SIGN>(b);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = b[k2];
+  }
+}
+
 // One stage helper: load R inputs of butterfly (line, j), twiddle, butterfly.
 template <typename T, int SIGN, int R>
 __device__ __forceinline__ void stage_load(const cplx<T>* __restrict__ base, int j, int nr, int jm,
@@ -142,6 +228,9 @@ __device__ __forceinline__ void stage_load(const cplx<T>* __restrict__ base, int
   if (R == 3) bfly3<T, SIGN>(v);
   if (R == 4) bfly4<T, SIGN>(v);
   if (R == 5) bfly5<T, SIGN>(v);
+  if (R == 8) bfly8<T, SIGN>(v);
+  if (R == 9) bfly9<T, SIGN>(v);
+  if (R == 16) bfly16<T, SIGN>(v);
 }
 
 // One Stockham stage with compile-time radix R; each thread owns up to MB
@@ -236,6 +325,11 @@ __device__ cplx<T>* smem_fft_pp(cplx<T>* a, cplx<T>* b, int nlines, int lstride,
   for (int st = 0; st < p.nst; ++st) {
     const int R = p.R[st];
     if (R == 4) fft_stage_pp<T, SIGN, 4>(a, b, nlines, lstride, p, st, tw);
+    else if (R == 8) fft_stage_pp<T, SIGN, 8>(a, b, nlines, lstride, p, st, tw);
+    else if (R == 16) {  // FP32 lines only (16 FP64 values would not fit the registers)
+      if constexpr (sizeof(T) == 4) fft_stage_pp<T, SIGN, 16>(a, b, nlines, lstride, p, st, tw);
+    }
+    else if (R == 9) fft_stage_pp<T, SIGN, 9>(a, b, nlines, lstride, p, st, tw);
     else if (R == 2) fft_stage_pp<T, SIGN, 2>(a, b, nlines, lstride, p, st, tw);
     else if (R == 3) fft_stage_pp<T, SIGN, 3>(a, b, nlines, lstride, p, st, tw);
     else fft_stage_pp<T, SIGN, 5>(a, b, nlines, lstride, p, st, tw);

@@ -661,7 +661,7 @@ int pick_zl_curl(const Dims& d) {
 }
 
 template <typename T, int XR>
-int run_xprod(Handle* h, cplx<T>* wy, const cplx<T>* tw_px) {
+int run_xprod(Handle* h, cplx<T>* wy, const FftPlan& px, const cplx<T>* tw_px) {
   const Dims d = fft_view(h->d);
   const size_t smem = xprod_smem<T>(d, XR);
   if (!set_smem(h, k_xprod<T, XR>, smem)) return CHF_E_CUDA;
@@ -669,7 +669,7 @@ int run_xprod(Handle* h, cplx<T>* wy, const cplx<T>* tw_px) {
   dim3 grid((unsigned)((nrows + XR - 1) / XR));
   cudaEvent_t ev;
   prof_begin(h, K_XPROD, &ev);
-  k_xprod<T, XR><<<grid, X_THREADS, smem, h->stream>>>(wy, d, (T)h->cfg.re_p, h->px, tw_px);
+  k_xprod<T, XR><<<grid, X_THREADS, smem, h->stream>>>(wy, d, (T)h->cfg.re_p, px, tw_px);
   prof_end(h, K_XPROD, ev);
   return cuda_ok(h, cudaGetLastError(), "k_xprod") ? CHF_OK : CHF_E_CUDA;
 }
@@ -786,8 +786,20 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     const int rc = launch_yinv_fields(h, wzf, wyf, twy, 0, 6);
     return rc == CHF_OK ? launch_xprod_yfwd(h, wzf, wyf, twy, twx) : rc;
   }
-  const int kxb = h->tune.kxb ? h->tune.kxb : pick_kxb<T>(d);
-  const int xr = h->tune.xr ? h->tune.xr : pick_xr<T>(d);
+  // the handle's own line precision takes the tuned plans and shapes; FP64
+  // lines of a mixed handle take the FP64 rules
+  const bool own = (sizeof(T) == 8) == !mixed_front(h);
+  const FftPlan& py = own ? h->py : h->py64;
+  const FftPlan& px = own ? h->px : h->px64;
+  if (sizeof(T) == 8)
+    for (const FftPlan* p : {&py, &px})
+      for (int s = 0; s < p->nst; ++s)
+        if (p->R[s] > 9) {
+          h->err = "x/y transforms: radix above 9 in an FP64 plan";
+          return CHF_E_INVALID;
+        }
+  const int kxb = own && h->tune.kxb ? h->tune.kxb : pick_kxb<T>(d);
+  const int xr = own && h->tune.xr ? h->tune.xr : pick_xr<T>(d);
   if (!kxb || !xr) {
     h->err = "x/y transforms: FFT length too large for the launch shapes";
     return CHF_E_INVALID;
@@ -798,15 +810,15 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     dim3 grid(d.KX / kxb, d.MP, 6);
     cudaEvent_t ev;
     prof_begin(h, K_YINV, &ev);
-    k_yinv<T><<<grid, Y_THREADS, smem, st>>>(wz, wy, d, kxb, h->py, tw_py);
+    k_yinv<T><<<grid, Y_THREADS, smem, st>>>(wz, wy, d, kxb, py, tw_py);
     prof_end(h, K_YINV, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_yinv")) return CHF_E_CUDA;
   }
   {
-    int rc = xr == 8 ? run_xprod<T, 8>(h, wy, tw_px)
-           : xr == 4 ? run_xprod<T, 4>(h, wy, tw_px)
-           : xr == 2 ? run_xprod<T, 2>(h, wy, tw_px)
-                     : run_xprod<T, 1>(h, wy, tw_px);
+    int rc = xr == 8 ? run_xprod<T, 8>(h, wy, px, tw_px)
+           : xr == 4 ? run_xprod<T, 4>(h, wy, px, tw_px)
+           : xr == 2 ? run_xprod<T, 2>(h, wy, px, tw_px)
+                     : run_xprod<T, 1>(h, wy, px, tw_px);
     if (rc != CHF_OK) return rc;
   }
   {
@@ -816,7 +828,7 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     T scale = (T)(1.0 / ((double)d.PX * (double)d.PY));
     cudaEvent_t ev;
     prof_begin(h, K_YFWD, &ev);
-    k_yfwd<T><<<grid, Y_THREADS, smem, st>>>(wy, wz, d, kxb, h->py, tw_py, scale);
+    k_yfwd<T><<<grid, Y_THREADS, smem, st>>>(wy, wz, d, kxb, py, tw_py, scale);
     prof_end(h, K_YFWD, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_yfwd")) return CHF_E_CUDA;
   }
