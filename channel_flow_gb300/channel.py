@@ -28,7 +28,7 @@ EXPORTS = ("chf_create", "chf_destroy", "chf_last_error", "chf_upload_state",
            "chf_batch_handle", "chf_batch_step", "chf_batch_synchronize",
            "chf_set_flow_rate", "chf_get_flow_rate", "chf_statistics", "chf_pressure",
            "chf_transform", "chf_cfl", "chf_physical_velocity", "chf_write_velocity",
-           "chf_autotune", "chf_tuning", "chf_test_wait_timeout")
+           "chf_autotune", "chf_tuning", "chf_set_launch_shape", "chf_test_wait_timeout")
 
 
 class ChannelError(RuntimeError):
@@ -105,6 +105,7 @@ def load_library(path: str = None):
     L.chf_autotune.argtypes = [vp, ctypes.c_int]
     L.chf_test_wait_timeout.argtypes = [vp, ctypes.c_int]
     L.chf_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
+    L.chf_set_launch_shape.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
     L.chf_cfl.argtypes = [vp, dp, dp, dp]
     L.chf_physical_velocity.argtypes = [vp, dp, dp]
     L.chf_write_velocity.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, dp]
@@ -273,6 +274,11 @@ class Channel:
         buf = ctypes.create_string_buffer(1024)
         self._check(self.L.chf_tuning(self.h, buf, len(buf)))
         return buf.value.decode()
+
+    def set_launch_shape(self, name: str, value: int) -> None:
+        """One launch shape by name (chf_set_launch_shape): "inc_modes",
+        "inc_columns", "inc_rows", "kxb", "xr", "zl_c2v" or "zl_curl"."""
+        self._check(self.L.chf_set_launch_shape(self.h, name.encode(), int(value)))
 
     def transform(self, isign: int, u: np.ndarray) -> np.ndarray:
         """transform (poiseuilleflow.f90:919-1005) of one array in the field

@@ -152,7 +152,7 @@ static void release(chf_handle* h) {
   for (auto& p : h->mean) cudaFree(p);
   void* ptrs[] = {h->iapha, h->ibeta, h->t0, h->t2, h->t4, h->k2vals, h->xinv, h->xmean,
                   h->group_start, h->group_modes, h->tw_py, h->tw_px, h->tw_z2, h->tw_zm,
-                  h->twf_py, h->twf_px, h->incm, h->incx, h->incr_exp, h->phi, h->flow, h->stats_buf, h->pres_buf, h->phys_buf, h->tw_pxu, h->tw_pyu, h->group_re, h->ubphi_dev, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
+                  h->twf_py, h->twf_px, h->incm, h->incx, h->incr_exp, h->inc_items, h->phi, h->flow, h->stats_buf, h->pres_buf, h->phys_buf, h->tw_pxu, h->tw_pyu, h->group_re, h->ubphi_dev, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
                   h->agl, h->bimg, h->wz32, h->wy32, h->lc64, h->aexp1, h->aexp2, h->aexp3, h->bexp, h->z2_tail, h->gl_tail};
   for (void* p : ptrs) cudaFree(p);
   for (auto& p : h->pending) {

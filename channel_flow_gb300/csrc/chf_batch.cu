@@ -298,6 +298,10 @@ int build_stack(chf_batch* b, Stack& S) {
                             cudaMemcpyDeviceToDevice), "class increment operators"))
         return CHF_E_CUDA;
     }
+    if (setup_inc_items(h) != CHF_OK) {
+      b->err = "class set-up: " + h->err;
+      return CHF_E_CUDA;
+    }
     if (!ok(b, cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !ok(b, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming), "cudaEventCreate") ||
         !ok(b, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming), "cudaEventCreate"))

@@ -104,8 +104,11 @@ struct Tuning {
   int zl_c2v = 0;   // modes per CTA of the FP64 z transform to the product grid
   int zl_curl = 0;  // modes per CTA of the FP64 z transform + curl
   int inc_mch = 4;  // modes per pass of the increment solve (2 or 4)
-  int inc_cb = 3;   // matrix columns per load batch of the increment solve (2..4)
+  int inc_cb = 4;   // matrix columns per load batch of the increment solve (2..4)
+  int inc_rpt = 1;  // rows per thread of the increment solve (1 or 2; 2 with 2 or 3 columns)
+  int inc_wide = 1; // one row per thread: every block row in one pass (1) or loop (0)
   bool tuned = false;
+  bool manual = false;  // a shape was set by chf_set_launch_shape
 };
 
 struct Handle {
@@ -137,6 +140,10 @@ struct Handle {
   float2* incm = nullptr;
   float* incx = nullptr;
   signed char* incr_exp = nullptr;
+  // k_inc_solve work items {group, first mode index}: runs of at most 4
+  // modes (n_inc_items[1] of them), then runs of at most 2 (n_inc_items[0])
+  int2* inc_items = nullptr;
+  int n_inc_items[2] = {0, 0};
   double* xmean = nullptr;    // inverse of the (0,0) operator, NZ x NZ column-major
   int* group_start = nullptr; // nk2 + 1 (modes grouped by k^2)
   int* group_modes = nullptr; // solved modes, sorted by k^2 index
@@ -297,6 +304,8 @@ int step_once(Handle* h);
 // launchers (k_solve.cu)
 int setup_solver(Handle* h);
 int setup_solver_mixed(Handle* h);
+// the work items of k_inc_solve from the handle's k^2 groups
+int setup_inc_items(Handle* h);
 bool xy_register_path(const Dims& d);
 int launch_yinv_fields(Handle* h, cf* wz, cf* wy, const cf* tw_py, int f0, int nf);
 int launch_xprod_yfwd(Handle* h, cf* wz, cf* wy, const cf* tw_py, const cf* tw_px);

@@ -118,10 +118,11 @@ std::string describe(const Handle* h, double ms_rule, double ms_best) {
   char buf[512];
   std::snprintf(buf, sizeof buf,
                 "fft radices py %s px %s pz2 %s pzm %s; kxb %d xr %d zl_c2v %d zl_curl %d; "
-                "increment solve %d modes x %d columns; step %.4f ms (rules %.4f ms)",
+                "increment solve %d modes x %d columns x %d rows per thread%s; step %.4f ms (rules %.4f ms)",
                 radix_string(h->py).c_str(), radix_string(h->px).c_str(), radix_string(h->pz2).c_str(),
                 radix_string(h->pzm).c_str(), h->tune.kxb, h->tune.xr, h->tune.zl_c2v, h->tune.zl_curl,
-                h->tune.inc_mch, h->tune.inc_cb, ms_best, ms_rule);
+                h->tune.inc_mch, h->tune.inc_cb, h->tune.inc_rpt, h->tune.inc_wide ? "" : " (288-thread blocks)",
+                ms_best, ms_rule);
   return buf;
 }
 
@@ -226,10 +227,24 @@ int chf_autotune(chf_handle* h, int reps) {
   // CHF_MIXED_F64SOLVE, the (0,0) mode in CHF_MIXED)
   try_knob([&](const FftPlan& p) { h->pz2 = p; }, with_current(h->pz2, plan_candidates(make_plan(2 * d.N))));
   if (increment_solve(h)) {
-    std::vector<std::pair<int, int>> maps{{h->tune.inc_mch, h->tune.inc_cb}};
+    struct IncMap {
+      int mch, cb, rpt, wide;
+    };
+    std::vector<IncMap> maps{{h->tune.inc_mch, h->tune.inc_cb, h->tune.inc_rpt, h->tune.inc_wide}};
+    const SolveLayout& sl = h->sl;
+    const bool long_blocks = sl.ne_v + sl.no_v + sl.ne_w + sl.no_w > 288;  // the one-row block loops
+    for (int wide : {1, 0}) {
+      if (wide == 0 && !long_blocks) continue;
+      for (int mch : {4, 2})
+        for (int cb : {4, 3, 2}) maps.push_back({mch, cb, 1, wide});
+    }
     for (int mch : {4, 2})
-      for (int cb : {3, 2, 4}) maps.push_back({mch, cb});
-    try_knob([&](const std::pair<int, int>& m) { h->tune.inc_mch = m.first, h->tune.inc_cb = m.second; }, maps);
+      for (int cb : {3, 2}) maps.push_back({mch, cb, 2, 1});
+    try_knob(
+        [&](const IncMap& m) {
+          h->tune.inc_mch = m.mch, h->tune.inc_cb = m.cb, h->tune.inc_rpt = m.rpt, h->tune.inc_wide = m.wide;
+        },
+        maps);
   }
   h->profiling = was_profiling;
   // put the state back
@@ -253,9 +268,59 @@ int chf_autotune(chf_handle* h, int reps) {
     return CHF_E_CUDA;
   }
   h->tune.tuned = true;
+  h->tune.manual = false;
   Choice c{h->tune, h->py, h->px, h->pz2, h->pzm, describe(h, rule, best)};
   std::lock_guard<std::mutex> lock(g_mu);
   g_cache[key_of(h)] = c;
+  return CHF_OK;
+}
+
+int chf_set_launch_shape(chf_handle* h, const char* name, int value) {
+  if (!h) return CHF_E_INVALID;
+  if (!name) {
+    h->err = "chf_set_launch_shape: no name";
+    return CHF_E_INVALID;
+  }
+  const std::string n(name);
+  Tuning t = h->tune;
+  auto bad = [&](const char* why) {
+    h->err = "chf_set_launch_shape(" + n + ", " + std::to_string(value) + "): " + why;
+    return CHF_E_INVALID;
+  };
+  if (n == "inc_modes") {
+    if (value != 2 && value != 4) return bad("2 or 4 modes per CTA");
+    t.inc_mch = value;
+  } else if (n == "inc_columns") {
+    if (value < 2 || value > 4) return bad("2, 3 or 4 columns per batch");
+    t.inc_cb = value;
+  } else if (n == "inc_rows") {
+    if (value != 1 && value != 2) return bad("1 or 2 rows per thread");
+    t.inc_rpt = value;
+  } else if (n == "inc_wide") {
+    if (value != 0 && value != 1) return bad("0 or 1");
+    t.inc_wide = value;
+  } else {
+    static const char* knobs[] = {"kxb", "xr", "zl_c2v", "zl_curl"};
+    int k = -1;
+    for (int i = 0; i < 4; ++i)
+      if (n == knobs[i]) k = i;
+    if (k < 0) return bad("unknown name");
+    if (value != 0) {
+      const auto c = shape_candidates(h, k);
+      if (std::find(c.begin(), c.end(), value) == c.end()) return bad("not a shape that fits this grid");
+    }
+    int* f[] = {&t.kxb, &t.xr, &t.zl_c2v, &t.zl_curl};
+    *f[k] = value;
+  }
+  if (t.inc_rpt == 2 && t.inc_cb == 4) return bad("two rows per thread take 2 or 3 columns per batch");
+  if (!cuda_ok(h, cudaSetDevice(h->device), "cudaSetDevice") ||
+      !cuda_ok(h, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))
+    return CHF_E_CUDA;
+  t.manual = true;
+  h->tune = t;
+  // the captured step graphs hold the old shapes
+  for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
+  h->graphs.clear();
   return CHF_OK;
 }
 
@@ -265,7 +330,8 @@ int chf_tuning(const chf_handle* h, char* buf, int len) {
   {
     std::lock_guard<std::mutex> lock(g_mu);
     auto it = g_cache.find(key_of(h));
-    s = (h->tune.tuned || it != g_cache.end()) && it != g_cache.end()
+    s = h->tune.manual ? describe(h, 0.0, 0.0) + " (set by chf_set_launch_shape)"
+        : (h->tune.tuned || it != g_cache.end()) && it != g_cache.end()
             ? it->second.report
             : describe(h, 0.0, 0.0) + " (launch rules; not tuned)";
   }

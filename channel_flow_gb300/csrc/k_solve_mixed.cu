@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "chf_internal.h"
 #include "f32x2.cuh"
@@ -125,8 +126,8 @@ __global__ void __launch_bounds__(128) k_incr_rowexp(const float2* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// k_inc_solve: one CTA per k^2 group (mean excluded), MCH modes of the group
-// per pass.  Per mode the CTA stages in shared memory
+// k_inc_solve: one CTA per work item, up to MCH modes of one k^2 group (mean
+// excluded; setup_inc_items).  Per mode the CTA stages in shared memory
 //   * the coefficients c of v and omega_y as (hi, lo) floats, ordered as the
 //     four blocks' columns (v even j, v odd j, omega even j, omega odd j);
 //   * the AB2 term r = dt (3/2 N^n - 1/2 N^{n-1}) at the Gauss-Lobatto
@@ -166,106 +167,151 @@ __device__ __forceinline__ void sig_mac2(f32x2 mh, f32x2 ml, f32x2 ch, f32x2 cl,
   C = fma2(ml, ch, fma2(mh, cl, add2(C, u)));
 }
 
-// Rows of one pass of k_inc_solve for NM staged modes: thread t owns row t of
-// the four blocks (v even, v odd, omega even, omega odd).
-template <int NM, int CB>
+// Rows of one pass of k_inc_solve for NM staged modes: each thread owns RPT
+// adjacent rows of one of the four blocks (v even, v odd, omega even,
+// omega odd), so that every staged coefficient and AB2 value read from
+// shared memory serves RPT rows.  The arithmetic of a row does not depend on
+// RPT.
+template <int NM, int CB, int RPT>
 __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g, const float2* __restrict__ Mg,
                                          const float* __restrict__ Xg, const SolveLayout& sl,
                                          const BlockOffsets& bo, int NZ, long modes, const cd* Cd,
                                          const CoefHL* Cs, const float2* Rs, const int* s_mode,
                                          const signed char* __restrict__ rexp, const int* s_cexp) {
   const int nev = sl.ne_v, nov = sl.no_v, new_ = sl.ne_w, now_ = sl.no_w;
-  const int rows = nev + nov + new_ + now_;
-  for (int t = threadIdx.x; t < rows; t += blockDim.x) {
-    int b, row, n;
+  // slots (groups of RPT rows) per block
+  const int sev = (nev + RPT - 1) / RPT, sov = (nov + RPT - 1) / RPT, sew = (new_ + RPT - 1) / RPT,
+            sow = (now_ + RPT - 1) / RPT;
+  const int slots = sev + sov + sew + sow;
+  for (int t = threadIdx.x; t < slots; t += blockDim.x) {
+    int b, slot, n;
     size_t boff;
-    if (t < nev) { b = 0; row = t; n = nev; boff = bo.ve; }
-    else if (t < nev + nov) { b = 1; row = t - nev; n = nov; boff = bo.vo; }
-    else if (t < nev + nov + new_) { b = 2; row = t - nev - nov; n = new_; boff = bo.we; }
-    else { b = 3; row = t - nev - nov - new_; n = now_; boff = bo.wo; }
+    if (t < sev) { b = 0; slot = t; n = nev; boff = bo.ve; }
+    else if (t < sev + sov) { b = 1; slot = t - sev; n = nov; boff = bo.vo; }
+    else if (t < sev + sov + sew) { b = 2; slot = t - sev - sov; n = new_; boff = bo.we; }
+    else { b = 3; slot = t - sev - sov - sew; n = now_; boff = bo.wo; }
     // offset of block b inside a mode's 2 NZ staged entries
     const int roff = b == 0 ? 0 : b == 1 ? nev : b == 2 ? NZ : NZ + new_;
-    const float2* Mb = Mg + boff + row;
-    const float* Xb = Xg + boff + row;
-    f32x2 S[NM], C[NM];  // (re, im) pairs
-    const int er = rexp[roff + row];
+    const int row0 = slot * RPT;
+    bool live[RPT];
+    const float2* Mb[RPT];
+    const float* Xb[RPT];
+    f32x2 S[RPT][NM], C[RPT][NM];  // (re, im) pairs
 #pragma unroll
-    for (int q = 0; q < NM; ++q) {  // S starts at sigma of mode q for this row
-      const int e = max(-120, min(120, er + s_cexp[4 * q + b] + 3));
-      const float sg = __int_as_float((127 + e) << 23);
-      S[q] = pk(sg, sg);
-      C[q] = 0ull;
+    for (int i = 0; i < RPT; ++i) {
+      live[i] = row0 + i < n;
+      const int row = live[i] ? row0 + i : row0;  // a dead row reads its live neighbour
+      Mb[i] = Mg + boff + row;
+      Xb[i] = Xg + boff + row;
+      const int er = rexp[roff + row];
+#pragma unroll
+      for (int q = 0; q < NM; ++q) {  // S starts at sigma of mode q for this row
+        const int e = max(-120, min(120, er + s_cexp[4 * q + b] + 3));
+        const float sg = __int_as_float((127 + e) << 23);
+        S[i][q] = pk(sg, sg);
+        C[i][q] = 0ull;
+      }
     }
     // columns c < r0 of X meet the zero wall entries of the staged rhs
-    float2 ma[CB];
-    float xa[CB];
+    float2 ma[RPT][CB];
+    float xa[RPT][CB];
 #pragma unroll
-    for (int u = 0; u < CB; ++u) {
-      ma[u] = u < n ? __ldg(Mb + (size_t)u * n) : make_float2(0.f, 0.f);
-      xa[u] = u < n ? __ldg(Xb + (size_t)u * n) : 0.f;
-    }
+    for (int u = 0; u < CB; ++u)
+#pragma unroll
+      for (int i = 0; i < RPT; ++i) {
+        ma[i][u] = u < n ? __ldg(Mb[i] + (size_t)u * n) : make_float2(0.f, 0.f);
+        xa[i][u] = u < n ? __ldg(Xb[i] + (size_t)u * n) : 0.f;
+      }
     const f32x2* Rs2 = reinterpret_cast<const f32x2*>(Rs);
     for (int c0 = 0; c0 < n; c0 += CB) {
-      float2 mb[CB];
-      float xb[CB];
+      float2 mb[RPT][CB];
+      float xb[RPT][CB];
 #pragma unroll
       for (int u = 0; u < CB; ++u) {
         const int c = c0 + CB + u;
-        mb[u] = c < n ? __ldg(Mb + (size_t)c * n) : make_float2(0.f, 0.f);
-        xb[u] = c < n ? __ldg(Xb + (size_t)c * n) : 0.f;
-      }
 #pragma unroll
-      for (int u = 0; u < CB; ++u) {
-        if (c0 + u < n) {
-          const f32x2 mh = pk(ma[u].x, ma[u].x), ml = pk(ma[u].y, ma[u].y);
-          const f32x2 xx = pk(xa[u], xa[u]);
-#pragma unroll
-          for (int q = 0; q < NM; ++q) {
-            const int si = q * 2 * NZ + roff + c0 + u;
-            const float4 ch = reinterpret_cast<const float4*>(Cs)[si];  // one 16-byte load
-            sig_mac2(mh, ml, pk(ch.x, ch.y), pk(ch.z, ch.w), S[q], C[q]);
-            C[q] = fma2(xx, Rs2[si], C[q]);
-          }
+        for (int i = 0; i < RPT; ++i) {
+          mb[i][u] = c < n ? __ldg(Mb[i] + (size_t)c * n) : make_float2(0.f, 0.f);
+          xb[i][u] = c < n ? __ldg(Xb[i] + (size_t)c * n) : 0.f;
         }
       }
 #pragma unroll
       for (int u = 0; u < CB; ++u) {
-        ma[u] = mb[u];
-        xa[u] = xb[u];
+        if (c0 + u < n) {
+#pragma unroll
+          for (int q = 0; q < NM; ++q) {
+            const int si = q * 2 * NZ + roff + c0 + u;
+            const float4 ch = reinterpret_cast<const float4*>(Cs)[si];  // one 16-byte load
+            const f32x2 rr = Rs2[si];
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+              const f32x2 mh = pk(ma[i][u].x, ma[i][u].x), ml = pk(ma[i][u].y, ma[i][u].y);
+              sig_mac2(mh, ml, pk(ch.x, ch.y), pk(ch.z, ch.w), S[i][q], C[i][q]);
+              C[i][q] = fma2(pk(xa[i][u], xa[i][u]), rr, C[i][q]);
+            }
+          }
+        }
       }
+#pragma unroll
+      for (int u = 0; u < CB; ++u)
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+          ma[i][u] = mb[i][u];
+          xa[i][u] = xb[i][u];
+        }
     }
-    const int j = (b == 0 || b == 2) ? 2 * row : 2 * row + 1;
     cd* dst = b < 2 ? v : g;
 #pragma unroll
-    for (int q = 0; q < NM; ++q) {
-      const cd c0 = Cd[q * 2 * NZ + roff + row];
-      float Sv[2], Cv[2];
-      upk(S[q], Sv[0], Sv[1]);
-      upk(C[q], Cv[0], Cv[1]);
-      double x[2];
+    for (int i = 0; i < RPT; ++i) {
+      if (!live[i]) continue;
+      const int row = row0 + i;
+      const int j = (b == 0 || b == 2) ? 2 * row : 2 * row + 1;
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        // S - sigma (exact): S lies within (7/8, 9/8) sigma, so sigma is S's
-        // power of two, rounded up when S's significand is at least 1.5
-        const float d = Sv[k] - __int_as_float((__float_as_int(Sv[k]) + 0x400000) & 0xff800000);
-        // x = c + delta with two FP64 additions (the float -> double moves
-        // are integer operations)
-        x[k] = ((k == 0 ? c0.re : c0.im) + bits::widen(d)) + bits::widen(Cv[k]);
+      for (int q = 0; q < NM; ++q) {
+        const cd c0 = Cd[q * 2 * NZ + roff + row];
+        float Sv[2], Cv[2];
+        upk(S[i][q], Sv[0], Sv[1]);
+        upk(C[i][q], Cv[0], Cv[1]);
+        double x[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          // S - sigma (exact): S lies within (7/8, 9/8) sigma, so sigma is S's
+          // power of two, rounded up when S's significand is at least 1.5
+          const float d = Sv[k] - __int_as_float((__float_as_int(Sv[k]) + 0x400000) & 0xff800000);
+          // x = c + delta with two FP64 additions (the float -> double moves
+          // are integer operations)
+          x[k] = ((k == 0 ? c0.re : c0.im) + bits::widen(d)) + bits::widen(Cv[k]);
+        }
+        dst[(size_t)j * modes + s_mode[q]] = cd{x[0], x[1]};
       }
-      dst[(size_t)j * modes + s_mode[q]] = cd{x[0], x[1]};
     }
   }
 }
 
-template <int MCH, int CB>
-__global__ void __launch_bounds__(MV_THREADS, MCH == 2 ? 4 : 3) k_inc_solve(cd* __restrict__ v, cd* __restrict__ g,
+// block size and minimum CTAs per SM of k_inc_solve: one row per thread at
+// MV_THREADS threads (RPT = 1; blocks of more rows loop), one row per thread
+// with every row in one pass at up to MV_WIDE threads (RPT = 0, for
+// wall-normal grids of more than MV_THREADS block rows), or two rows per
+// thread at up to 256 threads (RPT = 2)
+constexpr int MV_WIDE = 416;
+template <int MCH, int RPT>
+struct IncShape {
+  static constexpr int threads = RPT == 1 ? MV_THREADS : RPT == 0 ? MV_WIDE : 256;
+  static constexpr int min_ctas = RPT == 1 ? (MCH == 2 ? 4 : 3) : 2;
+  static constexpr int rows = RPT == 0 ? 1 : RPT;  // block rows per thread
+};
+
+template <int MCH, int CB, int RPT>
+__global__ void __launch_bounds__(IncShape<MCH, RPT>::threads, IncShape<MCH, RPT>::min_ctas)
+    k_inc_solve(cd* __restrict__ v, cd* __restrict__ g,
                                                              const cd* __restrict__ rv, const cd* __restrict__ uh,
                                                              const cd* __restrict__ rg, const cd* __restrict__ wh,
                                                              const float2* __restrict__ incm,
                                                              const float* __restrict__ incx,
                                                              const signed char* __restrict__ rowexp, SolveLayout sl,
                                                              const int* __restrict__ group_start,
-                                                             const int* __restrict__ group_modes, Dims d,
+                                                             const int* __restrict__ group_modes,
+                                                             const int2* __restrict__ items, Dims d,
                                                              float c3, float c1) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = d.N, NZ = d.NZ, ne = N / 2 + 1;
@@ -275,13 +321,14 @@ __global__ void __launch_bounds__(MV_THREADS, MCH == 2 ? 4 : 3) k_inc_solve(cd* 
   float2* Rs = reinterpret_cast<float2*>(Cs + MCH * 2 * NZ);  // [MCH][2 NZ] folded AB2 term
   __shared__ int s_mode[MCH];
   __shared__ int s_cexp[MCH * 4];  // largest |hi| per (mode, block): float bits, then its exponent
-  const int grp = blockIdx.x;
-  const int gs = group_start[grp], ge = group_start[grp + 1];
+  // work item: up to MCH modes of one k^2 group, from base
+  const int2 it = items[blockIdx.x];
+  const int grp = it.x, base = it.y;
   const BlockOffsets bo = block_offsets(sl);
   const float2* Mg = incm + (size_t)grp * sl.stride;
   const float* Xg = incx + (size_t)grp * sl.stride;
-  for (int base = gs; base < ge; base += MCH) {
-    const int nm = min(MCH, ge - base);
+  {
+    const int nm = min(MCH, group_start[grp + 1] - base);
     if (threadIdx.x < nm) s_mode[threadIdx.x] = group_modes[base + threadIdx.x];
     if (threadIdx.x < MCH * 4) s_cexp[threadIdx.x] = 0;
     __syncthreads();
@@ -323,16 +370,15 @@ __global__ void __launch_bounds__(MV_THREADS, MCH == 2 ? 4 : 3) k_inc_solve(cd* 
     __syncthreads();
     const signed char* rexp = rowexp + (size_t)grp * 2 * NZ;
     switch (nm) {
-      case 1: inc_rows<1, CB>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
-      case 2: inc_rows<2, CB>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      case 1: inc_rows<1, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      case 2: inc_rows<2, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
       default:
         if constexpr (MCH >= 4) {
-          if (nm == 3) inc_rows<3, CB>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
-          else inc_rows<4, CB>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
+          if (nm == 3) inc_rows<3, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
+          else inc_rows<4, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
         }
         break;
     }
-    __syncthreads();
   }
 }
 
@@ -471,6 +517,35 @@ int setup_solver_mixed(Handle* h) {
   if (!cuda_ok(h, cudaGetLastError(), "k_incr_rowexp") ||
       !cuda_ok(h, cudaStreamSynchronize(h->stream), "k_build_incr sync"))
     return CHF_E_CUDA;
+  return setup_inc_items(h);
+}
+
+// Work items of k_inc_solve, one CTA each: a k^2 group's modes in runs of at
+// most 4 (the first n_inc_items[1] entries) or 2 (the next n_inc_items[0]).
+// The runs of one group are adjacent in the list, so the CTAs that stream the
+// same operators run at the same time and share them through L2 instead of a
+// group's later runs reading them from HBM again.  Groups stay in k^2 order:
+// modes next to each other in memory (kx, kx + 1) have nearby k^2, so the
+// CTAs that gather them run close in time and the other half of each 32-byte
+// sector of the mode-major fields is still in L2.
+int setup_inc_items(Handle* h) {
+  const int ng = h->nk2;
+  std::vector<int> gs(ng + 1);
+  if (!cuda_ok(h, cudaMemcpy(gs.data(), h->group_start, sizeof(int) * gs.size(), cudaMemcpyDeviceToHost),
+               "increment solve items"))
+    return CHF_E_CUDA;
+  std::vector<int2> items;
+  for (int mch : {4, 2}) {
+    const size_t first = items.size();
+    for (int g = 0; g < ng; ++g)
+      for (int base = gs[g]; base < gs[g + 1]; base += mch) items.push_back(make_int2(g, base));
+    h->n_inc_items[mch == 4 ? 1 : 0] = (int)(items.size() - first);
+  }
+  if (items.empty()) return CHF_OK;
+  if (!cuda_ok(h, cudaMalloc((void**)&h->inc_items, sizeof(int2) * items.size()), "increment solve items") ||
+      !cuda_ok(h, cudaMemcpy(h->inc_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice),
+               "increment solve items"))
+    return CHF_E_NOMEM;
   return CHF_OK;
 }
 
@@ -494,18 +569,32 @@ int launch_solve_mixed(Handle* h) {
     if (!cuda_ok(h, cudaEventRecord(h->ev_join, h->side_stream), "solve join")) return CHF_E_CUDA;
   }
   if (h->nk2 > 0) {
+    const SolveLayout& sl = h->sl;
+    const int rows = sl.ne_v + sl.no_v + sl.ne_w + sl.no_w;
     const int mch = h->tune.inc_mch == 2 ? 2 : 4, cb = h->tune.inc_cb;
-    auto kern = mch == 2 ? (cb == 2 ? k_inc_solve<2, 2> : cb == 4 ? k_inc_solve<2, 4> : k_inc_solve<2, 3>)
-                         : (cb == 2 ? k_inc_solve<4, 2> : cb == 4 ? k_inc_solve<4, 4> : k_inc_solve<4, 3>);
+    // the wide block only where one row per thread at MV_THREADS would loop
+    const int rpt = h->tune.inc_rpt == 2 ? 2 : h->tune.inc_wide && rows > MV_THREADS ? 0 : 1;
+    auto kern = rpt == 2 ? (mch == 2 ? (cb == 2 ? k_inc_solve<2, 2, 2> : k_inc_solve<2, 3, 2>)
+                                     : (cb == 2 ? k_inc_solve<4, 2, 2> : k_inc_solve<4, 3, 2>))
+              : rpt == 0 ? (mch == 2 ? (cb == 2 ? k_inc_solve<2, 2, 0> : cb == 4 ? k_inc_solve<2, 4, 0> : k_inc_solve<2, 3, 0>)
+                                     : (cb == 2 ? k_inc_solve<4, 2, 0> : cb == 4 ? k_inc_solve<4, 4, 0> : k_inc_solve<4, 3, 0>))
+              : mch == 2 ? (cb == 2 ? k_inc_solve<2, 2, 1> : cb == 4 ? k_inc_solve<2, 4, 1> : k_inc_solve<2, 3, 1>)
+                         : (cb == 2 ? k_inc_solve<4, 2, 1> : cb == 4 ? k_inc_solve<4, 4, 1> : k_inc_solve<4, 3, 1>);
+    const int slots2 = (sl.ne_v + 1) / 2 + (sl.no_v + 1) / 2 + (sl.ne_w + 1) / 2 + (sl.no_w + 1) / 2;
+    const int threads = rpt == 1 ? MV_THREADS
+                      : rpt == 0 ? std::min(MV_WIDE, (rows + 31) / 32 * 32)
+                                 : std::min(256, (slots2 + 31) / 32 * 32);
     const size_t smem = (sizeof(cd) + sizeof(CoefHL) + sizeof(float2)) * mch * 2 * (size_t)NZ;
     if (smem > 48 * 1024 &&
         !cuda_ok(h, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                  "k_inc_solve smem"))
       return CHF_E_CUDA;
     prof_begin(h, K_INC_SOLVE, &ev);
-    kern<<<h->nk2, MV_THREADS, smem, st>>>(h->f[F_V], h->f[F_OY], h->f[F_RV], h->f[F_U], h->f[F_RG],
-                                                   h->f[F_W], h->incm, h->incx, h->incr_exp, h->sl, h->group_start,
-                                                   h->group_modes, d, (float)(1.5 * dt), (float)(0.5 * dt));
+    const int nitems = h->n_inc_items[mch == 4 ? 1 : 0];
+    const int2* items = h->inc_items + (mch == 4 ? 0 : h->n_inc_items[1]);
+    kern<<<nitems, threads, smem, st>>>(h->f[F_V], h->f[F_OY], h->f[F_RV], h->f[F_U], h->f[F_RG],
+                                           h->f[F_W], h->incm, h->incx, h->incr_exp, h->sl, h->group_start,
+                                           h->group_modes, items, d, (float)(1.5 * dt), (float)(0.5 * dt));
     prof_end(h, K_INC_SOLVE, ev);
     if (h->after_inc && !cuda_ok(h, cudaEventRecord(h->after_inc, st), "increment solve event")) return CHF_E_CUDA;
   }

@@ -191,6 +191,19 @@ int chf_autotune(chf_handle* h, int reps);
 /* The handle's launch shapes and radix orders as text (the measured step
  * times when tuned), NUL-terminated in buf[0..len-1]. */
 int chf_tuning(const chf_handle* h, char* buf, int len);
+/* Sets one launch shape by name, in place of the rule or the autotuner's
+ * choice (every shape computes the same results, bit for bit):
+ *   "inc_modes"    modes per CTA of the CHF_MIXED increment solve: 2 or 4
+ *   "inc_columns"  its matrix columns per load batch: 2, 3 or 4
+ *   "inc_rows"     its block rows per thread: 1 or 2 (2 with 2 or 3 columns)
+ *   "inc_wide"     with one row per thread, every block row in one pass (1,
+ *                  up to 416 threads) or 288-thread blocks that loop (0)
+ *   "kxb", "xr", "zl_c2v", "zl_curl"  lines per CTA of the shared-memory
+ *                  FFT kernels: one of the shapes that fit the grid, or 0
+ *                  for the launcher's rule
+ * CHF_E_INVALID for an unknown name or a value that the grid or the other
+ * shapes rule out (the handle is then unchanged).  Synchronous. */
+int chf_set_launch_shape(chf_handle* h, const char* name, int value);
 
 /* Per-kernel timing with CUDA events recorded around every launch on the
  * handle's stream (off by default; the reference's only instrumentation is
