@@ -298,6 +298,7 @@ int build_stack(chf_batch* b, Stack& S) {
                             cudaMemcpyDeviceToDevice), "class increment operators"))
         return CHF_E_CUDA;
     }
+    h->rec_df_rule = c0.rec_df_rule;  // the members' arithmetic
     if (setup_inc_items(h) != CHF_OK) {
       b->err = "class set-up: " + h->err;
       return CHF_E_CUDA;

@@ -107,6 +107,9 @@ struct Tuning {
   int inc_cb = 4;   // matrix columns per load batch of the increment solve (2..4)
   int inc_rpt = 1;  // rows per thread of the increment solve (1 or 2; 2 with 2 or 3 columns)
   int inc_wide = 1; // one row per thread: every block row in one pass (1) or loop (0)
+  // arithmetic of k_inc_recover (not searched by the autotuner): -1 the
+  // handle's rule, 0 FP64, 1 double-float (2^-44 relative)
+  int rec_form = -1;
   bool tuned = false;
   bool manual = false;  // a shape was set by chf_set_launch_shape
 };
@@ -144,6 +147,7 @@ struct Handle {
   // modes (n_inc_items[1] of them), then runs of at most 2 (n_inc_items[0])
   int2* inc_items = nullptr;
   int n_inc_items[2] = {0, 0};
+  bool rec_df_rule = false;  // k_inc_recover's double-float form (setup_solver_mixed)
   double* xmean = nullptr;    // inverse of the (0,0) operator, NZ x NZ column-major
   int* group_start = nullptr; // nk2 + 1 (modes grouped by k^2)
   int* group_modes = nullptr; // solved modes, sorted by k^2 index

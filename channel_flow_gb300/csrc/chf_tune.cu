@@ -118,11 +118,13 @@ std::string describe(const Handle* h, double ms_rule, double ms_best) {
   char buf[512];
   std::snprintf(buf, sizeof buf,
                 "fft radices py %s px %s pz2 %s pzm %s; kxb %d xr %d zl_c2v %d zl_curl %d; "
-                "increment solve %d modes x %d columns x %d rows per thread%s; step %.4f ms (rules %.4f ms)",
+                "increment solve %d modes x %d columns x %d rows per thread%s, %s recovery; step %.4f ms "
+                "(rules %.4f ms)",
                 radix_string(h->py).c_str(), radix_string(h->px).c_str(), radix_string(h->pz2).c_str(),
                 radix_string(h->pzm).c_str(), h->tune.kxb, h->tune.xr, h->tune.zl_c2v, h->tune.zl_curl,
                 h->tune.inc_mch, h->tune.inc_cb, h->tune.inc_rpt, h->tune.inc_wide ? "" : " (288-thread blocks)",
-                ms_best, ms_rule);
+                (h->tune.rec_form >= 0 ? h->tune.rec_form == 1 : h->rec_df_rule) ? "double-float" : "FP64", ms_best,
+                ms_rule);
   return buf;
 }
 
@@ -299,6 +301,9 @@ int chf_set_launch_shape(chf_handle* h, const char* name, int value) {
   } else if (n == "inc_wide") {
     if (value != 0 && value != 1) return bad("0 or 1");
     t.inc_wide = value;
+  } else if (n == "recover_form") {
+    if (value < -1 || value > 1) return bad("-1 (rule), 0 (FP64) or 1 (double-float)");
+    t.rec_form = value;
   } else {
     static const char* knobs[] = {"kxb", "xr", "zl_c2v", "zl_curl"};
     int k = -1;

@@ -390,6 +390,195 @@ __global__ void __launch_bounds__(IncShape<MCH, RPT>::threads, IncShape<MCH, RPT
 //   u = (i a Dv - i b g) / k^2,            w = (i b Dv + i a g) / k^2,
 //   omega_z = -Du + i a v = (i b Dg - i a D^2 v) / k^2 + i a v,
 //   omega_x =  Dw - i b v = (i b D^2 v + i a Dg) / k^2 - i b v.
+// The dz recurrences (b_0 halved on output) run on descending rows; the
+// even-k and odd-k chains of Dv and Dg are independent, so the pair of parity
+// threads of a component runs them in lockstep (even rows 2s below the top,
+// odd rows one below those); D^2 v at row k needs Dv at row k + 1 from the
+// other chain, and Dv, Dg at row k need v, g at row k + 1, the other chain's
+// row: both come by shuffle (the odd thread takes the even thread's current
+// values, the even thread the odd thread's previous ones).  The other re/im
+// component comes by shuffle too, and multiplying by i folds into the signs
+// of the per-thread coefficients.
+// Arithmetic: double-float (hi, lo) pairs of FP32.  v and omega_y enter as
+// their (hi, lo) splits (bits::split: 2^-46 relative); a recurrence step
+// t a + b (t = 2 (k + 1), an exact FP32 integer) is an exact product and an
+// exact sum (Knuth's two-sum) plus the low parts, renormalised; an output is
+// a sum of double-float products.  Every operation is a __f*_rn intrinsic,
+// which the compiler never contracts into an FMA (a contracted
+// multiply-subtract would break the two-sum).  Each output leaves as hi + lo
+// in one FP64 addition (the only FP64 operations: 4 per element; the FP64
+// pipe retires about 2 lane-operations per clock per SM, FP32 about 128).
+// Relative to the largest term of each sum the result is within about
+// 2^-44, against 2^-53 for FP64 throughout; RC_PF steps of v and omega_y are
+// loaded ahead.
+// ---------------------------------------------------------------------------
+constexpr int RC_THREADS = 32;  // one warp: 1024 CTAs at 128^3, balanced over the SMs
+constexpr int RC_PF = 8;  // steps of v, omega_y loaded ahead of the recurrences
+
+// a double-float value h + l
+struct DF {
+  float h, l;
+};
+
+// s + e = a + b exactly (Knuth's two-sum)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// t a + b for an exact FP32 integer t, renormalised
+__device__ __forceinline__ DF df_fma_int(float t, const DF& a, const DF& b) {
+  const float p = __fmul_rn(t, a.h);
+  const float pe = __fmaf_rn(t, a.h, -p);  // t a.h - p, exact
+  float s, e;
+  two_sum(b.h, p, s, e);
+  const float lo = __fadd_rn(e, __fadd_rn(b.l, __fmaf_rn(t, a.l, pe)));
+  DF r;
+  two_sum(s, lo, r.h, r.l);
+  return r;
+}
+
+// c x as (ph, pl), unnormalised: ph = RN(c.h x.h), pl = the rest
+__device__ __forceinline__ void df_prod(const DF& c, const DF& x, float& ph, float& pl) {
+  ph = __fmul_rn(c.h, x.h);
+  pl = __fmaf_rn(c.h, x.l, __fmaf_rn(c.l, x.h, __fmaf_rn(c.h, x.h, -ph)));
+}
+
+__device__ __forceinline__ DF df_of(double x) {
+  DF r;
+  bits::split(x, r.h, r.l);
+  return r;
+}
+
+// c1 x1 + c2 x2 (+ c3 x3) as FP64: the products' high parts summed exactly,
+// the rest in FP32, hi + lo in one FP64 addition (the float -> double moves
+// are integer operations)
+__device__ __forceinline__ double df_dot2(const DF& c1, const DF& x1, const DF& c2, const DF& x2) {
+  float p1, q1, p2, q2, s, e;
+  df_prod(c1, x1, p1, q1);
+  df_prod(c2, x2, p2, q2);
+  two_sum(p1, p2, s, e);
+  return bits::widen(s) + bits::widen(__fadd_rn(e, __fadd_rn(q1, q2)));
+}
+__device__ __forceinline__ double df_dot3(const DF& c1, const DF& x1, const DF& c2, const DF& x2, const DF& c3,
+                                          const DF& x3) {
+  float p1, q1, p2, q2, p3, q3, s, e, s2, e2;
+  df_prod(c1, x1, p1, q1);
+  df_prod(c2, x2, p2, q2);
+  df_prod(c3, x3, p3, q3);
+  two_sum(p1, p2, s, e);
+  two_sum(s, p3, s2, e2);
+  return bits::widen(s2) + bits::widen(__fadd_rn(__fadd_rn(e, e2), __fadd_rn(q1, __fadd_rn(q2, q3))));
+}
+
+__device__ __forceinline__ DF shfl_df(const DF& x, int m) {
+  return DF{__shfl_xor_sync(0xffffffffu, x.h, m), __shfl_xor_sync(0xffffffffu, x.l, m)};
+}
+
+__global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict__ v, const cd* __restrict__ g,
+                                                            cd* __restrict__ u, cd* __restrict__ w,
+                                                            cd* __restrict__ ox, cd* __restrict__ oz,
+                                                            const double* __restrict__ iapha,
+                                                            const double* __restrict__ ibeta, Dims d) {
+  const long modes = d.modes(), ncols = 2 * modes;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int comp = (int)(t & 1), par = (int)((t >> 1) & 1);
+  const long mt = t >> 2;
+  const bool in = mt < modes;  // every lane takes part in the shuffles
+  const long m = in ? mt : 0;
+  const long col = 2 * m + comp;
+  // not a channel's (0,0) mode nor its spanwise Nyquist slot
+  const bool live = in && (m % d.chm) > 0 && ((m % d.chm) / d.KX) != d.NYQ;
+  double sak = 0.0, sbk = 0.0, sa = 0.0, sb = 0.0;
+  if (live) {
+    // (i z)_re = -z_im, (i z)_im = z_re: the sign s of the partner term
+    const double s = comp ? 1.0 : -1.0;
+    const double a = iapha[m % d.KX], b = ibeta[m / d.KX], ik2 = 1.0 / (a * a + b * b);
+    sa = s * a;
+    sb = s * b;
+    sak = sa * ik2;
+    sbk = sb * ik2;
+  }
+  const DF c_ak = df_of(sak), c_bk = df_of(sbk), c_a = df_of(sa), c_b = df_of(sb);
+  const DF c_nak = DF{-c_ak.h, -c_ak.l}, c_nbk = DF{-c_bk.h, -c_bk.l}, c_nb = DF{-c_b.h, -c_b.l};
+  const double* vd = reinterpret_cast<const double*>(v);
+  const double* gd = reinterpret_cast<const double*>(g);
+  double* ud = reinterpret_cast<double*>(u);
+  double* wd = reinterpret_cast<double*>(w);
+  double* oxd = reinterpret_cast<double*>(ox);
+  double* ozd = reinterpret_cast<double*>(oz);
+  const int N = d.N;
+  const int ktop = ((N - par) & ~1) | par;  // the largest k <= N with k = par (mod 2)
+  const int nsteps = N / 2 + 1;             // the even chain's rows N, N-2, ..., 0 (N is even)
+  // this chain's Dv, D^2 v, Dg at k + 2; the other chain's Dv at k + 1 and
+  // v, g at row k + 1
+  const DF zero{0.f, 0.f};
+  DF dv2 = zero, d2v2 = zero, dg2 = zero, dvx = zero, vu = zero, gu = zero;
+  for (int s0 = 0; s0 < nsteps; s0 += RC_PF) {
+    double vk[RC_PF], gk[RC_PF];
+#pragma unroll
+    for (int i = 0; i < RC_PF; ++i) {
+      const int k = min(max(ktop - 2 * (s0 + i), 0), N);
+      const size_t idx = (size_t)k * ncols + col;
+      vk[i] = vd[idx];
+      gk[i] = gd[idx];
+    }
+#pragma unroll
+    for (int i = 0; i < RC_PF; ++i) {
+      const int st = s0 + i;
+      if (st >= nsteps) break;
+      const int k = ktop - 2 * st;  // -1 for the odd chain's last step
+      const bool row = k >= 0;
+      const DF vv = df_of(vk[i]), gg = df_of(gk[i]);  // v, g at row k
+      // v, g at row k + 1: the even thread's current row for the odd thread,
+      // the odd thread's previous row for the even thread
+      const DF xv = shfl_df(vv, 2), xg = shfl_df(gg, 2);
+      if (par == 1) vu = xv, gu = xg;
+      const bool inner = row && k < N;
+      const float tk = inner ? (float)(2 * (k + 1)) : 0.f;  // exact; 0 gives the b term alone
+      DF dv = df_fma_int(tk, vu, dv2), dg = df_fma_int(tk, gu, dg2);
+      if (!inner) dv = zero, dg = zero;
+      if (par == 0) vu = xv, gu = xg;
+      // exchange Dv with the other chain: the odd thread needs the even
+      // thread's Dv of this step (row k + 1), the even thread keeps the odd
+      // thread's for its next step (also its row k + 1 then)
+      const DF xd = shfl_df(dv, 2);
+      if (par == 1) dvx = xd;
+      DF d2v = df_fma_int(tk, dvx, d2v2);
+      if (!inner) d2v = zero;
+      if (par == 0) dvx = xd;
+      dv2 = dv;
+      d2v2 = d2v;
+      dg2 = dg;
+      if (k == 0) {  // the k = 0 outputs of dz are halved (exact)
+        dv = DF{__fmul_rn(0.5f, dv.h), __fmul_rn(0.5f, dv.l)};
+        dg = DF{__fmul_rn(0.5f, dg.h), __fmul_rn(0.5f, dg.l)};
+        d2v = DF{__fmul_rn(0.5f, d2v.h), __fmul_rn(0.5f, d2v.l)};
+      }
+      // the partner component's values
+      const DF dv_p = shfl_df(dv, 1), dg_p = shfl_df(dg, 1), d2v_p = shfl_df(d2v, 1);
+      const DF v_p = shfl_df(vv, 1), g_p = shfl_df(gg, 1);
+      if (live && row) {
+        const size_t idx = (size_t)k * ncols + col;
+        ud[idx] = df_dot2(c_ak, dv_p, c_nbk, g_p);                  // sak Dv - sbk g
+        wd[idx] = df_dot2(c_bk, dv_p, c_ak, g_p);                   // sbk Dv + sak g
+        ozd[idx] = df_dot3(c_bk, dg_p, c_nak, d2v_p, c_a, v_p);     // sbk Dg - sak D^2 v + sa v
+        oxd[idx] = df_dot3(c_bk, d2v_p, c_ak, dg_p, c_nb, v_p);     // sbk D^2 v + sak Dg - sb v
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_inc_recover64: the FP64 form of k_inc_recover (above), four threads per
+// mode (lane = 4 mode + 2 parity + re/im),
+// grid (ceil(4 modes / RC_THREADS)); u, w, omega_x, omega_z from v and
+// omega_y (getvelocityandvorticity, REF:2347-2407) for every solved mode
+// (not (0,0), not the spanwise Nyquist slot):
+//   u = (i a Dv - i b g) / k^2,            w = (i b Dv + i a g) / k^2,
+//   omega_z = -Du + i a v = (i b Dg - i a D^2 v) / k^2 + i a v,
+//   omega_x =  Dw - i b v = (i b D^2 v + i a Dg) / k^2 - i b v.
 // The dz recurrences (b_0 halved on output) run in FP64 registers on
 // descending rows; the even-k and odd-k chains of Dv and Dg are independent,
 // so the pair of parity threads of a component runs them in lockstep (even
@@ -401,10 +590,8 @@ __global__ void __launch_bounds__(IncShape<MCH, RPT>::threads, IncShape<MCH, RPT
 // FP64 operations per element; the factors 2 (k + 1) are built by integer
 // operations; RC_PF steps of v and omega_y loaded ahead.
 // ---------------------------------------------------------------------------
-constexpr int RC_THREADS = 32;  // one warp: 1024 CTAs at 128^3, balanced over the SMs
-constexpr int RC_PF = 8;  // steps of v, omega_y loaded ahead of the recurrences
 
-__global__ void __launch_bounds__(RC_THREADS) k_inc_recover(const cd* __restrict__ v, const cd* __restrict__ g,
+__global__ void __launch_bounds__(RC_THREADS) k_inc_recover64(const cd* __restrict__ v, const cd* __restrict__ g,
                                                             cd* __restrict__ u, cd* __restrict__ w,
                                                             cd* __restrict__ ox, cd* __restrict__ oz,
                                                             const double* __restrict__ iapha,
@@ -517,6 +704,13 @@ int setup_solver_mixed(Handle* h) {
   if (!cuda_ok(h, cudaGetLastError(), "k_incr_rowexp") ||
       !cuda_ok(h, cudaStreamSynchronize(h->stream), "k_build_incr sync"))
     return CHF_E_CUDA;
+  // k_inc_recover's double-float form from 16 warps per SM on (measured on
+  // GB300: at 7 warps per SM, 128^3, it is issue-bound and 14% slower than
+  // the FP64 form; at 60, 384 x 193 x 384, 17% faster)
+  int nsm = 0;
+  if (!cuda_ok(h, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device), "SM count"))
+    return CHF_E_CUDA;
+  h->rec_df_rule = (4 * h->d.modes() + 31) / 32 >= 16L * nsm;
   return setup_inc_items(h);
 }
 
@@ -599,8 +793,12 @@ int launch_solve_mixed(Handle* h) {
     if (h->after_inc && !cuda_ok(h, cudaEventRecord(h->after_inc, st), "increment solve event")) return CHF_E_CUDA;
   }
   {
+    // the double-float form where the grid gives it enough warps to hide its
+    // longer instruction stream, the FP64 form otherwise (fixed per grid)
+    const bool df = h->tune.rec_form >= 0 ? h->tune.rec_form == 1 : h->rec_df_rule;
+    auto kern = df ? k_inc_recover : k_inc_recover64;
     prof_begin(h, K_INC_RECOVER, &ev);
-    k_inc_recover<<<(unsigned)((4 * modes + RC_THREADS - 1) / RC_THREADS), RC_THREADS, 0, st>>>(
+    kern<<<(unsigned)((4 * modes + RC_THREADS - 1) / RC_THREADS), RC_THREADS, 0, st>>>(
         h->f[F_V], h->f[F_OY], h->f[F_U], h->f[F_W], h->f[F_OX], h->f[F_OZ], h->iapha, h->ibeta, d);
     prof_end(h, K_INC_RECOVER, ev);
   }

@@ -192,12 +192,19 @@ int chf_autotune(chf_handle* h, int reps);
  * times when tuned), NUL-terminated in buf[0..len-1]. */
 int chf_tuning(const chf_handle* h, char* buf, int len);
 /* Sets one launch shape by name, in place of the rule or the autotuner's
- * choice (every shape computes the same results, bit for bit):
+ * choice (every shape but "recover_form" computes the same results, bit for
+ * bit):
  *   "inc_modes"    modes per CTA of the CHF_MIXED increment solve: 2 or 4
  *   "inc_columns"  its matrix columns per load batch: 2, 3 or 4
  *   "inc_rows"     its block rows per thread: 1 or 2 (2 with 2 or 3 columns)
  *   "inc_wide"     with one row per thread, every block row in one pass (1,
  *                  up to 416 threads) or 288-thread blocks that loop (0)
+ *   "recover_form" arithmetic of the CHF_MIXED recovery of u, w, omega_x,
+ *                  omega_z from v and omega_y: 0 FP64, 1 double-float
+ *                  (about 2^-44 of the largest term), -1 the rule (double-
+ *                  float where the grid has at least 16 x 32 x SMs / 4
+ *                  modes).  The one setting whose results differ (in the
+ *                  last bits); the autotuner leaves it alone.
  *   "kxb", "xr", "zl_c2v", "zl_curl"  lines per CTA of the shared-memory
  *                  FFT kernels: one of the shapes that fit the grid, or 0
  *                  for the launcher's rule

@@ -169,3 +169,33 @@ def test_mixed_from_reference_initial_field(chflow_lib, name, precision):
     b = run(cfg, st, precision, 5)
     errs = vel_err(b, a)
     assert max(errs.values()) < 1e-5, errs
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed/fp64 recovery", "mixed/double-float recovery"])
+@pytest.mark.parametrize("name", ["small16", "mixed_radix", "long_xz", "warp192"])
+def test_mixed_recovery_matches_fp64(chflow_lib, name, form):
+    """The recovery of u, w, omega_x, omega_z from v and omega_y after three
+    steps (k_inc_recover64 in FP64, k_inc_recover in double-float, about
+    2^-44; the FP64 path's own in k_solve) against getvelocityandvorticity in
+    FP64 NumPy applied to the same v and omega_y: to 1e-11 relative (FP32
+    arithmetic would leave about 1e-6)."""
+    cfg = CASES[name]
+    st = fields.turbulent_start_state(cfg, seed=21)
+    precision = form.split("/")[0]
+    with Channel(cfg, precision=precision) as g:
+        if precision == "mixed":
+            g.set_launch_shape("recover_form", 1 if "double" in form else 0)
+        g.upload_state(st)
+        g.getnonlinear()
+        g.solve()
+        g.step(3)
+        out = g.download_state()
+    ref = {k: v.copy() for k, v in out.items()}
+    fields.recover_velocity(cfg, ref)
+    nyq = cfg.nny // 2
+    for k in ("unp1", "wnp1", "omegaxnp1", "omegaznp1"):
+        a, b = out[k].copy(), ref[k].copy()
+        a[:, nyq, :] = 0.0
+        b[:, nyq, :] = 0.0
+        e = rel_l2(a, b)
+        assert e < 1e-11, (k, e)
