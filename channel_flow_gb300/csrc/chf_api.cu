@@ -63,6 +63,33 @@ static bool factors_235(int n) {
   return n == 1;
 }
 
+int upload_stage_twiddles(Handle* h) {
+  const bool f32 = mixed_front(h);
+  struct Tab {
+    void** dst;
+    const FftPlan* p;
+    bool f32;
+  } tabs[] = {{&h->stw_py, &h->py, f32},
+              {&h->stw_px, &h->px, f32},
+              {(void**)&h->stw_py64, &h->py64, false},
+              {(void**)&h->stw_px64, &h->px64, false}};
+  for (const Tab& t : tabs) {
+    if (!f32 && (t.dst == (void**)&h->stw_py64 || t.dst == (void**)&h->stw_px64)) continue;  // FP64 handle: py, px
+    const int L = t.p->L;
+    const size_t es = t.f32 ? sizeof(cf) : sizeof(cd);
+    if (!*t.dst && !cuda_ok(h, cudaMalloc(t.dst, es * (size_t)L), "stage twiddles")) return CHF_E_NOMEM;
+    const std::vector<cd> tw = twiddles(L);
+    std::vector<unsigned char> host(es * (size_t)L, 0);
+    if (t.f32)
+      fft_stage_twiddles<float>(*t.p, tw, reinterpret_cast<cf*>(host.data()));
+    else
+      fft_stage_twiddles<double>(*t.p, tw, reinterpret_cast<cd*>(host.data()));
+    if (!cuda_ok(h, cudaMemcpy(*t.dst, host.data(), host.size(), cudaMemcpyHostToDevice), "stage twiddles"))
+      return CHF_E_CUDA;
+  }
+  return CHF_OK;
+}
+
 std::vector<cd> twiddles(int L) {
   std::vector<cd> t(L);
   const double twopi = 8.0 * std::atan(1.0);
@@ -152,7 +179,7 @@ static void release(chf_handle* h) {
   for (auto& p : h->mean) cudaFree(p);
   void* ptrs[] = {h->iapha, h->ibeta, h->t0, h->t2, h->t4, h->k2vals, h->xinv, h->xmean,
                   h->group_start, h->group_modes, h->tw_py, h->tw_px, h->tw_z2, h->tw_zm,
-                  h->twf_py, h->twf_px, h->incm, h->incx, h->incr_exp, h->inc_items, h->phi, h->flow, h->stats_buf, h->pres_buf, h->phys_buf, h->tw_pxu, h->tw_pyu, h->group_re, h->ubphi_dev, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
+                  h->twf_py, h->twf_px, h->stw_py, h->stw_px, h->stw_py64, h->stw_px64, h->incm, h->incx, h->incr_exp, h->inc_items, h->phi, h->flow, h->stats_buf, h->pres_buf, h->phys_buf, h->tw_pxu, h->tw_pyu, h->group_re, h->ubphi_dev, h->wz, h->wy, h->scratch, h->dev_status, h->az1, h->az2,
                   h->agl, h->bimg, h->wz32, h->wy32, h->lc64, h->aexp1, h->aexp2, h->aexp3, h->bexp, h->z2_tail, h->gl_tail};
   for (void* p : ptrs) cudaFree(p);
   for (auto& p : h->pending) {
@@ -331,6 +358,7 @@ int chf_create(const chf_config* cfg, chf_handle** out) {
       return fail(CHF_E_CUDA);
   }
   apply_cached_tuning(h);  // a measured choice for this grid earlier in the process
+  if (upload_stage_twiddles(h) != CHF_OK) return fail(CHF_E_CUDA);
   int rc = setup_solver(h);
   if (rc != CHF_OK) return fail(rc);
   if (mixed_front(h)) {

@@ -211,6 +211,10 @@ int build_stack(chf_batch* b, Stack& S) {
   h->px = c0.px;
   h->py64 = c0.py64;
   h->px64 = c0.px64;
+  if (upload_stage_twiddles(h) != CHF_OK) {
+    b->err = "class set-up: " + h->err;
+    return CHF_E_CUDA;
+  }
   h->pz2 = c0.pz2;
   h->pzm = c0.pzm;
   if (!dup(b, &h->tw_py, c0.tw_py, c0.d.PY, "class twiddles") || !dup(b, &h->tw_px, c0.tw_px, c0.d.PX, "class twiddles") ||

@@ -169,6 +169,13 @@ struct Handle {
   // chf_pressure/chf_lamb on a mixed handle): the radix-8 rule and the launch
   // rules, never the FP32 tuning, so those results equal an FP64 handle's
   FftPlan py64, px64;
+  // stage twiddle tables of the two-buffer x / y stages (fft_stage_twiddles),
+  // PY / PX entries each: of py and px in the precision of the handle's
+  // x / y lines (cf for a mixed front, cd for CHF_FP64), and of py64 and px64
+  // in FP64 (mixed handles); rebuilt whenever a plan changes
+  // (upload_stage_twiddles)
+  void *stw_py = nullptr, *stw_px = nullptr;
+  cd *stw_py64 = nullptr, *stw_px64 = nullptr;
   cd *tw_py = nullptr, *tw_px = nullptr, *tw_z2 = nullptr, *tw_zm = nullptr;
   cf *twf_py = nullptr, *twf_px = nullptr;
 
@@ -310,6 +317,9 @@ int setup_solver(Handle* h);
 int setup_solver_mixed(Handle* h);
 // the work items of k_inc_solve from the handle's k^2 groups
 int setup_inc_items(Handle* h);
+// (re)writes the stage twiddle tables of h->py, h->px, h->py64, h->px64
+// (allocated on the first call); synchronous, outside stream capture
+int upload_stage_twiddles(Handle* h);
 bool xy_register_path(const Dims& d);
 int launch_yinv_fields(Handle* h, cf* wz, cf* wy, const cf* tw_py, int f0, int nf);
 int launch_xprod_yfwd(Handle* h, cf* wz, cf* wy, const cf* tw_py, const cf* tw_px);

@@ -206,6 +206,7 @@ int chf_autotune(chf_handle* h, int reps) {
     for (auto& c : cands) out.push_back(c);
     return out;
   };
+  bool tw_ok = true;
   const bool reg_xy = mixed_front(h) && xy_register_path(d);
   if (!reg_xy) {
     // two-buffer stages: the large-radix rule's orders, and radices up to 4
@@ -215,8 +216,11 @@ int chf_autotune(chf_handle* h, int reps) {
       for (auto& q : plan_candidates(make_plan(L))) c.push_back(q);
       return c;
     };
-    try_knob([&](const FftPlan& p) { h->py = p; }, with_current(h->py, xy_cands(d.PY)));
-    try_knob([&](const FftPlan& p) { h->px = p; }, with_current(h->px, xy_cands(d.PX)));
+    // a plan change rewrites the plan's stage twiddle table before it runs
+    try_knob([&](const FftPlan& p) { h->py = p, tw_ok = tw_ok && upload_stage_twiddles(h) == CHF_OK; },
+             with_current(h->py, xy_cands(d.PY)));
+    try_knob([&](const FftPlan& p) { h->px = p, tw_ok = tw_ok && upload_stage_twiddles(h) == CHF_OK; },
+             with_current(h->px, xy_cands(d.PX)));
     try_knob([&](int v) { h->tune.kxb = v; }, with_current(h->tune.kxb, shape_candidates(h, 0)));
     try_knob([&](int v) { h->tune.xr = v; }, with_current(h->tune.xr, shape_candidates(h, 1)));
   }
@@ -265,7 +269,7 @@ int chf_autotune(chf_handle* h, int reps) {
   // the captured step graphs hold the old shapes
   for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
   h->graphs.clear();
-  if (!good || best < 0) {
+  if (!good || best < 0 || !tw_ok) {
     if (h->err.empty()) h->err = "chf_autotune: a timed step failed";
     return CHF_E_CUDA;
   }

@@ -28,6 +28,11 @@ struct FftPlan {
   // shift (fft_plan_divisors): q = (umulhi(n, m) + n) >> s for 0 <= n < 2^31
   unsigned int nr_m[16], ns_m[16];
   int nr_s[16], ns_s[16];
+  // two-buffer stages (smem_fft_pp): offset of stage st's twiddles in the
+  // plan's stage table, which holds w^(r jm L / (Ns R)) at (r - 1) Ns + jm
+  // for r = 1 .. R - 1, jm = 0 .. Ns - 1 (L - 1 entries in all), so that the
+  // threads of a stage read consecutive entries
+  int twoff[16];
 };
 
 // m, s of the division by d (d >= 1) used in FftPlan: l = ceil(log2 d),
@@ -42,9 +47,12 @@ inline void fft_divisor(unsigned int d, unsigned int* m, int* s) {
 
 // fill the divisors of every stage of p (after R, Ns, nst, L are set)
 inline void fft_plan_divisors(FftPlan& p) {
+  int off = 0;
   for (int st = 0; st < p.nst; ++st) {
     fft_divisor((unsigned int)(p.L / p.R[st]), &p.nr_m[st], &p.nr_s[st]);
     fft_divisor((unsigned int)p.Ns[st], &p.ns_m[st], &p.ns_s[st]);
+    p.twoff[st] = off;
+    off += (p.R[st] - 1) * p.Ns[st];
   }
 }
 
@@ -301,44 +309,76 @@ __device__ void smem_fft(cplx<T>* s, int nlines, int lstride, const FftPlan& p,
 template <typename T, int SIGN, int R>
 __device__ __forceinline__ void fft_stage_pp(const cplx<T>* __restrict__ src, cplx<T>* __restrict__ dst,
                                              int nlines, int lstride, const FftPlan& p, int st,
-                                             const cplx<T>* __restrict__ tw) {
+                                             const cplx<T>* __restrict__ stab) {
   const int L = p.L, Ns = p.Ns[st];
   const int nr = L / R;
   const int total = nlines * nr;
-  const int twstep = L / (Ns * R);
   const unsigned int nrm = p.nr_m[st], nsm = p.ns_m[st];
   const int nrs = p.nr_s[st], nss = p.ns_s[st];
+  const cplx<T>* __restrict__ tws = stab + p.twoff[st];  // this stage's (r - 1) Ns + jm table
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     const int line = fft_div(t, nrm, nrs), j = t - line * nr;
     const int q = fft_div(j, nsm, nss), jm = j - q * Ns;
     cplx<T> v[R];
-    stage_load<T, SIGN, R>(src + line * lstride, j, nr, jm, twstep, tw, v);
+    const cplx<T>* in = src + line * lstride;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      cplx<T> x = in[j + r * nr];
+      if (r > 0) {
+        cplx<T> w = tws[(r - 1) * Ns + jm];
+        if (SIGN > 0) w.im = -w.im;
+        x = cmul(x, w);
+      }
+      v[r] = x;
+    }
+    if (R == 2) bfly2<T, SIGN>(v);
+    if (R == 3) bfly3<T, SIGN>(v);
+    if (R == 4) bfly4<T, SIGN>(v);
+    if (R == 5) bfly5<T, SIGN>(v);
+    if (R == 8) bfly8<T, SIGN>(v);
+    if (R == 9) bfly9<T, SIGN>(v);
+    if (R == 16) bfly16<T, SIGN>(v);
     cplx<T>* base = dst + line * lstride + q * Ns * R + jm;
 #pragma unroll
     for (int r = 0; r < R; ++r) base[r * Ns] = v[r];
   }
 }
 
+// stab: the plan's stage twiddle table (FftPlan::twoff, fft_stage_twiddles).
 template <typename T, int SIGN>
 __device__ cplx<T>* smem_fft_pp(cplx<T>* a, cplx<T>* b, int nlines, int lstride, const FftPlan& p,
-                                const cplx<T>* __restrict__ tw) {
+                                const cplx<T>* __restrict__ stab) {
   for (int st = 0; st < p.nst; ++st) {
     const int R = p.R[st];
-    if (R == 4) fft_stage_pp<T, SIGN, 4>(a, b, nlines, lstride, p, st, tw);
-    else if (R == 8) fft_stage_pp<T, SIGN, 8>(a, b, nlines, lstride, p, st, tw);
+    if (R == 4) fft_stage_pp<T, SIGN, 4>(a, b, nlines, lstride, p, st, stab);
+    else if (R == 8) fft_stage_pp<T, SIGN, 8>(a, b, nlines, lstride, p, st, stab);
     else if (R == 16) {  // FP32 lines only (16 FP64 values would not fit the registers)
-      if constexpr (sizeof(T) == 4) fft_stage_pp<T, SIGN, 16>(a, b, nlines, lstride, p, st, tw);
+      if constexpr (sizeof(T) == 4) fft_stage_pp<T, SIGN, 16>(a, b, nlines, lstride, p, st, stab);
     }
-    else if (R == 9) fft_stage_pp<T, SIGN, 9>(a, b, nlines, lstride, p, st, tw);
-    else if (R == 2) fft_stage_pp<T, SIGN, 2>(a, b, nlines, lstride, p, st, tw);
-    else if (R == 3) fft_stage_pp<T, SIGN, 3>(a, b, nlines, lstride, p, st, tw);
-    else fft_stage_pp<T, SIGN, 5>(a, b, nlines, lstride, p, st, tw);
+    else if (R == 9) fft_stage_pp<T, SIGN, 9>(a, b, nlines, lstride, p, st, stab);
+    else if (R == 2) fft_stage_pp<T, SIGN, 2>(a, b, nlines, lstride, p, st, stab);
+    else if (R == 3) fft_stage_pp<T, SIGN, 3>(a, b, nlines, lstride, p, st, stab);
+    else fft_stage_pp<T, SIGN, 5>(a, b, nlines, lstride, p, st, stab);
     __syncthreads();
     cplx<T>* t = a;
     a = b;
     b = t;
   }
   return a;
+}
+
+// Host side: the stage twiddle table of plan p (L - 1 entries, FftPlan::twoff)
+// from the length-L table tw[k] = exp(-2 pi i k / L), converted to T.
+template <typename T, typename V>
+inline void fft_stage_twiddles(const FftPlan& p, const V& tw, cplx<T>* out) {
+  for (int st = 0; st < p.nst; ++st) {
+    const int R = p.R[st], Ns = p.Ns[st], step = p.L / (Ns * R);
+    for (int r = 1; r < R; ++r)
+      for (int jm = 0; jm < Ns; ++jm) {
+        const auto& w = tw[(size_t)r * jm * step];
+        out[p.twoff[st] + (r - 1) * Ns + jm] = cplx<T>{(T)w.re, (T)w.im};
+      }
+  }
 }
 
 // Host-side check of the MB2 bound for a launch.

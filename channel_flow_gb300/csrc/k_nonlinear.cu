@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(ZC_THREADS) k_zc2v(SixPtr in, cd* __restrict__
 template <typename T>
 __global__ void __launch_bounds__(Y_THREADS, 4) k_yinv(const cplx<T>* __restrict__ wz, cplx<T>* __restrict__ wy,
                                                        Dims d, int kxb, const __grid_constant__ FftPlan py,
-                                                       const cplx<T>* __restrict__ tw) {
+                                                       const cplx<T>* __restrict__ stab) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s2 = s + kxb * (d.PY + 1);
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(Y_THREADS, 4) k_yinv(const cplx<T>* __restrict
     s[l * ls + slot] = src[(size_t)ky * d.KX + kx0 + l];
   }
   __syncthreads();
-  const cplx<T>* r = smem_fft_pp<T, +1>(s, s2, kxb, ls, py, tw);
+  const cplx<T>* r = smem_fft_pp<T, +1>(s, s2, kxb, ls, py, stab);
   cplx<T>* __restrict__ dst = wy + ((size_t)f * d.MP + p) * (size_t)d.PY * d.KX;
   for (int t = threadIdx.x; t < kxb * d.PY; t += blockDim.x) {
     int l = t % kxb, yp = t / kxb;
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(Y_THREADS, 4) k_yinv(const cplx<T>* __restrict
 // ---------------------------------------------------------------------------
 template <typename T, int XR>
 __global__ void __launch_bounds__(X_THREADS, 4) k_xprod(cplx<T>* __restrict__ wy, Dims d, T re_p,
-                                                        const __grid_constant__ FftPlan px, const cplx<T>* __restrict__ tw) {
+                                                        const __grid_constant__ FftPlan px, const cplx<T>* __restrict__ stab) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using C = cplx<T>;
   C* s = reinterpret_cast<C*>(smem_raw);
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(X_THREADS, 4) k_xprod(cplx<T>* __restrict__ wy
     }
   }
   __syncthreads();
-  s = smem_fft_pp<T, +1>(s, s2, XR * 3, ls, px, tw);  // s: the physical lines
+  s = smem_fft_pp<T, +1>(s, s2, XR * 3, ls, px, stab);  // s: the physical lines
   s2 = (s == reinterpret_cast<C*>(smem_raw)) ? s + XR * 3 * ls : reinterpret_cast<C*>(smem_raw);
   // products at every physical point; write (H1 + i H2) to pair 0, (H3 + 0i) to pair 1
   for (int t = threadIdx.x; t < XR * PX; t += blockDim.x) {
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(X_THREADS, 4) k_xprod(cplx<T>* __restrict__ wy
   }
   __syncthreads();
   // forward DFT of the 2 * XR lines holding (H1 + i H2) and H3
-  s = smem_fft_pp<T, -1>(s, s2, XR * 2, ls, px, tw);
+  s = smem_fft_pp<T, -1>(s, s2, XR * 2, ls, px, stab);
   for (int t = threadIdx.x; t < XR * KX; t += blockDim.x) {
     int k = t % KX, q = t / KX;
     long r = r0 + q;
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(X_THREADS, 4) k_xprod(cplx<T>* __restrict__ wy
 template <typename T>
 __global__ void __launch_bounds__(Y_THREADS, 4) k_yfwd(const cplx<T>* __restrict__ wy, cplx<T>* __restrict__ wz,
                                                        Dims d, int kxb, const __grid_constant__ FftPlan py,
-                                                       const cplx<T>* __restrict__ tw, T scale) {
+                                                       const cplx<T>* __restrict__ stab, T scale) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s2 = s + kxb * (d.PY + 1);
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(Y_THREADS, 4) k_yfwd(const cplx<T>* __restrict
     s[l * ls + yp] = src[(size_t)yp * d.KX + kx0 + l];
   }
   __syncthreads();
-  const cplx<T>* r = smem_fft_pp<T, -1>(s, s2, kxb, ls, py, tw);
+  const cplx<T>* r = smem_fft_pp<T, -1>(s, s2, kxb, ls, py, stab);
   cplx<T>* __restrict__ dst = wz + ((size_t)f * d.MP + p) * modes;
   for (int t = threadIdx.x; t < kxb * d.KY; t += blockDim.x) {
     int l = t % kxb, ky = t / kxb;
@@ -791,6 +791,9 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
   const bool own = (sizeof(T) == 8) == !mixed_front(h);
   const FftPlan& py = own ? h->py : h->py64;
   const FftPlan& px = own ? h->px : h->px64;
+  // the plans' stage twiddle tables (tw_py, tw_px serve the register path)
+  const cplx<T>* stw_py = own ? static_cast<const cplx<T>*>(h->stw_py) : reinterpret_cast<const cplx<T>*>(h->stw_py64);
+  const cplx<T>* stw_px = own ? static_cast<const cplx<T>*>(h->stw_px) : reinterpret_cast<const cplx<T>*>(h->stw_px64);
   if (sizeof(T) == 8)
     for (const FftPlan* p : {&py, &px})
       for (int s = 0; s < p->nst; ++s)
@@ -810,15 +813,15 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     dim3 grid(d.KX / kxb, d.MP, 6);
     cudaEvent_t ev;
     prof_begin(h, K_YINV, &ev);
-    k_yinv<T><<<grid, Y_THREADS, smem, st>>>(wz, wy, d, kxb, py, tw_py);
+    k_yinv<T><<<grid, Y_THREADS, smem, st>>>(wz, wy, d, kxb, py, stw_py);
     prof_end(h, K_YINV, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_yinv")) return CHF_E_CUDA;
   }
   {
-    int rc = xr == 8 ? run_xprod<T, 8>(h, wy, px, tw_px)
-           : xr == 4 ? run_xprod<T, 4>(h, wy, px, tw_px)
-           : xr == 2 ? run_xprod<T, 2>(h, wy, px, tw_px)
-                     : run_xprod<T, 1>(h, wy, px, tw_px);
+    int rc = xr == 8 ? run_xprod<T, 8>(h, wy, px, stw_px)
+           : xr == 4 ? run_xprod<T, 4>(h, wy, px, stw_px)
+           : xr == 2 ? run_xprod<T, 2>(h, wy, px, stw_px)
+                     : run_xprod<T, 1>(h, wy, px, stw_px);
     if (rc != CHF_OK) return rc;
   }
   {
@@ -828,7 +831,7 @@ int launch_xy(Handle* h, cplx<T>* wz, cplx<T>* wy, const cplx<T>* tw_py, const c
     T scale = (T)(1.0 / ((double)d.PX * (double)d.PY));
     cudaEvent_t ev;
     prof_begin(h, K_YFWD, &ev);
-    k_yfwd<T><<<grid, Y_THREADS, smem, st>>>(wy, wz, d, kxb, py, tw_py, scale);
+    k_yfwd<T><<<grid, Y_THREADS, smem, st>>>(wy, wz, d, kxb, py, stw_py, scale);
     prof_end(h, K_YFWD, ev);
     if (!cuda_ok(h, cudaGetLastError(), "k_yfwd")) return CHF_E_CUDA;
   }

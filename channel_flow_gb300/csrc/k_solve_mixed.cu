@@ -159,7 +159,10 @@ struct __align__(16) CoefHL {
 
 // S, C for one matrix entry (mh + ml) and one coefficient (ch + cl), real and
 // imaginary parts as a pair: S += mh ch, C += (mh ch - (s - S)) + mh cl + ml ch
-// (S against its offset sigma, so s - S is exact).  mh, ml broadcast.
+// (S against its offset sigma, so s - S is exact).  mh, ml broadcast.  The
+// compiler may fuse the product into the first sum (ptxas contracts packed
+// multiply-add pairs); u is then the error of that fused sum, rounded once,
+// and the bound is the same.
 __device__ __forceinline__ void sig_mac2(f32x2 mh, f32x2 ml, f32x2 ch, f32x2 cl, f32x2& S, f32x2& C) {
   const f32x2 s = add2(S, mul2(mh, ch));
   const f32x2 u = fma2(mh, ch, sub2(S, s));

@@ -111,3 +111,32 @@ def test_c3_dt5e4_diverges_at_the_same_step(chflow_lib, oracle_mod):
     assert calm.sum() >= 10
     rel = np.abs(eg[calm] - eo[calm]) / eo[calm]
     assert rel.max() < 1e-10, rel.max()
+
+
+def test_c4_time_step_bounded_at_5e5_not_1e4(chflow_lib):
+    """The 384 x 193 x 384 Re_tau 550 channel from its wall-law start: at
+    dt = 1e-4 the step (mixed path, whose nonlinear term carries the
+    instability the FP64 path shows too) grows without bound within 200
+    steps, at dt = 5e-5 the energy stays within 1% over 200 steps; the
+    workload runs at 5e-5."""
+    import bench
+    base = config.CONFIGS["c4_retau550_384"]
+    out = {}
+    for dt in (1e-4, 5e-5):
+        cfg = config.ChannelConfig(base.nnx, base.nny, base.nnz, base.aphi, base.beta, dt, base.re, base.re_p)
+        st = bench.start_state(cfg, seed=0)
+        with Channel(cfg, precision="mixed", zpad=300) as g:
+            g.upload_state(st)
+            g.getnonlinear()
+            g.solve()
+            e0 = g.diagnostics()["energy"]
+            hist = []
+            for _ in range(10):
+                g.step(20)
+                d = g.diagnostics()
+                hist.append(d["energy"] / e0 if d["finite"] else np.inf)
+                if not np.isfinite(hist[-1]):
+                    break
+        out[dt] = np.array(hist)
+    assert (out[1e-4] > 1e6).any(), out[1e-4]
+    assert np.all(np.abs(out[5e-5] - 1.0) < 0.01), out[5e-5]
