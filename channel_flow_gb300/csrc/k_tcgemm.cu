@@ -23,12 +23,13 @@
 // tensor-core FP32 accumulation of a level is EXACT.  B data are taken as
 // FP32 (FP64 coefficients are rounded to FP32 first: a relative error per
 // coefficient, not a flat floor).  Levels 0..NP-1 (ten or six products) go
-// to NP TMEM accumulators; the epilogue combines them exactly into one
-// 64-bit integer
+// to NP TMEM accumulators; the epilogue combines
 //   NP = 4:  t = acc_0 2^21 + acc_1 2^14 + acc_2 2^7 + acc_3,   |t| < 2^46
 //   NP = 3:  t = acc_0 2^16 + acc_1 2^8 + acc_2,                 |t| < 2^41
-// converted once (exactly to FP64, correctly rounded to FP32) and scaled by
-// 2^(f_m + e_c - 35) or 2^(f_m + e_c - 32).  What is dropped -- the higher
+// for FP64 outputs exactly, as one 64-bit integer converted once (the levels
+// can cancel), for FP32 outputs by FMAs on the levels (within about 2^-24 of
+// the maxima below), and scales by 2^(f_m + e_c - 35) or 2^(f_m + e_c - 32).
+// What is dropped -- the higher
 // levels and the digit remainders -- is below 2^-28 (NP = 4) or 2^-24
 // (NP = 3) of max|A row| * max|B column| per term, instead of 2^-24 of each
 // running FP32 sum.  The 4-plane format serves the transforms whose output
@@ -150,22 +151,27 @@ template <int NP>
 __host__ __device__ constexpr int fx_shift() { return NP == 4 ? 35 : 32; }
 template <typename OutT, int NP>
 __device__ __forceinline__ OutT fx_out(const uint32_t* acc, int n);
-// FP32: t = t_h 2^23 + t_l with |t_h| < 2^23 and 0 <= t_l < 2^23, both exact
-// in binary32, so one FMA rounds the exact t once (to nearest even); the
-// scaling by 2^n is two exact power-of-two multiplies
+// FP32: the levels are exact integers below 2^24 held in binary32, so the
+// sum is formed by FMAs on them directly, lowest level first (3 planes: two
+// FMAs, 4 planes: three), without conversions to integers (which run at a
+// quarter of the FMA rate).  Each FMA rounds once: the result is within one
+// unit in the last place of t where the levels do not cancel, and within
+// 2^-23 max|A row| max|B column| where they do (the format's own truncation
+// is 2^-24 of that); the scaling by 2^n is two exact power-of-two multiplies
 template <>
 __device__ __forceinline__ float fx_out<float, 4>(const uint32_t* acc, int n) {
-  const long long t = fx_level_sum<4>(acc);
-  const float v = __fmaf_rn(__int2float_rn((int)(t >> 23)), 8388608.0f, __int2float_rn((int)(t & 0x7fffff)));
+  const float v = __fmaf_rn(__uint_as_float(acc[0]), 2097152.0f,
+                            __fmaf_rn(__uint_as_float(acc[1]), 16384.0f,
+                                      __fmaf_rn(__uint_as_float(acc[2]), 128.0f, __uint_as_float(acc[3]))));
   const int h = n / 2;  // two factors keep each power of two in range
-  return v * __int_as_float((127 + h) << 23) * __int_as_float((127 + n - h) << 23);
+  return __fmul_rn(__fmul_rn(v, __int_as_float((127 + h) << 23)), __int_as_float((127 + n - h) << 23));
 }
 template <>
 __device__ __forceinline__ float fx_out<float, 3>(const uint32_t* acc, int n) {
-  const long long t = fx_level_sum<3>(acc);
-  const float v = __fmaf_rn(__int2float_rn((int)(t >> 23)), 8388608.0f, __int2float_rn((int)(t & 0x7fffff)));
+  const float v = __fmaf_rn(__uint_as_float(acc[0]), 65536.0f,
+                            __fmaf_rn(__uint_as_float(acc[1]), 256.0f, __uint_as_float(acc[2])));
   const int h = n / 2;  // two factors keep each power of two in range
-  return v * __int_as_float((127 + h) << 23) * __int_as_float((127 + n - h) << 23);
+  return __fmul_rn(__fmul_rn(v, __int_as_float((127 + h) << 23)), __int_as_float((127 + n - h) << 23));
 }
 // FP64: exact, built from the 64-bit integer by bit operations (off the
 // narrow FP64 pipe)
