@@ -13,8 +13,14 @@
 //   * the lines per CTA of the shared-memory FFT kernels (y: streamwise
 //     modes per CTA; x: rows per CTA; FP64 z: modes per CTA), every shape the
 //     launch rules accept;
-//   * the increment solve's thread mapping (CHF_MIXED): modes per pass
-//     (2 or 4) and matrix columns per load batch (2, 3 or 4).
+//   * the increment solve's thread mapping (CHF_MIXED): modes per CTA (2 or
+//     4), matrix columns per load batch (2, 3 or 4), block rows per thread
+//     (1 or 2) and, where one row per thread at 288 threads would loop, one
+//     pass in wide blocks or the loop.
+// Every candidate computes the same results bit for bit (a plan change
+// rewrites the plan's stage twiddle table first, with the same values).  The
+// recovery's arithmetic (chf_set_launch_shape "recover_form") is not
+// searched: its two forms differ in the last bits.
 // Each knob is tuned in turn (coordinate descent), every candidate timed as
 // whole time steps with CUDA events on the handle's stream, best of `reps`
 // runs; a candidate replaces the current choice only when it is at least 1%

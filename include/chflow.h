@@ -182,8 +182,10 @@ int chf_test_wait_timeout(chf_handle* h, int wait_us);
  * (poiseuilleflow.f90:100-112): times whole steps of the handle's state
  * (saved first and put back) for the candidate radix orders of the
  * shared-memory FFTs, lines per CTA of the FFT kernels and, for CHF_MIXED,
- * the increment solve's modes per pass and columns per load batch, and keeps
- * the fastest (each knob in turn; a candidate must be 1% faster).  reps:
+ * the increment solve's modes per CTA, columns per load batch, rows per
+ * thread and block width, and keeps the fastest (each knob in turn; a
+ * candidate must be 1% faster; every candidate computes the same results
+ * bit for bit).  reps:
  * timed runs per candidate (0: 3).  The choice is cached for the process:
  * later chf_create calls for the same device, grid, product grid and
  * precision start from it.  Synchronous; needs an uploaded state. */
