@@ -18,11 +18,13 @@
 // M = A^-1 (B - A) = A^-1 B - I maps coefficients to coefficients and has no
 // such cancellation (its rows sum to within ~10x of the result; at 128^3
 // the largest row sum is ~150, the median ~2).  A step is then
-//   k_inc_solve    one CTA per k^2 group: delta = M c (compensated FP32 on
-//                  (hi, lo) splits of M and c, summed against a power-of-two
-//                  offset) + A^-1 r (FP32), x = c + delta in FP64
+//   k_inc_solve    one CTA per run of at most 4 (or 2) modes of one k^2
+//                  group: delta = M c (compensated FP32 on (hi, lo) splits of
+//                  M and c, summed against a power-of-two offset) + A^-1 r
+//                  (FP32), x = c + delta in FP64
 //   k_inc_recover  u, w, omega_x, omega_z from v and omega_y (getvelocityandvorticity,
-//                  REF:2347-2407), FP64 recurrences, four threads per mode
+//                  REF:2347-2407), four threads per mode, in double-float
+//                  (k_inc_recover) or FP64 (k_inc_recover64)
 // FP64 arithmetic and double <-> float conversions share GB300's narrow FP64
 // pipe, so the conversions here are integer operations (f64bits.cuh).
 // The (0,0) mode (REF:401-474) stays with k_solve (FP64, one CTA).
@@ -40,9 +42,9 @@ namespace chf {
 namespace {
 
 constexpr int MV_THREADS = 288;  // threads over the 2 NZ rows of one group's four blocks
-// modes per pass (MCH) and matrix columns per load batch (CB) of
-// k_inc_solve are template parameters: the defaults 4 and 3, others picked
-// by the autotuner (chf_tune.cu)
+// modes per CTA (MCH), matrix columns per load batch (CB) and rows per thread
+// of k_inc_solve are template parameters: the defaults 4, 4 and 1, others
+// picked by the autotuner (chf_tune.cu)
 
 // Chebyshev derivative recurrence (dz, REF:570-599), descending in k:
 //   b_k = b_{k+2} + 2 (k+1) a_{k+1}   (b_0 halved on output)
@@ -173,9 +175,12 @@ __device__ __forceinline__ void sig_mac2(f32x2 mh, f32x2 ml, f32x2 ch, f32x2 cl,
 // Rows of one pass of k_inc_solve for NM staged modes: each thread owns RPT
 // adjacent rows of one of the four blocks (v even, v odd, omega even,
 // omega odd), so that every staged coefficient and AB2 value read from
-// shared memory serves RPT rows.  The arithmetic of a row does not depend on
-// RPT.
-template <int NM, int CB, int RPT>
+// shared memory serves RPT rows.  The staged values of entry e of mode q sit
+// at e MS + q (MS = the kernel's modes per CTA), so one address per column
+// reaches every mode by constant offsets; the matrix columns are walked by
+// element offsets advanced per batch, and only the last batch checks the
+// column count.  The arithmetic of a row does not depend on RPT.
+template <int NM, int MS, int CB, int RPT>
 __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g, const float2* __restrict__ Mg,
                                          const float* __restrict__ Xg, const SolveLayout& sl,
                                          const BlockOffsets& bo, int NZ, long modes, const cd* Cd,
@@ -188,24 +193,22 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
   const int slots = sev + sov + sew + sow;
   for (int t = threadIdx.x; t < slots; t += blockDim.x) {
     int b, slot, n;
-    size_t boff;
-    if (t < sev) { b = 0; slot = t; n = nev; boff = bo.ve; }
-    else if (t < sev + sov) { b = 1; slot = t - sev; n = nov; boff = bo.vo; }
-    else if (t < sev + sov + sew) { b = 2; slot = t - sev - sov; n = new_; boff = bo.we; }
-    else { b = 3; slot = t - sev - sov - sew; n = now_; boff = bo.wo; }
+    int boff;
+    if (t < sev) { b = 0; slot = t; n = nev; boff = (int)bo.ve; }
+    else if (t < sev + sov) { b = 1; slot = t - sev; n = nov; boff = (int)bo.vo; }
+    else if (t < sev + sov + sew) { b = 2; slot = t - sev - sov; n = new_; boff = (int)bo.we; }
+    else { b = 3; slot = t - sev - sov - sew; n = now_; boff = (int)bo.wo; }
     // offset of block b inside a mode's 2 NZ staged entries
     const int roff = b == 0 ? 0 : b == 1 ? nev : b == 2 ? NZ : NZ + new_;
     const int row0 = slot * RPT;
     bool live[RPT];
-    const float2* Mb[RPT];
-    const float* Xb[RPT];
+    int off[RPT];  // element offset of the row's current column in the group's blocks
     f32x2 S[RPT][NM], C[RPT][NM];  // (re, im) pairs
 #pragma unroll
     for (int i = 0; i < RPT; ++i) {
       live[i] = row0 + i < n;
       const int row = live[i] ? row0 + i : row0;  // a dead row reads its live neighbour
-      Mb[i] = Mg + boff + row;
-      Xb[i] = Xg + boff + row;
+      off[i] = boff + row;
       const int er = rexp[roff + row];
 #pragma unroll
       for (int q = 0; q < NM; ++q) {  // S starts at sigma of mode q for this row
@@ -222,39 +225,59 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
     for (int u = 0; u < CB; ++u)
 #pragma unroll
       for (int i = 0; i < RPT; ++i) {
-        ma[i][u] = u < n ? __ldg(Mb[i] + (size_t)u * n) : make_float2(0.f, 0.f);
-        xa[i][u] = u < n ? __ldg(Xb[i] + (size_t)u * n) : 0.f;
-      }
-    const f32x2* Rs2 = reinterpret_cast<const f32x2*>(Rs);
-    for (int c0 = 0; c0 < n; c0 += CB) {
-      float2 mb[RPT][CB];
-      float xb[RPT][CB];
-#pragma unroll
-      for (int u = 0; u < CB; ++u) {
-        const int c = c0 + CB + u;
-#pragma unroll
-        for (int i = 0; i < RPT; ++i) {
-          mb[i][u] = c < n ? __ldg(Mb[i] + (size_t)c * n) : make_float2(0.f, 0.f);
-          xb[i][u] = c < n ? __ldg(Xb[i] + (size_t)c * n) : 0.f;
-        }
+        ma[i][u] = u < n ? __ldg(Mg + off[i] + u * n) : make_float2(0.f, 0.f);
+        xa[i][u] = u < n ? __ldg(Xg + off[i] + u * n) : 0.f;
       }
 #pragma unroll
+    for (int i = 0; i < RPT; ++i) off[i] += CB * n;
+    const float4* cc = reinterpret_cast<const float4*>(Cs) + roff * MS;  // column 0, mode 0
+    const f32x2* rr = reinterpret_cast<const f32x2*>(Rs) + roff * MS;
+    auto columns = [&](const float2(&mc)[RPT][CB], const float(&xc)[RPT][CB], int ncol) {
+#pragma unroll
       for (int u = 0; u < CB; ++u) {
-        if (c0 + u < n) {
+        if (u < ncol) {
 #pragma unroll
           for (int q = 0; q < NM; ++q) {
-            const int si = q * 2 * NZ + roff + c0 + u;
-            const float4 ch = reinterpret_cast<const float4*>(Cs)[si];  // one 16-byte load
-            const f32x2 rr = Rs2[si];
+            const float4 ch = cc[u * MS + q];  // one 16-byte load
+            const f32x2 r2 = rr[u * MS + q];
 #pragma unroll
             for (int i = 0; i < RPT; ++i) {
-              const f32x2 mh = pk(ma[i][u].x, ma[i][u].x), ml = pk(ma[i][u].y, ma[i][u].y);
+              const f32x2 mh = pk(mc[i][u].x, mc[i][u].x), ml = pk(mc[i][u].y, mc[i][u].y);
               sig_mac2(mh, ml, pk(ch.x, ch.y), pk(ch.z, ch.w), S[i][q], C[i][q]);
-              C[i][q] = fma2(pk(xa[i][u], xa[i][u]), rr, C[i][q]);
+              C[i][q] = fma2(pk(xc[i][u], xc[i][u]), r2, C[i][q]);
             }
           }
         }
       }
+    };
+    int c0 = 0;
+    for (; c0 + CB <= n; c0 += CB) {
+      float2 mb[RPT][CB];
+      float xb[RPT][CB];
+      if (c0 + 2 * CB <= n) {  // the next batch is whole
+#pragma unroll
+        for (int u = 0; u < CB; ++u)
+#pragma unroll
+          for (int i = 0; i < RPT; ++i) {
+            mb[i][u] = __ldg(Mg + off[i] + u * n);
+            xb[i][u] = __ldg(Xg + off[i] + u * n);
+          }
+      } else {
+#pragma unroll
+        for (int u = 0; u < CB; ++u) {
+          const bool in = c0 + CB + u < n;
+#pragma unroll
+          for (int i = 0; i < RPT; ++i) {
+            mb[i][u] = in ? __ldg(Mg + off[i] + u * n) : make_float2(0.f, 0.f);
+            xb[i][u] = in ? __ldg(Xg + off[i] + u * n) : 0.f;
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < RPT; ++i) off[i] += CB * n;
+      columns(ma, xa, CB);
+      cc += CB * MS;
+      rr += CB * MS;
 #pragma unroll
       for (int u = 0; u < CB; ++u)
 #pragma unroll
@@ -263,6 +286,7 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
           xa[i][u] = xb[i][u];
         }
     }
+    columns(ma, xa, n - c0);  // the last n mod CB columns
     cd* dst = b < 2 ? v : g;
 #pragma unroll
     for (int i = 0; i < RPT; ++i) {
@@ -271,7 +295,7 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
       const int j = (b == 0 || b == 2) ? 2 * row : 2 * row + 1;
 #pragma unroll
       for (int q = 0; q < NM; ++q) {
-        const cd c0 = Cd[q * 2 * NZ + roff + row];
+        const cd c0v = Cd[q * 2 * NZ + roff + row];
         float Sv[2], Cv[2];
         upk(S[i][q], Sv[0], Sv[1]);
         upk(C[i][q], Cv[0], Cv[1]);
@@ -283,7 +307,7 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
           const float d = Sv[k] - __int_as_float((__float_as_int(Sv[k]) + 0x400000) & 0xff800000);
           // x = c + delta with two FP64 additions (the float -> double moves
           // are integer operations)
-          x[k] = ((k == 0 ? c0.re : c0.im) + bits::widen(d)) + bits::widen(Cv[k]);
+          x[k] = ((k == 0 ? c0v.re : c0v.im) + bits::widen(d)) + bits::widen(Cv[k]);
         }
         dst[(size_t)j * modes + s_mode[q]] = cd{x[0], x[1]};
       }
@@ -320,8 +344,8 @@ __global__ void __launch_bounds__(IncShape<MCH, RPT>::threads, IncShape<MCH, RPT
   const int N = d.N, NZ = d.NZ, ne = N / 2 + 1;
   const long modes = d.modes();
   cd* Cd = reinterpret_cast<cd*>(smem_raw);                   // [MCH][2 NZ] FP64 coefficients
-  CoefHL* Cs = reinterpret_cast<CoefHL*>(Cd + MCH * 2 * NZ);  // [MCH][2 NZ] their (hi, lo) splits
-  float2* Rs = reinterpret_cast<float2*>(Cs + MCH * 2 * NZ);  // [MCH][2 NZ] folded AB2 term
+  CoefHL* Cs = reinterpret_cast<CoefHL*>(Cd + MCH * 2 * NZ);  // [2 NZ][MCH] their (hi, lo) splits
+  float2* Rs = reinterpret_cast<float2*>(Cs + MCH * 2 * NZ);  // [2 NZ][MCH] folded AB2 term
   __shared__ int s_mode[MCH];
   __shared__ int s_cexp[MCH * 4];  // largest |hi| per (mode, block): float bits, then its exponent
   // work item: up to MCH modes of one k^2 group, from base
@@ -338,12 +362,12 @@ __global__ void __launch_bounds__(IncShape<MCH, RPT>::threads, IncShape<MCH, RPT
     for (int e = threadIdx.x; e < nm * 2 * NZ; e += blockDim.x) {
       const int q = e / (2 * NZ), i = e % (2 * NZ), f = i / NZ, k = i % NZ;
       const cd x = (f == 0 ? v : g)[(size_t)k * modes + s_mode[q]];
-      const int slot = q * 2 * NZ + f * NZ + ((k & 1) ? ne + k / 2 : k / 2);
-      Cd[slot] = x;
+      const int en = f * NZ + ((k & 1) ? ne + k / 2 : k / 2);  // entry within the mode
+      Cd[q * 2 * NZ + en] = x;
       CoefHL h;
       bits::split(x.re, h.hr, h.lr);
       bits::split(x.im, h.hi, h.li);
-      Cs[slot] = h;
+      Cs[en * MCH + q] = h;
       atomicMax(&s_cexp[4 * q + 2 * f + (k & 1)], __float_as_int(fmaxf(fabsf(h.hr), fabsf(h.hi))));
     }
     // the AB2 term in FP32 (X r is an FP32 product of an O(dt) term)
@@ -359,9 +383,10 @@ __global__ void __launch_bounds__(IncShape<MCH, RPT>::threads, IncShape<MCH, RPT
       const float qr = c3 * bits::narrow(hq.re) - c1 * bits::narrow(oq.re);
       const float qi = c3 * bits::narrow(hq.im) - c1 * bits::narrow(oq.im);
       const bool wall = (f == 0) ? (r < 2) : (r < 1);
-      float2* out = Rs + q * 2 * NZ + f * NZ;
-      out[r] = wall ? make_float2(0.f, 0.f) : make_float2(0.5f * (pr + qr), 0.5f * (pi + qi));
-      if (r < N / 2) out[ne + r] = wall ? make_float2(0.f, 0.f) : make_float2(0.5f * (pr - qr), 0.5f * (pi - qi));
+      float2* out = Rs + (size_t)f * NZ * MCH + q;  // entry e of mode q at e MCH + q
+      out[r * MCH] = wall ? make_float2(0.f, 0.f) : make_float2(0.5f * (pr + qr), 0.5f * (pi + qi));
+      if (r < N / 2)
+        out[(ne + r) * MCH] = wall ? make_float2(0.f, 0.f) : make_float2(0.5f * (pr - qr), 0.5f * (pi - qi));
     }
     __syncthreads();
     if (threadIdx.x < nm * 4) {  // max < 2^e
@@ -373,12 +398,12 @@ __global__ void __launch_bounds__(IncShape<MCH, RPT>::threads, IncShape<MCH, RPT
     __syncthreads();
     const signed char* rexp = rowexp + (size_t)grp * 2 * NZ;
     switch (nm) {
-      case 1: inc_rows<1, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
-      case 2: inc_rows<2, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      case 1: inc_rows<1, MCH, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
+      case 2: inc_rows<2, MCH, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp); break;
       default:
         if constexpr (MCH >= 4) {
-          if (nm == 3) inc_rows<3, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
-          else inc_rows<4, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
+          if (nm == 3) inc_rows<3, MCH, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
+          else inc_rows<4, MCH, CB, IncShape<MCH, RPT>::rows>(v, g, Mg, Xg, sl, bo, NZ, modes, Cd, Cs, Rs, s_mode, rexp, s_cexp);
         }
         break;
     }
