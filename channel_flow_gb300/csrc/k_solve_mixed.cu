@@ -236,15 +236,21 @@ __device__ __forceinline__ void inc_rows(cd* __restrict__ v, cd* __restrict__ g,
 #pragma unroll
       for (int u = 0; u < CB; ++u) {
         if (u < ncol) {
+          f32x2 mh[RPT], ml[RPT], xx[RPT];  // the column's entries, broadcast to (re, im)
+#pragma unroll
+          for (int i = 0; i < RPT; ++i) {
+            mh[i] = pk(mc[i][u].x, mc[i][u].x);
+            ml[i] = pk(mc[i][u].y, mc[i][u].y);
+            xx[i] = pk(xc[i][u], xc[i][u]);
+          }
 #pragma unroll
           for (int q = 0; q < NM; ++q) {
             const float4 ch = cc[u * MS + q];  // one 16-byte load
             const f32x2 r2 = rr[u * MS + q];
 #pragma unroll
             for (int i = 0; i < RPT; ++i) {
-              const f32x2 mh = pk(mc[i][u].x, mc[i][u].x), ml = pk(mc[i][u].y, mc[i][u].y);
-              sig_mac2(mh, ml, pk(ch.x, ch.y), pk(ch.z, ch.w), S[i][q], C[i][q]);
-              C[i][q] = fma2(pk(xc[i][u], xc[i][u]), r2, C[i][q]);
+              sig_mac2(mh[i], ml[i], pk(ch.x, ch.y), pk(ch.z, ch.w), S[i][q], C[i][q]);
+              C[i][q] = fma2(xx[i], r2, C[i][q]);
             }
           }
         }
@@ -359,8 +365,10 @@ __global__ void __launch_bounds__(IncShape<MCH, RPT>::threads, IncShape<MCH, RPT
     if (threadIdx.x < nm) s_mode[threadIdx.x] = group_modes[base + threadIdx.x];
     if (threadIdx.x < MCH * 4) s_cexp[threadIdx.x] = 0;
     __syncthreads();
-    for (int e = threadIdx.x; e < nm * 2 * NZ; e += blockDim.x) {
-      const int q = e / (2 * NZ), i = e % (2 * NZ), f = i / NZ, k = i % NZ;
+    // (mode, entry) loops without divisions by the run-time sizes
+    for (int q = 0; q < nm; ++q)
+    for (int i = threadIdx.x; i < 2 * NZ; i += blockDim.x) {
+      const int f = i >= NZ, k = i - f * NZ;
       const cd x = (f == 0 ? v : g)[(size_t)k * modes + s_mode[q]];
       const int en = f * NZ + ((k & 1) ? ne + k / 2 : k / 2);  // entry within the mode
       Cd[q * 2 * NZ + en] = x;
@@ -371,8 +379,9 @@ __global__ void __launch_bounds__(IncShape<MCH, RPT>::threads, IncShape<MCH, RPT
       atomicMax(&s_cexp[4 * q + 2 * f + (k & 1)], __float_as_int(fmaxf(fabsf(h.hr), fabsf(h.hi))));
     }
     // the AB2 term in FP32 (X r is an FP32 product of an O(dt) term)
-    for (int e = threadIdx.x; e < nm * 2 * ne; e += blockDim.x) {
-      const int q = e / (2 * ne), i = e % (2 * ne), f = i / ne, r = i % ne;
+    for (int q = 0; q < nm; ++q)
+    for (int i = threadIdx.x; i < 2 * ne; i += blockDim.x) {
+      const int f = i >= ne, r = i - f * ne;
       const long m = s_mode[q];
       const cd* H = f == 0 ? rv : rg;   // N^n (GL values)
       const cd* Ho = f == 0 ? uh : wh;  // N^{n-1}
