@@ -538,46 +538,20 @@ def ensemble_configs(n, seed=5):
     return out
 
 
-def ensemble_rate(n, device, precision="mixed_fp64solve", steps=20, warmup=4):
+def ensemble_rate(n, device, forms=("mixed_fp64solve", "mixed"), steps=20, warmup=4):
     """Channel-steps/s of n uneven channels advanced by one chf_batch (channels
     of one grid stacked into one set of buffers, one graph launch per pair of
     steps), of the same channels stepped one after another on one stream
-    (chf_step each, same precision), and of the plain FP64 path one channel
-    after another.  Host wall clock around the calls and a synchronize."""
+    (chf_step each, same precision), for each mixed form; and of the plain
+    FP64 path one channel after another.  Host wall clock around the calls and
+    a synchronize."""
     import torch
     from channel_flow_gb300 import Batch, Channel, fields
     cfgs = ensemble_configs(n)
     starts = [fields.turbulent_start_state(c, seed=100 + i) for i, c in enumerate(cfgs)]
-    t0 = time.perf_counter()
     zpads = [resolve_zpad("auto", c.nnz) for c in cfgs]
-    b = Batch(cfgs, precision=precision, zpad=zpads, device=device)
-    t_create = time.perf_counter() - t0
-    for ch, st in zip(b, starts):
-        ch.upload_state(st)
-        ch.getnonlinear()
-        ch.solve()
-    b.step(warmup)
-    b.synchronize()
-    t0 = time.perf_counter()
-    b.step(steps)
-    b.synchronize()
-    t_batch = time.perf_counter() - t0
-    # the same channels one after another on one stream
+    points = sum(c.points for c in cfgs)
     s = torch.cuda.Stream(device=device)
-    for ch in b:
-        ch.set_stream(s.cuda_stream)
-    for ch in b:
-        ch.step(2)
-    torch.cuda.synchronize(device)
-    t0 = time.perf_counter()
-    for ch in b:
-        ch.step(steps)
-    torch.cuda.synchronize(device)
-    t_seq = time.perf_counter() - t0
-    for ch in b:
-        ch.set_stream(None)
-    finite = all(ch.diagnostics()["finite"] for ch in b)
-    b.close()
     # the plain FP64 path, one channel after another
     f64 = []
     for c, st, z in zip(cfgs, starts, zpads):
@@ -596,18 +570,48 @@ def ensemble_rate(n, device, precision="mixed_fp64solve", steps=20, warmup=4):
     t_f64 = time.perf_counter() - t0
     for ch in f64:
         ch.close()
-    points = sum(c.points for c in cfgs)
-    return {"channels": n, "precision": precision, "steps": steps,
-            "workload": "nnz in {32,64,96}, nnx = nny in {32,64}, Re_tau U[100,300], 2pi x 2 x pi, dt 2e-4",
+    out = {"channels": n, "steps": steps,
+           "workload": "nnz in {32,64,96}, nnx = nny in {32,64}, Re_tau U[100,300], 2pi x 2 x pi, dt 2e-4",
+           "fp64_sequential_grid_point_steps_per_s": points * steps / t_f64,
+           "timing": "host wall clock around chf_batch_step + synchronize (the batch call gathers the channels "
+                     "into their classes and scatters them back once per call)", "forms": {}}
+    for precision in forms:
+        t0 = time.perf_counter()
+        b = Batch(cfgs, precision=precision, zpad=zpads, device=device)
+        t_create = time.perf_counter() - t0
+        for ch, st in zip(b, starts):
+            ch.upload_state(st)
+            ch.getnonlinear()
+            ch.solve()
+        b.step(warmup)
+        b.synchronize()
+        t0 = time.perf_counter()
+        b.step(steps)
+        b.synchronize()
+        t_batch = time.perf_counter() - t0
+        # the same channels one after another on one stream
+        for ch in b:
+            ch.set_stream(s.cuda_stream)
+        for ch in b:
+            ch.step(2)
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        for ch in b:
+            ch.step(steps)
+        torch.cuda.synchronize(device)
+        t_seq = time.perf_counter() - t0
+        for ch in b:
+            ch.set_stream(None)
+        finite = all(ch.diagnostics()["finite"] for ch in b)
+        b.close()
+        out["forms"][precision] = {
             "channel_steps_per_s": n * steps / t_batch,
             "grid_point_steps_per_s": points * steps / t_batch,
             "sequential_channel_steps_per_s": n * steps / t_seq,
             "batch_over_sequential": t_seq / t_batch,
-            "fp64_sequential_grid_point_steps_per_s": points * steps / t_f64,
             "batch_over_fp64_sequential": t_f64 / t_batch,
-            "create_s": t_create, "finite": finite,
-            "timing": "host wall clock around chf_batch_step + synchronize (the batch call gathers the channels "
-                      "into their classes and scatters them back once per call)"}
+            "create_s": t_create, "finite": finite}
+    return out
 
 
 def accuracy_vs_fp64(Channel, cfg, st, zpad, device, nsteps, forms=("mixed",)):
