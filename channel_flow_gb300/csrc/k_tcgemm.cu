@@ -372,15 +372,16 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_tc_gemm_fx(const __grid_const
       // decisions stay warp-uniform: tcgen05.ld needs the whole warp
       if (__shfl_sync(0xffffffffu, *fail, 0)) break;
       const uint32_t b = tc & 1u, tph = (tc >> 1) & 1u;
+      const int f = (int)(j / plan.ntiles), nt = (int)(j % plan.ntiles);
+      // column exponents of this warp's 32 columns, one per lane (loaded
+      // before the wait for the accumulators, so the load's latency overlaps it)
+      const int ecl = bexp[(size_t)f * plan.bexp_stride() + (size_t)nt * FX_NT + cbase + lane];
       if (!__all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull[b]), tph, wait_ns))) {
         if (lane == 0) *fail = 5;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const int f = (int)(j / plan.ntiles), nt = (int)(j % plan.ntiles);
       OutT* out = outs.p[f];
-      // column exponents of this warp's 32 columns, one per lane
-      const int ecl = bexp[(size_t)f * plan.bexp_stride() + (size_t)nt * FX_NT + cbase + lane];
 #pragma unroll
       for (int g2 = 0; g2 < 2; ++g2) {
         const int c0 = cbase + 16 * g2;
