@@ -103,7 +103,7 @@ struct Tuning {
   int xr = 0;       // (plane, y) rows per CTA of the shared-memory x transform
   int zl_c2v = 0;   // modes per CTA of the FP64 z transform to the product grid
   int zl_curl = 0;  // modes per CTA of the FP64 z transform + curl
-  int inc_mch = 4;  // modes per pass of the increment solve (2 or 4)
+  int inc_mch = 4;  // modes per CTA (work item) of the increment solve (2 or 4)
   int inc_cb = 4;   // matrix columns per load batch of the increment solve (2..4)
   int inc_rpt = 1;  // rows per thread of the increment solve (1 or 2; 2 with 2 or 3 columns)
   int inc_wide = 1; // one row per thread: every block row in one pass (1) or loop (0)
