@@ -72,6 +72,24 @@ def resolve_zpad(z, nnz):
         m += 1
 
 
+def max_over_ranks(x, dist, device):
+    """The largest x over the ranks (x itself without a process group): the
+    time of the slowest replica sets the job's time."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world, steps, seconds):
+    """Whole-job steps/s of `world` independent replicas that each took
+    `steps` steps in at most `seconds` (weak scaling: every rank advances its
+    own channel)."""
+    return world * steps / seconds
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -356,12 +374,8 @@ def main():
     ch.profile(False)
     prof_ms = sum(v[1] for v in prof.values()) / nprof
     diag = ch.diagnostics()
-    t_max = ms
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * args.steps / (t_max / 1e3)
+    t_max = max_over_ranks(ms, dist, f"cuda:{local}")
+    value = replica_rate(world, args.steps, t_max / 1e3)
     # ---- end to end through the C ABI with pinned host buffers: every step
     # uploads the module arrays, advances one step and downloads them
     host = {}
@@ -380,12 +394,8 @@ def main():
     for _ in range(ne2e):
         out = ch.step_host(host, 1)
     el = time.perf_counter() - t0
-    e2e_t = el
-    if dist:
-        t = torch.tensor([el], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_t = float(t.item())
-    e2e = {"value": world * ne2e / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": h2d,
+    e2e_t = max_over_ranks(el, dist, f"cuda:{local}")
+    e2e = {"value": replica_rate(world, ne2e, e2e_t), "unit": "steps/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": sum(a.nbytes for a in out.values()),
            "what": "chf_step_host(1) on pinned host module arrays: all 14 arrays up and down every step, "
                    "copies overlapped with the step"}
