@@ -33,7 +33,7 @@ def _rank_main(rank, world, port, out):
 
 def test_replicas_take_the_slowest_rank():
     world = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank_main, args=(world, free_port(), out), nprocs=world, join=True)
         res = dict(out)
