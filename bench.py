@@ -201,6 +201,37 @@ def kernel_work(cfg, zpad=0, precision="fp64"):
     return w
 
 
+# which pipe bounds each kernel's counted flops: the exact GEMMs' digit
+# products run on the bf16 tensor pipe; the curl recurrences, the recovery and
+# every kernel of the FP64 path count FP64 operations; the mixed path's FP32
+# FFT and product kernels are bound by HBM alone
+TENSOR_KERNELS = ("k_tc_gemm_z1", "k_tc_gemm_z2", "k_tc_gemm_gl")
+FP64_MIXED_KERNELS = ("k_curl", "k_inc_recover", "k_solve")
+
+
+def step_roofline(work, precision, ms_per_step, hbm_gbs, tensor_tflops, fp64_tflops):
+    """Whole-step roofline: T_roof = sum over the step's kernels of
+    max(bytes_k / BW_HBM, flops_k / peak_k), peak_k being the bf16 tensor rate
+    for the exact GEMMs and the FP64 rate for FP64 work; achieved =
+    T_roof / T_measured (1.0 = every kernel at its own bound, run back to
+    back).  `work` maps kernel -> (bytes, flops) per step."""
+    per = {}
+    total = 0.0
+    for k, (nb, nf) in work.items():
+        t_mem = nb / (hbm_gbs * 1e9)
+        if k in TENSOR_KERNELS:
+            t_fl, pipe = nf / (tensor_tflops * 1e12), "tensor"
+        elif precision == "fp64" or k in FP64_MIXED_KERNELS:
+            t_fl, pipe = nf / (fp64_tflops * 1e12), "fp64"
+        else:
+            t_fl, pipe = 0.0, "none"
+        t = max(t_mem, t_fl)
+        total += t
+        per[k] = {"roof_us": t * 1e6, "bound": "hbm" if t_mem >= t_fl else pipe}
+    return {"t_roof_ms": total * 1e3, "t_measured_ms": ms_per_step,
+            "achieved": total * 1e3 / ms_per_step, "kernels": per}
+
+
 # --------------------------------------------------------------------------
 # clocks during the timed region
 # --------------------------------------------------------------------------
@@ -456,10 +487,17 @@ def main():
                 "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback",
                 "traffic": traffic, "algorithmic_bytes": nbytes, "avg_launch_ms": avg_ms}
+    fp64_peak = fp64_peak_tflops(torch, f"cuda:{local}")
+    # the step's kernels that ran in the timed graph (the (0,0) mode solve runs
+    # beside k_inc_solve and moves no operator bytes)
+    ran = {k: v for k, v in work.items() if prof.get(k, (0, 0))[0] > 0}
+    roofline["step"] = step_roofline(ran, args.precision, t_max / args.steps, hbm_peak,
+                                     peaks.get("bf16_tflops_sustained", 1700.0), fp64_peak)
+    roofline["step"]["peaks"] = ("HBM: MEASURED_PEAKS.json hbm_gbs; tensor: bf16_tflops_sustained "
+                                 "(measured); FP64: cuBLAS DGEMM 4096^3 measured in this run")
     if args.precision == "fp64":
         # the FP64 path's kernels are bound by the FP64 pipe: their rate against
         # the measured DGEMM peak
-        fp64_peak = fp64_peak_tflops(torch, f"cuda:{local}")
         roofline.update({"fp64_tflops_achieved": nflops / (avg_ms / 1e3) / 1e12,
                          "fp64_tflops_peak": fp64_peak,
                          "fp64_peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
