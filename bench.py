@@ -138,7 +138,7 @@ def workload_name(cfg):
 # --------------------------------------------------------------------------
 # algorithmic work per kernel launch (bytes read + written once, FP64 flops)
 # --------------------------------------------------------------------------
-def kernel_work(cfg, zpad=0, precision="fp64"):
+def kernel_work(cfg, zpad=0, precision="fp64", recover_df=False):
     N = cfg.nnz
     NZ = N + 1
     KX, KY = cfg.nnx // 2, cfg.nny
@@ -193,11 +193,16 @@ def kernel_work(cfg, zpad=0, precision="fp64"):
     w["k_tc_split_z2"] = (3 * MP * cols * 4 + 3 * kp(MP) * cols * img, 0)
     # Z2 and GL run one 128-row tile (rows 0..N-1); row N is formed beside the digits
     w["k_tc_gemm_z2"] = (3 * kp(MP) * cols * img + 3 * N * cols * 8, 3 * 10 * 2 * N * cols * kp(MP))
-    w["k_curl"] = (3 * NZ * cols * 8 + 2 * kp(NZ) * cols * img, nsolve * NZ * 12)
+    # FP64 flops, an FMA counting 2 as in the DGEMM rate: per (mode, re/im,
+    # row) 7 for h_v (the G product, the recurrence, k^2 H2 + D G), 3 for h_g
+    w["k_curl"] = (3 * NZ * cols * 8 + 2 * kp(NZ) * cols * img, modes * NZ * 2 * 10)
     w["k_tc_gemm_gl"] = (2 * kp(NZ) * cols * img + 2 * N * cols * 8, 2 * 10 * 2 * N * cols * kp(NZ))
     w["k_inc_solve"] = (nk2 * stride * (8 + 4) + 8 * NZ * modes * c,
                         nsolve * 2 * (2 * (ne * ne + no * no)) * 2)
-    w["k_inc_recover"] = (6 * NZ * modes * c, nsolve * NZ * 26)
+    # FP64 flops per (mode, re/im, row): 3 recurrence FMAs and the four
+    # outputs (16) in the FP64 form; the double-float form leaves one FP64
+    # addition per output
+    w["k_inc_recover"] = (6 * NZ * modes * c, nsolve * NZ * 2 * (4 if recover_df else 22))
     return w
 
 
@@ -469,7 +474,7 @@ def main():
             dist.destroy_process_group()
         return 0
     # ---- roofline of the dominant kernel
-    work = kernel_work(cfg, args.zpad, args.precision)
+    work = kernel_work(cfg, args.zpad, args.precision, recover_df="double-float recovery" in tuning)
     kname = max((k for k in prof if prof[k][0] > 0), key=lambda k: prof[k][1])
     launches, kms = prof[kname]
     avg_ms = kms / launches

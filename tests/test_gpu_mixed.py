@@ -18,6 +18,8 @@ CASES = {
     "warp192": config.small(nnx=128, nny=128, nnz=16, aphi=2.0, beta=2.0 / 3.0, dt=2e-4, re=180.0, re_p=1.0),
     "long_xz": config.small(nnx=384, nny=8, nnz=192, aphi=1.0, beta=0.5, dt=2e-4, re=550.0, re_p=1.0),
     "long_y": config.small(nnx=8, nny=384, nnz=16, aphi=1.0, beta=0.5, dt=2e-4, re=550.0, re_p=1.0),
+    # 257 wall-normal points: K = 272 digit rows in Z1 (four planes), 513-point product grid
+    "tall_z": config.small(nnx=8, nny=8, nnz=256, aphi=1.0, beta=0.5, dt=1e-4, re=550.0, re_p=1.0),
 }
 VEL = ("unp1", "vnp1", "wnp1")
 
