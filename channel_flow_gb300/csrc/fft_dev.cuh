@@ -218,14 +218,16 @@ __device__ __forceinline__ void bfly16(cplx<T>* v) {
 }
 
 // One stage helper: load R inputs of butterfly (line, j), twiddle, butterfly.
+// The first stage (Ns = 1, jm = 0) has every twiddle equal to 1 (tw[0] is
+// exactly (1, 0)) and skips them.
 template <typename T, int SIGN, int R>
 __device__ __forceinline__ void stage_load(const cplx<T>* __restrict__ base, int j, int nr, int jm,
                                            int twstep, const cplx<T>* __restrict__ tw,
-                                           cplx<T>* v) {
+                                           cplx<T>* v, bool twiddled) {
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     cplx<T> x = base[j + r * nr];
-    if (r > 0) {
+    if (r > 0 && twiddled) {
       cplx<T> w = tw[r * jm * twstep];
       if (SIGN > 0) w.im = -w.im;
       x = cmul(x, w);
@@ -263,7 +265,7 @@ __device__ __forceinline__ void fft_stage(cplx<T>* s, int nlines, int lstride, c
     if (t < total) {
       const int line = fft_div(t, nrm, nrs), j = t - line * nr;
       const int q = fft_div(j, nsm, nss), jm = j - q * Ns;
-      stage_load<T, SIGN, R>(s + line * lstride, j, nr, jm, twstep, tw, v[b]);
+      stage_load<T, SIGN, R>(s + line * lstride, j, nr, jm, twstep, tw, v[b], Ns > 1);
       off[b] = line * lstride + q * Ns * R + jm;
     }
   }
@@ -324,7 +326,7 @@ __device__ __forceinline__ void fft_stage_pp(const cplx<T>* __restrict__ src, cp
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       cplx<T> x = in[j + r * nr];
-      if (r > 0) {
+      if (r > 0 && Ns > 1) {  // the first stage's twiddles are all 1
         cplx<T> w = tws[(r - 1) * Ns + jm];
         if (SIGN > 0) w.im = -w.im;
         x = cmul(x, w);
