@@ -158,7 +158,9 @@ static std::string validate(const chf_config* c) {
   if (c->nnx < 4 || c->nnx % 4) return "nnx must be a positive multiple of 4";
   if (c->nny < 4 || c->nny % 4) return "nny must be a positive multiple of 4";
   if (c->nnz < 4 || c->nnz % 2) return "nnz must be even and >= 4";
-  if (c->nnz > 382) return "nnz must be <= 382";
+  // the solve kernels hold a column of nnz + 1 <= 256 values in one warp
+  // (k_solve.cu: WD_EMAX) and two chunks of 2 nnz-point lines in a CTA
+  if (c->nnz > 254) return "nnz must be <= 254";
   if (!(c->aphi > 0) || !(c->beta > 0)) return "aphi and beta must be positive";
   if (!(c->dt > 0) || !(c->re > 0)) return "dt and re must be positive";
   if (!std::isfinite(c->re_p)) return "re_p must be finite";

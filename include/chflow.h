@@ -55,7 +55,8 @@ extern "C" {
 typedef struct chf_config {
   int nnx;        /* streamwise points, paraandcons.f90:5  (multiple of 4) */
   int nny;        /* spanwise points, paraandcons.f90:6    (multiple of 4) */
-  int nnz;        /* Chebyshev degree, paraandcons.f90:7   (even)          */
+  int nnz;        /* Chebyshev degree, paraandcons.f90:7   (even, 4..254:
+                     the solve holds a column of nnz + 1 values in one warp) */
   double aphi;    /* streamwise box 2*pi*aphi, paraandcons.f90:22 */
   double beta;    /* spanwise box 2*pi*beta, paraandcons.f90:22   */
   double dt;      /* time step, paraandcons.f90:23 */

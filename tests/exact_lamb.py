@@ -73,3 +73,50 @@ def lamb(cfg, st):
     h2 = oz * u - ox * w
     h3 = ox * v - oy * u
     return _to_spec(h1, mats), _to_spec(h2, mats), _to_spec(h3, mats)
+
+
+def _to_spec_ld(f, mats):
+    """_to_spec without the final rounding: clongdouble [n][ky][kx]."""
+    Tz, Wz, Ey, Fy, Ex, Fx = mats
+    s = np.einsum("kX,pYX->pYk", Fx, f.astype(np.clongdouble))
+    s = np.einsum("yY,pYk->pyk", Fy, s)
+    return np.einsum("np,pyk->nyk", Wz, s)
+
+
+def nonlinear_histories(cfg, st):
+    """rhsvn and rhsomegayn as getnonlinear leaves them (poiseuilleflow.f90:
+    1502-1609): h_v = k^2 H2 + i a D H1 + i b D H3 and h_g = i a H3 - i b H1
+    (D the Chebyshev derivative of dz, :570-599), as values at the Gauss-
+    Lobatto points cos(pi k / N), all in longdouble from the products on;
+    rounded to FP64 once, in the field layout [n][ky][2 kx]."""
+    mats = _mats(cfg)
+    P = {k: _to_phys(st[k], mats) for k in ("unp1", "vnp1", "wnp1", "omegaxnp1", "omegaynp1", "omegaznp1")}
+    u, v, w = P["unp1"], P["vnp1"], P["wnp1"]
+    ox, oy, oz = P["omegaxnp1"], P["omegaynp1"], P["omegaznp1"]
+    h1 = _to_spec_ld((oy * w - LD(cfg.re_p)) - oz * v, mats)
+    h2 = _to_spec_ld(oz * u - ox * w, mats)
+    h3 = _to_spec_ld(ox * v - oy * u, mats)
+    N = cfg.nnz
+    D = np.zeros((N + 1, N + 1), dtype=LD)
+    for i in range(N):
+        for j in range(i + 1, N + 1):
+            if (i + j) % 2:
+                D[i, j] = LD(j) if i == 0 else LD(2 * j)
+    ia, ib = fields.wavenumbers(cfg)
+    a = np.asarray(ia, dtype=LD)[None, None, :]
+    b = np.asarray(ib, dtype=LD)[None, :, None]
+    k2 = a * a + b * b
+    d1 = np.einsum("ij,jyx->iyx", D, h1)
+    d3 = np.einsum("ij,jyx->iyx", D, h3)
+    hv = k2 * h2 + 1j * a * d1 + 1j * b * d3
+    hg = 1j * a * h3 - 1j * b * h1
+    n = np.arange(N + 1, dtype=LD)
+    G = np.cos(LD(np.pi) * np.outer(n, n) / N)  # [k][j]: T_j at cos(pi k / N)
+    out = []
+    for h in (hv, hg):
+        g = np.einsum("kj,jyx->kyx", G, h)
+        o = np.empty(g.shape[:2] + (2 * g.shape[2],))
+        o[:, :, 0::2] = np.asarray(g.real, dtype=np.float64)
+        o[:, :, 1::2] = np.asarray(g.imag, dtype=np.float64)
+        out.append(o)
+    return out[0], out[1]

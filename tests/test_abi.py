@@ -34,7 +34,7 @@ def _create(lib, c):
 
 
 @pytest.mark.parametrize("field,value,msg", [
-    ("nnx", 30, "nnx"), ("nny", 6, "nny"), ("nnz", 33, "nnz"), ("nnz", 2, "nnz"),
+    ("nnx", 30, "nnx"), ("nny", 6, "nny"), ("nnz", 33, "nnz"), ("nnz", 2, "nnz"), ("nnz", 256, "nnz"),
     ("dt", 0.0, "dt"), ("re", -1.0, "re"), ("aphi", 0.0, "aphi"), ("precision", 7, "precision"),
     ("zpad", 20, "zpad"), ("nnx", 28, "nnx"),
 ])

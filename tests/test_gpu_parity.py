@@ -15,9 +15,9 @@ import pytest
 
 from channel_flow_gb300 import Channel, ChannelError, config, fields
 from channel_flow_gb300.fields import FIELD_NAMES, MEAN_NAMES
-from exact_lamb import lamb
+from exact_lamb import lamb, nonlinear_histories
 from exact_mean import mean_h1
-from parity import PROG, bad_parts, check, compare, oracle_sensitivity, worst
+from parity import PROG, bad_parts, check, compare, oracle_sensitivity, rel_l2, split, worst
 
 pytestmark = pytest.mark.gpu
 
@@ -32,7 +32,26 @@ CASES = {
     # and 768-point z lines (fewer lines per CTA), and 576-point y lines
     "long_xz": config.small(nnx=384, nny=8, nnz=192, aphi=1.0, beta=0.5, dt=2e-4, re=550.0, re_p=1.0),
     "long_y": config.small(nnx=8, nny=384, nnz=16, aphi=1.0, beta=0.5, dt=2e-4, re=550.0, re_p=1.0),
+    # the largest wall-normal degree chf_create accepts (251 points, 500-point z lines)
+    "tall_z": config.small(nnx=8, nny=8, nnz=250, aphi=1.0, beta=0.5, dt=1e-4, re=550.0, re_p=1.0),
 }
+
+
+# Cases where the reference algorithm (the oracle) is itself far from exact
+# in the nonlinear histories: at nnz = 250 its rhsvn / rhsomegayn are 2.4e-8 /
+# 7.5e-8 from an extended-precision evaluation (the derivative of the curl
+# multiplies the products' rounding by up to 2 nnz) and its plane-averaged H1
+# 1.8e-6.  There the GPU's histories are held to that evaluation instead, at
+# least as accurate as the oracle's (test_mean_lamb_accuracy for the (0,0)
+# mode).
+EXACT_HIST = ("tall_z",)
+
+# Per-case bar of the prognostic arrays after one solve.  tall_z: the v
+# operator's condition number is 3.4e9 at nnz = 250 (4.3e8 at 192); the
+# oracle's explicit FP64 inverse leaves |A X - I| = 1.8e-10, so two
+# independent eliminations (full LU here, even/odd Gauss-Jordan on the GPU)
+# agree in v to about 1e-9 (omega_y, condition 28, to 1e-15).
+SOLVE_TOL = {"tall_z": 1e-8}
 
 
 def exact_zpad(n):
@@ -91,7 +110,8 @@ def test_getnonlinear_matches_oracle(chflow_lib, oracle_mod, name):
     for k in ("omegaxnp1", "omegaznp1"):
         gs.pop(k)
         os_.pop(k)
-    names = tuple(k for k in os_)
+    hist = ("rhsvn", "rhsomegayn", "clamb1n", "clamb3n") if name in EXACT_HIST else ()
+    names = tuple(k for k in os_ if k not in hist)
     errs = compare(gs, os_, names=names)
     bad = bad_parts(errs, 1e-10, 1e-7)
     if bad:
@@ -100,6 +120,12 @@ def test_getnonlinear_matches_oracle(chflow_lib, oracle_mod, name):
         floor = oracle_sensitivity(oracle_mod, cfg, st, lambda o: o.getnonlinear(), names=names)
         bad = bad_parts(errs, 1e-10, 1e-7, floor)
     assert not bad, (bad, errs)
+    if hist:
+        ev, eg = nonlinear_histories(cfg, st)
+        for k, ex in (("rhsvn", ev), ("rhsomegayn", eg)):
+            e_g = rel_l2(split(gs[k], k)[k], split(ex, k)[k])
+            e_o = rel_l2(split(os_[k], k)[k], split(ex, k)[k])
+            assert e_g <= max(2.0 * e_o, 1e-12), (k, e_g, e_o)
 
 
 @pytest.mark.parametrize("name", ["small16", "c2_os", "mixed_radix"])
@@ -132,7 +158,7 @@ def test_solve_matches_oracle(chflow_lib, oracle_mod, name):
     g.upload_state(mid)
     o.solve()
     g.solve()
-    check(g.download_state(), o.get_state(), 1e-10, 1e-7)
+    check(g.download_state(), o.get_state(), SOLVE_TOL.get(name, 1e-10), 1e-7)
 
 
 # Per-case bar for the prognostic arrays after several steps.  long_xz: the
@@ -272,7 +298,7 @@ def test_full_size_two_steps(chflow_lib, oracle_mod):
     check(g.download_state(), o.get_state(), 1e-10, 1e-6)
 
 
-@pytest.mark.parametrize("name", ["c1_32", "c2_os", "small16", "long_xz"])
+@pytest.mark.parametrize("name", ["c1_32", "c2_os", "small16", "long_xz", "tall_z"])
 def test_mean_lamb_accuracy(chflow_lib, oracle_mod, name):
     """H1(0,0) (left in omegaxnp1 by getnonlinear, REF:1489-1496) against its
     extended-precision value: the GPU must be at least as accurate as the
