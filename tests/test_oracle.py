@@ -132,3 +132,47 @@ def test_golden_steps(oracle_mod, name):
     ref = {k[3:]: g[k] for k in g.files if k.startswith("s1_")}
     errs = compare(o.get_state(), ref, names=FIELD_NAMES + MEAN_NAMES)
     assert max(errs.values()) < 1e-12, errs
+
+
+TALL = config.small(nnx=8, nny=8, nnz=250, aphi=1.0, beta=0.5, dt=1e-4, re=550.0, re_p=1.0)
+
+
+@pytest.mark.parametrize("cfg,bar", [(SMALL, 1e-12), (config.CONFIGS["c1_poiseuille_32"], 1e-12)])
+def test_extended_histories_match_oracle(oracle_mod, cfg, bar):
+    """The extended-precision curl and Gauss-Lobatto values (the reference the
+    GPU histories are held to at the largest degree) agree with the oracle's
+    getnonlinear where both are accurate."""
+    from exact_lamb import nonlinear_histories
+    from parity import rel_l2, split
+    st = fields.reference_like_state(cfg, seed=3, epsilon=0.3, noise=0.02, gamma=5.0)
+    ev, eg = nonlinear_histories(cfg, st)
+    o = oracle_mod.Oracle.from_config(cfg)
+    o.setup()
+    o.set_state(st)
+    o.getnonlinear()
+    got = o.get_state()
+    for k, ex in (("rhsvn", ev), ("rhsomegayn", eg)):
+        assert rel_l2(split(got[k], k)[k], split(ex, k)[k]) < bar, k
+
+
+def test_largest_degree_oracle_accuracy(oracle_mod):
+    """At nnz = 250 the reference algorithm's nonlinear histories are only
+    ~1e-8 accurate (the derivative of the curl amplifies the products'
+    rounding), and the v operator is ill-conditioned (~3e9): the facts the GPU
+    parity bars at that degree rest on."""
+    from exact_lamb import nonlinear_histories
+    from parity import rel_l2, split
+    st = fields.reference_like_state(TALL, seed=3, epsilon=0.3, noise=0.02, gamma=5.0)
+    ev, eg = nonlinear_histories(TALL, st)
+    o = oracle_mod.Oracle.from_config(TALL)
+    o.setup()
+    o.set_state(st)
+    o.getnonlinear()
+    got = o.get_state()
+    ev_err = rel_l2(split(got["rhsvn"], "rhsvn")["rhsvn"], split(ev, "rhsvn")["rhsvn"])
+    eg_err = rel_l2(split(got["rhsomegayn"], "rhsomegayn")["rhsomegayn"], split(eg, "rhsomegayn")["rhsomegayn"])
+    assert 1e-9 < ev_err < 1e-6 and 1e-9 < eg_err < 1e-6, (ev_err, eg_err)
+    av, ae, xv, xe = o.matrices(17.0)
+    assert 1e9 < np.linalg.cond(av) < 1e10
+    assert np.linalg.cond(ae) < 100.0
+    assert np.linalg.norm(av @ xv - np.eye(av.shape[0])) < 1e-9
